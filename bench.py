@@ -1,0 +1,343 @@
+#!/usr/bin/env python3
+"""Benchmark: query x data-graph pairs per second of the batched engine on one GB300.
+
+One step = one full pass of the fused pipeline over the whole workload with
+inputs resident in HBM: signatures -> filter + 6 refinement steps -> GMCR ->
+join (count-all, EXACT semantics, bit-exact counts), i.e. bms_run.  The
+workload is mol100k: 100,000 seeded synthetic molecular data graphs (N(28, 9)
+atoms clipped to 10-60) x 600 queries of 5-30 nodes, 30% pure-carbon chains
+and rings — the shapes of the reference's plain-method GPU configuration.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--order learned|plain]
+  python bench.py --impl reference ...   # the CPU restatement of the reference
+
+With N > 1 (torchrun, one rank per GPU) every rank processes its own shard of
+data graphs (seeded by rank): weak scaling, no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = "mol100k"
+REFINE_STEPS = 6
+METRIC = "query x data-graph pairs/s (count-all, bit-exact counts)"
+HBM_FALLBACK_GBS = 6800.0
+
+
+def peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK_GBS, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.out = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.out,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.out.flush()
+        rows = [r.split(",") for r in Path(self.out.name).read_text().strip().splitlines() if r.strip()]
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() in ("active", "1"):
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_filter_bytes(qn: int, dn: int, R: int) -> float:
+    """Compulsory bytes of filter + refine: the Qn x Dn candidate bits written
+    once plus the node signatures read (label 1 + row offset 4 + path 32 +
+    cycle 8 bytes, and 8 bytes per refinement step) on both sides."""
+    return qn * dn / 8.0 + (dn + qn) * (45.0 + 8.0 * R)
+
+
+def cpu_baseline(q, d, threads: int, budget_s: float = 15.0) -> dict:
+    """The CPU restatement of the reference pipeline (OpenMP over nodes, words,
+    pairs) on a bounded sample: all queries x the first k data graphs."""
+    import oracle
+    from bms2_gb300 import Graphs
+
+    a = d.arrays()
+    Q = q.n_graphs
+    k = 256
+    t_one = None
+    while True:
+        sub = _head(a, k)
+        t0 = time.perf_counter()
+        res = oracle.run_pipeline(q, sub, REFINE_STEPS, threads=threads, keep_steps=False)
+        t = time.perf_counter() - t0
+        if t > budget_s / 4 or k >= len(a["graph_offsets"]) - 1:
+            t_one = t
+            break
+        k = min(k * 4, len(a["graph_offsets"]) - 1)
+    del Graphs
+    return {"value": Q * k / t_one, "unit": "pairs/s", "cores": threads, "kind": "port",
+            "sample": f"{Q} queries x first {k} of {len(a['graph_offsets']) - 1} data graphs, R={REFINE_STEPS}, "
+                      f"count-all, {t_one:.2f} s", "matches": int(res.total)}
+
+
+def _head(a: dict, k: int) -> dict:
+    go = a["graph_offsets"][: k + 1]
+    n = int(go[-1])
+    ro = a["row_offsets"][: n + 1]
+    e = int(ro[-1])
+    return {"graph_offsets": go.copy(), "row_offsets": ro.copy(), "column_indices": a["column_indices"][:e].copy(),
+            "node_labels": a["node_labels"][:n].copy(), "edge_labels": a["edge_labels"][:e].copy()}
+
+
+def train_cost_model(ctx, seed: int, n_data: int) -> dict:
+    """Seed-A plain-order run with vertex logging -> features + targets -> GPU training."""
+    from bms2_gb300 import COUNT_ALL, DATA, ORDER_GMCR, QUERY, SEM_EXACT, workloads
+    from bms2_gb300.train import collect, train
+
+    qa, da = workloads.make(WORKLOAD, seed, n_data=n_data)
+    ctx.load(QUERY, qa)
+    ctx.load(DATA, da)
+    x, y = collect(ctx, REFINE_STEPS)
+    loss = train(ctx, x, y, seed=seed)
+    del COUNT_ALL, ORDER_GMCR, SEM_EXACT
+    return {"train_samples": int(len(y)), "train_loss": float(loss), "train_seed": seed, "train_data_graphs": n_data}
+
+
+def run_ours(args) -> None:
+    import torch
+    import torch.distributed as dist
+
+    from bms2_gb300 import COUNT_ALL, DATA, ORDER_GMCR, ORDER_LEARNED, QUERY, SEM_EXACT, Context, workloads
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    ctx = Context(local)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    order = ORDER_LEARNED if args.order == "learned" else ORDER_GMCR
+    extra = {}
+    if order == ORDER_LEARNED:
+        extra.update(train_cost_model(ctx, seed=101, n_data=args.train_graphs))
+    # evaluation workload (seed B; each rank its own shard)
+    q, d = workloads.make(WORKLOAD, 202 + rank)
+    Q, D = q.n_graphs, d.n_graphs
+    qa, da = q.arrays(), d.arrays()
+    ctx.load(QUERY, q)
+    ctx.load(DATA, d)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+
+    def step():
+        return ctx.run(REFINE_STEPS, COUNT_ALL, order, SEM_EXACT)
+
+    for _ in range(args.warmup):
+        step()
+    plain_total = None
+    if order == ORDER_LEARNED:
+        plain_total = ctx.run(REFINE_STEPS, COUNT_ALL, ORDER_GMCR, SEM_EXACT)
+        plain_exp = ctx.stats()["expansions"]
+        plain_ms = ctx.stats()["ms_join"]
+    clocks = Clocks(local)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    clocks.start()
+    ms_steps, stage = [], []
+    total = None
+    launches = 0
+    for _ in range(args.steps):
+        flush.fill_(1)  # L2 flush between steps (outside the timed events)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        total = step()
+        e1.record(stream)
+        e1.synchronize()
+        ms_steps.append(e0.elapsed_time(e1))
+        st = ctx.stats()
+        stage.append(st)
+        launches += st["kernel_launches"]
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    t_total = float(np.sum(ms_steps)) / 1e3
+    if world > 1:
+        tt = torch.tensor([t_total], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_total = float(tt.item())
+    st = stage[-1]
+    # e2e: host buffers in, counts out, through the C ABI
+    pin = {k: torch.from_numpy(v).pin_memory() for k, v in da.items()}
+    qpin = {k: torch.from_numpy(v).pin_memory() for k, v in qa.items()}
+    T = st["n_valid_pairs"]
+    out = torch.empty(max(T, 1), dtype=torch.int64).pin_memory()
+    import ctypes
+
+    from bms2_gb300 import native
+
+    L = native.lib()
+    e2e_ms = []
+    h2d = sum(int(v.numel() * v.element_size()) for v in list(pin.values()) + list(qpin.values()))
+    for i in range(args.warmup + args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for kind, p in ((QUERY, qpin), (DATA, pin)):
+            ctx.load_csr_ptrs(kind, len(p["graph_offsets"]) - 1, p["graph_offsets"].data_ptr(),
+                              p["row_offsets"].data_ptr(), p["column_indices"].data_ptr(), p["node_labels"].data_ptr(),
+                              p["edge_labels"].data_ptr())
+        step()
+        native._check(L.bms_get_pair_counts(ctx.handle, ctypes.cast(out.data_ptr(), native._u64p), out.numel()),
+                      ctx.handle)
+        torch.cuda.synchronize(dev)
+        if i >= args.warmup:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_s = float(np.mean(e2e_ms)) / 1e3
+    pairs = Q * D
+    value = world * pairs * args.steps / t_total
+    peak, peak_kind = peaks()
+    fbytes = algorithmic_filter_bytes(st["n_query_nodes"], st["n_data_nodes"], REFINE_STEPS)
+    f_ms = float(np.mean([s["ms_filter"] for s in stage]))
+    achieved = fbytes / (f_ms / 1e3) / 1e9
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "pairs/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": t_total * 1e3 / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u64",
+        "data": "synthetic",
+        "config": {"workload": f"{WORKLOAD}: {D} data graphs x {Q} queries per GPU, refine steps {REFINE_STEPS}, "
+                               f"count-all, EXACT semantics, order {args.order}",
+                   "data_graphs_per_gpu": D, "queries": Q, "refine_steps": REFINE_STEPS, "order": args.order,
+                   "l2": "flushed between steps (512 MiB write outside the timed events)",
+                   "parallelism": f"data-graph shards x{world}"},
+        "e2e": {"value": world * pairs / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": int(T * 8)},
+        "roofline": {"kernel": "pair_filter (fused filter + refine + GMCR validity)", "bound": "hbm",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_kind": f"{peak_kind} hbm_gbs",
+                     "algorithmic_bytes": fbytes, "ms": f_ms, "equivalent": True},
+        "stage_ms": {k: float(np.mean([s[k] for s in stage])) for k in
+                     ("ms_signatures", "ms_filter", "ms_map", "ms_order", "ms_join", "ms_total")},
+        "clocks": clk,
+        "gpu_launches": int(launches),
+        "results": {"total_matches": int(total), "valid_pairs": int(T), "expansions": int(st["expansions"])},
+    }
+    if plain_total is not None:
+        line["results"]["plain_total_matches"] = int(plain_total)
+        line["results"]["counts_equal_plain"] = bool(plain_total == total)
+        line["results"]["plain_expansions"] = int(plain_exp)
+        line["results"]["expansion_ratio_plain_over_learned"] = float(plain_exp) / max(1, st["expansions"])
+        line["results"]["plain_join_ms"] = float(plain_ms)
+    line["results"].update(extra)
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(q, d, os.cpu_count() or 1, args.cpu_budget)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def run_reference(args) -> None:
+    """The reference's CPU path: its SYCL CPU build cannot be built here, so the
+    oracle (a C++ restatement of the reference kernels, OpenMP over all host
+    threads) runs on a bounded sample of the same workload."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from bms2_gb300 import workloads
+
+    q, d = workloads.make(WORKLOAD, 202)
+    threads = os.cpu_count() or 1
+    cb = None
+    vals = []
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(q, d, threads, budget_s=args.cpu_budget if i >= args.warmup else 4.0)
+        if i >= args.warmup:
+            vals.append(cb["value"])
+    v = float(np.mean(vals))
+    cb["value"] = v
+    line = {"metric": METRIC, "value": v, "unit": "pairs/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"{WORKLOAD}: {d.n_graphs} data graphs x {q.n_graphs} queries (bounded sample per "
+                                   f"step), refine steps {REFINE_STEPS}, count-all", "order": "plain"},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--order", choices=["learned", "plain"], default="plain")
+    ap.add_argument("--train-graphs", type=int, default=20000)
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    from bms2_gb300 import build
+
+    build.build()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,8 @@
+"""bms2_gb300 — GB300-native batched subgraph-isomorphism engine.
+
+The engine is libbms.so (C ABI in include/bms.h); this package holds its CUDA
+and C++ sources (csrc/), the build recipe (build.py), the seeded workload
+presets (workloads.py) and the ctypes binding (native.py).
+"""
+from .native import (COUNT_ALL, DATA, FIND_FIRST, ORDER_GMCR, ORDER_LEARNED, QUERY, SEM_EXACT,  # noqa: F401
+                     SEM_REFERENCE_DFS, BmsError, Context, Graphs, lib)

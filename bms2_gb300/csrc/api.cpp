@@ -1,0 +1,795 @@
+// C ABI of libbms: contexts, uploads, the staged and fused pipelines, results.
+// Every entry point catches everything: no exception crosses the boundary.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/bms.h"
+#include "graphs.h"
+#include "internal.h"
+
+using namespace bms;
+
+#include "ctx.h"
+
+namespace bms {
+
+int fail(bms_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  bms::set_thread_error(msg);
+  return code;
+}
+int fail_cuda(bms_ctx* c, cudaError_t e, const char* what) {
+  cudaGetLastError();
+  return fail(c, e == cudaErrorMemoryAllocation ? BMS_ENOMEM : BMS_ECUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+}  // namespace bms
+
+namespace {
+
+int check_side_errors(bms_ctx* c, const char* side, uint32_t e) {
+  if (e & kErrRows) return fail(c, BMS_EINVAL, std::string(side) + ": row offsets decrease or exceed the entry count");
+  if (e & kErrColumn) return fail(c, BMS_EINVAL, std::string(side) + ": a column id lies outside its graph");
+  if (e & kErrTooLarge) return fail(c, BMS_EUNSUPPORTED, std::string(side) + ": a graph exceeds the node limit");
+  return BMS_OK;
+}
+
+int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const char* name) {
+  if (v.n_graphs && !v.graph_offsets) return fail(c, BMS_EINVAL, "graph_offsets is null");
+  const uint32_t G = v.n_graphs;
+  if (G && v.graph_offsets[0] != 0) return fail(c, BMS_EINVAL, "graph_offsets[0] must be 0");
+  uint32_t mx = 0;
+  for (uint32_t i = 0; i < G; ++i) {
+    if (v.graph_offsets[i + 1] < v.graph_offsets[i]) return fail(c, BMS_EINVAL, "graph_offsets must be non-decreasing");
+    mx = std::max(mx, v.graph_offsets[i + 1] - v.graph_offsets[i]);
+  }
+  if (mx > limit)
+    return fail(c, BMS_EUNSUPPORTED,
+                std::string(name) + " graph with " + std::to_string(mx) + " nodes exceeds the limit of " + std::to_string(limit));
+  const uint64_t N = G ? v.graph_offsets[G] : 0;
+  if (N && (!v.row_offsets || !v.node_labels)) return fail(c, BMS_EINVAL, "row_offsets or node_labels is null");
+  const uint64_t E = N ? v.row_offsets[N] : 0;
+  if (N && v.row_offsets[0] != 0) return fail(c, BMS_EINVAL, "row_offsets[0] must be 0");
+  if (E && !v.column_indices) return fail(c, BMS_EINVAL, "column_indices is null");
+  s.loaded = false;
+  s.sig_steps = -1;
+  s.G = G;
+  s.N = N;
+  s.E = E;
+  s.max_nodes = mx;
+  s.h_goff.assign(v.graph_offsets, v.graph_offsets + G + 1);
+  if (!G) s.h_goff.assign(1, 0);
+  CK(s.goff.ensure(sizeof(uint32_t) * (G + 1)));
+  CK(s.rowp.ensure(sizeof(uint32_t) * (N + 1)));
+  CK(s.col.ensure(sizeof(uint32_t) * (E ? E : 1)));
+  CK(s.lab.ensure(N ? N : 1));
+  CK(s.elab.ensure(E ? E : 1));
+  CK(cudaMemcpyAsync(s.goff.p, s.h_goff.data(), sizeof(uint32_t) * (G + 1), cudaMemcpyHostToDevice, c->st));
+  if (N) {
+    CK(cudaMemcpyAsync(s.rowp.p, v.row_offsets, sizeof(uint32_t) * (N + 1), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(s.lab.p, v.node_labels, N, cudaMemcpyHostToDevice, c->st));
+  } else {
+    CK(cudaMemsetAsync(s.rowp.p, 0, sizeof(uint32_t), c->st));
+  }
+  if (E) {
+    CK(cudaMemcpyAsync(s.col.p, v.column_indices, sizeof(uint32_t) * E, cudaMemcpyHostToDevice, c->st));
+    if (v.edge_labels) CK(cudaMemcpyAsync(s.elab.p, v.edge_labels, E, cudaMemcpyHostToDevice, c->st));
+    else CK(cudaMemsetAsync(s.elab.p, 0, E, c->st));
+  }
+  CK(s.frec.ensure(sizeof(uint64_t) * kRecWords * (N ? N : 1)));
+  CK(s.adj.ensure(sizeof(uint64_t) * 2 * (N ? N : 1)));
+  CK(s.ghist.ensure(sizeof(uint64_t) * (G ? G : 1)));
+  CK(s.glabset.ensure(sizeof(uint32_t) * (G ? G : 1)));
+  s.loaded = true;
+  return BMS_OK;
+}
+
+void invalidate_downstream(bms_ctx* c) {
+  c->have_cand = false;
+  c->mapped = false;
+  c->have_qidx = false;
+  c->have_results = false;
+  c->have_vexp = false;
+}
+
+// data graphs grouped by size class: <= 32, <= 64, <= 128 nodes
+int build_classes(bms_ctx* c) {
+  std::vector<uint32_t> perm;
+  perm.reserve(c->d.G);
+  const uint32_t bounds[3] = {32, 64, 128};
+  uint32_t lo = 0;
+  for (int k = 2; k >= 0; --k) {  // largest graphs first: they carry the most work
+    const uint32_t hi = bounds[k], lo_k = k ? bounds[k - 1] : 0;
+    c->class_begin[k] = uint32_t(perm.size());
+    for (uint32_t g = 0; g < c->d.G; ++g) {
+      const uint32_t m = c->d.h_goff[g + 1] - c->d.h_goff[g];
+      if (m > lo_k && m <= hi) perm.push_back(g);
+      if (k == 0 && m == 0) perm.push_back(g);
+    }
+    c->class_end[k] = uint32_t(perm.size());
+  }
+  (void)lo;
+  CK(c->dperm.ensure(sizeof(uint32_t) * (perm.size() ? perm.size() : 1)));
+  if (!perm.empty())
+    CK(cudaMemcpyAsync(c->dperm.p, perm.data(), sizeof(uint32_t) * perm.size(), cudaMemcpyHostToDevice, c->st));
+  return BMS_OK;
+}
+
+int run_signatures(bms_ctx* c, int R) {
+  CK(cudaMemsetAsync(c->errflag.p, 0, 4 * sizeof(uint32_t), c->st));
+  Side* sides[2] = {&c->d, &c->q};
+  for (int i = 0; i < 2; ++i) {
+    Side& s = *sides[i];
+    s.sig_steps = R;
+    CK(launch_signatures(s.dg(), s.ds(), i == 0 ? kMaxDataNodes : kMaxQueryNodes, c->errflag.as<uint32_t>() + i, c->st));
+  }
+  return BMS_OK;
+}
+
+int read_side_errors(bms_ctx* c) {
+  CK(cudaMemcpyAsync(c->h_err, c->errflag.p, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->d.asymmetric = (c->h_err[0] & kErrAsym) != 0;
+  c->q.asymmetric = (c->h_err[1] & kErrAsym) != 0;
+  int r = check_side_errors(c, "data", c->h_err[0]);
+  if (r) {
+    c->d.sig_steps = -1;
+    return r;
+  }
+  r = check_side_errors(c, "query", c->h_err[1]);
+  if (r) {
+    c->q.sig_steps = -1;
+    return r;
+  }
+  return BMS_OK;
+}
+
+int ensure_join_buffers(bms_ctx* c) {
+  CK(c->recs.ensure(sizeof(PairRec) * (c->rec_cap ? c->rec_cap : 1)));
+  CK(c->arena.ensure(sizeof(uint64_t) * 2 * (c->row_cap ? c->row_cap : 1)));
+  CK(c->tasks.ensure(sizeof(Task) * (c->task_cap ? c->task_cap : 1)));
+  CK(c->pair_count.ensure(sizeof(unsigned long long) * (c->rec_cap ? c->rec_cap : 1)));
+  CK(c->pair_exp.ensure(sizeof(unsigned long long) * (c->rec_cap ? c->rec_cap : 1)));
+  CK(c->pair_flag.ensure(sizeof(uint32_t) * (c->rec_cap ? c->rec_cap : 1)));
+  return BMS_OK;
+}
+
+DOrder order_of(bms_ctx* c) { return DOrder{c->perm.as<uint8_t>(), c->dadj.as<uint64_t>()}; }
+
+// Order, tasks, join and totals over the records already in place.
+int join_records(bms_ctx* c, int mode, int order, int sem, bool log_vertices) {
+  const uint64_t Qslots = uint64_t(c->q.G ? c->q.G : 1) * kMaxQueryNodes;
+  CK(c->perm.ensure(Qslots));
+  CK(c->dadj.ensure(sizeof(uint64_t) * Qslots));
+  if (order == BMS_ORDER_LEARNED) {
+    int r = learned_order(c);
+    if (r) return r;
+  } else {
+    CK(launch_plain_order(c->q.dg(), order_of(c), c->st));
+  }
+  CK(launch_order_adjacency(c->q.dg(), c->q.ds(), order_of(c), c->st));
+  CK(cudaEventRecord(c->ev[EV_ORDER], c->st));
+  CK(cudaMemsetAsync(c->pair_count.p, 0, sizeof(unsigned long long) * c->rec_cap, c->st));
+  CK(cudaMemsetAsync(c->pair_exp.p, 0, sizeof(unsigned long long) * c->rec_cap, c->st));
+  CK(cudaMemsetAsync(c->pair_flag.p, 0, sizeof(uint32_t) * c->rec_cap, c->st));
+  Counters* ctr = c->ctr.as<Counters>();
+  CK(launch_task_emit(c->recs.as<PairRec>(), c->rec_cap, c->q.dg(), order_of(c), c->arena.as<uint64_t>(),
+                      c->tasks.as<Task>(), c->task_cap, ctr, c->errflag.as<uint32_t>() + 2, c->st));
+  if (log_vertices) {
+    CK(c->vertex_exp.ensure(sizeof(unsigned long long) * (c->q.N ? c->q.N : 1)));
+    CK(cudaMemsetAsync(c->vertex_exp.p, 0, sizeof(unsigned long long) * (c->q.N ? c->q.N : 1), c->st));
+  }
+  JoinArgs ja{};
+  ja.q = c->q.dg();
+  ja.d = c->d.dg();
+  ja.ds = c->d.ds();
+  ja.o = order_of(c);
+  ja.recs = c->recs.as<PairRec>();
+  ja.arena = c->arena.as<uint64_t>();
+  ja.tasks = c->tasks.as<Task>();
+  ja.task_cap = c->task_cap;
+  ja.ctr = ctr;
+  ja.pair_count = c->pair_count.as<unsigned long long>();
+  ja.pair_exp = c->pair_exp.as<unsigned long long>();
+  ja.pair_flag = c->pair_flag.as<uint32_t>();
+  ja.vertex_exp = log_vertices ? c->vertex_exp.as<unsigned long long>() : nullptr;
+  ja.budget = c->budget;
+  ja.find_first = mode == BMS_FIND_FIRST;
+  ja.literal = sem == BMS_SEM_REFERENCE_DFS;
+  ja.steps = c->join_steps;
+  const int bucket = 0;
+  const int bps = c->sched.blocks_per_sm[bucket] ? int(c->sched.blocks_per_sm[bucket]) : 4;
+  const int wpb = c->sched.warps_per_block[bucket] ? int(c->sched.warps_per_block[bucket]) : 8;
+  CK(launch_join(ja, sm_count() * bps, wpb * 32, c->st));
+  CK(cudaEventRecord(c->ev[EV_JOIN], c->st));
+  CK(launch_totals(ctr, c->rec_cap, ja.pair_count, ja.pair_exp, ja.pair_flag, ja.find_first, ctr, c->st));
+  c->last_mode = mode;
+  c->last_order = order;
+  c->last_sem = sem;
+  return BMS_OK;
+}
+
+int finish_run(bms_ctx* c, uint64_t* total) {
+  CK(cudaEventRecord(c->ev[EV_END], c->st));
+  CK(cudaMemcpyAsync(c->h_ctr, c->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(c->h_err, c->errflag.p, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(c->h_T, c->gmcr_off.as<uint32_t>() + c->d.G, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return BMS_OK;
+  (void)total;
+}
+
+float elapsed(bms_ctx* c, Ev a, Ev b) {
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, c->ev[a], c->ev[b]) != cudaSuccess) {
+    cudaGetLastError();
+    return 0.f;
+  }
+  return ms;
+}
+
+int validate_modes(bms_ctx* c, int mode, int order, int sem) {
+  if (mode != BMS_FIND_FIRST && mode != BMS_COUNT_ALL) return fail(c, BMS_EINVAL, "invalid mode");
+  if (order != BMS_ORDER_GMCR && order != BMS_ORDER_LEARNED) return fail(c, BMS_EINVAL, "invalid order");
+  if (sem != BMS_SEM_EXACT && sem != BMS_SEM_REFERENCE_DFS) return fail(c, BMS_EINVAL, "invalid semantics");
+  if (sem == BMS_SEM_REFERENCE_DFS && order != BMS_ORDER_GMCR)
+    return fail(c, BMS_EINVAL, "REFERENCE_DFS semantics require the GMCR order");
+  if (order == BMS_ORDER_LEARNED && (c->q.asymmetric || c->d.asymmetric))
+    return fail(c, BMS_EINVAL, "the learned order requires symmetric adjacency");
+  return BMS_OK;
+}
+
+int run_fused(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total, bool log_vertices, int attempt);
+
+}  // namespace
+
+extern "C" {
+
+const char* bms_last_error(const void* ctx) {
+  if (!ctx) return bms::thread_error();
+  return static_cast<const bms_ctx*>(ctx)->err.c_str();
+}
+
+int bms_create(int device, bms_ctx** out) {
+  if (!out) return fail(nullptr, BMS_EINVAL, "out is null");
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) {
+    cudaGetLastError();
+    return fail(nullptr, BMS_ENODEV, "no CUDA device");
+  }
+  if (device < 0 || device >= n) return fail(nullptr, BMS_ENODEV, "device index out of range");
+  bms_ctx* c = new (std::nothrow) bms_ctx();
+  if (!c) return fail(nullptr, BMS_ENOMEM, "out of host memory");
+  c->device = device;
+  auto bad = [&](cudaError_t e, const char* w) {
+    int r = fail_cuda(c, e, w);
+    bms_destroy(c);
+    return r;
+  };
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return bad(e, "cudaSetDevice");
+  e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return bad(e, "cudaStreamCreate");
+  c->st = c->own;
+  for (int i = 0; i < EV_COUNT; ++i) {
+    e = cudaEventCreate(&c->ev[i]);
+    if (e != cudaSuccess) return bad(e, "cudaEventCreate");
+  }
+  if ((e = c->errflag.ensure(4 * sizeof(uint32_t))) != cudaSuccess) return bad(e, "alloc");
+  if ((e = c->ctr.ensure(sizeof(Counters))) != cudaSuccess) return bad(e, "alloc");
+  if ((e = cudaMallocHost(&c->h_err, 4 * sizeof(uint32_t))) != cudaSuccess) return bad(e, "cudaMallocHost");
+  if ((e = cudaMallocHost(&c->h_ctr, sizeof(Counters))) != cudaSuccess) return bad(e, "cudaMallocHost");
+  if ((e = cudaMallocHost(&c->h_T, sizeof(uint32_t))) != cudaSuccess) return bad(e, "cudaMallocHost");
+  std::memset(c->h_ctr, 0, sizeof(Counters));
+  *c->h_T = 0;
+  const uint32_t bounds[BMS_SCHED_BUCKETS] = {8, 16, 32, 64};
+  for (int i = 0; i < BMS_SCHED_BUCKETS; ++i) {
+    c->sched.max_query_nodes[i] = bounds[i];
+    c->sched.split_depth[i] = 1;
+    c->sched.blocks_per_sm[i] = 4;
+    c->sched.warps_per_block[i] = 8;
+  }
+  *out = c;
+  return BMS_OK;
+}
+
+void bms_destroy(bms_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->st) cudaStreamSynchronize(c->st);
+  for (int i = 0; i < EV_COUNT; ++i)
+    if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+  if (c->h_err) cudaFreeHost(c->h_err);
+  if (c->h_ctr) cudaFreeHost(c->h_ctr);
+  if (c->h_T) cudaFreeHost(c->h_T);
+  cudaStream_t own = c->own;
+  delete c;  // DevBuf destructors free device memory
+  if (own) cudaStreamDestroy(own);
+  cudaGetLastError();
+}
+
+int bms_set_stream(bms_ctx* c, void* stream) {
+  GUARD(c);
+  CK(cudaStreamSynchronize(c->st));
+  c->st = stream ? static_cast<cudaStream_t>(stream) : c->own;
+  return BMS_OK;
+}
+
+int bms_set_expansion_budget(bms_ctx* c, uint64_t budget) {
+  GUARD(c);
+  c->budget = budget;
+  return BMS_OK;
+}
+
+int bms_set_logging(bms_ctx* c, int vertex_expansions) {
+  GUARD(c);
+  c->log_vertices = vertex_expansions != 0;
+  return BMS_OK;
+}
+
+int bms_load_graphs(bms_ctx* c, int kind, const bms_graphs* g) {
+  GUARD(c);
+  if (!g) return fail(c, BMS_EINVAL, "graphs is null");
+  bms_graphs_view v;
+  bms_graphs_view_of(g, &v);
+  if (kind != BMS_QUERY && kind != BMS_DATA) return fail(c, BMS_EINVAL, "invalid kind");
+  invalidate_downstream(c);
+  Side& s = kind == BMS_QUERY ? c->q : c->d;
+  int r = upload(c, s, v, kind == BMS_QUERY ? kMaxQueryNodes : kMaxDataNodes, kind == BMS_QUERY ? "query" : "data");
+  if (r) return r;
+  if (kind == BMS_DATA) return build_classes(c);
+  return BMS_OK;
+}
+
+int bms_load_csr(bms_ctx* c, int kind, uint32_t n_graphs, const uint32_t* goff, const uint32_t* rowp,
+                 const uint32_t* col, const uint8_t* lab, const uint8_t* elab) {
+  GUARD(c);
+  if (kind != BMS_QUERY && kind != BMS_DATA) return fail(c, BMS_EINVAL, "invalid kind");
+  if (!goff) return fail(c, BMS_EINVAL, "graph_offsets is null");
+  bms_graphs_view v{};
+  v.n_graphs = n_graphs;
+  v.graph_offsets = goff;
+  v.row_offsets = rowp;
+  v.column_indices = col;
+  v.node_labels = lab;
+  v.edge_labels = elab;
+  invalidate_downstream(c);
+  Side& s = kind == BMS_QUERY ? c->q : c->d;
+  int r = upload(c, s, v, kind == BMS_QUERY ? kMaxQueryNodes : kMaxDataNodes, kind == BMS_QUERY ? "query" : "data");
+  if (r) return r;
+  if (kind == BMS_DATA) return build_classes(c);
+  return BMS_OK;
+}
+
+int bms_signatures(bms_ctx* c, int R) {
+  GUARD(c);
+  if (!c->q.loaded || !c->d.loaded) return fail(c, BMS_ESTATE, "load query and data graphs first");
+  if (R < 0 || R > BMS_MAX_REFINE_STEPS) return fail(c, BMS_EINVAL, "refine_steps must be in [0, 8]");
+  invalidate_downstream(c);
+  CK(cudaEventRecord(c->ev[EV_START], c->st));
+  int r = run_signatures(c, R);
+  if (r) return r;
+  CK(cudaEventRecord(c->ev[EV_SIG], c->st));
+  r = read_side_errors(c);
+  if (r) return r;
+  c->stats.ms_signatures = elapsed(c, EV_START, EV_SIG);
+  c->stats.refine_steps = uint32_t(R);
+  return BMS_OK;
+}
+
+int bms_filter(bms_ctx* c) {
+  GUARD(c);
+  if (c->q.sig_steps < 0 || c->d.sig_steps < 0) return fail(c, BMS_ESTATE, "compute signatures first");
+  c->W = (c->d.N + 31) / 32;
+  const uint64_t words = c->q.N * c->W;
+  CK(c->cand.ensure(sizeof(uint32_t) * (words ? words : 1)));
+  if (words) CK(cudaMemsetAsync(c->cand.p, 0, sizeof(uint32_t) * words, c->st));
+  CK(cudaEventRecord(c->ev[EV_SIG], c->st));
+  CK(launch_filter_dense(c->q.dg(), c->q.ds(), c->d.dg(), c->d.ds(), c->cand.as<uint32_t>(), c->W, c->st));
+  CK(cudaEventRecord(c->ev[EV_FILTER], c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->stats.ms_filter = elapsed(c, EV_SIG, EV_FILTER);
+  c->have_cand = true;
+  c->mapped = c->have_qidx = c->have_results = false;
+  return BMS_OK;
+}
+
+int bms_refine(bms_ctx* c, int step) {
+  GUARD(c);
+  if (!c->have_cand) return fail(c, BMS_ESTATE, "run bms_filter first");
+  if (step < 1 || step > c->q.sig_steps || step > c->d.sig_steps)
+    return fail(c, BMS_EINVAL, "step must be in [1, refine_steps of bms_signatures]");
+  CK(cudaEventRecord(c->ev[EV_SIG], c->st));
+  CK(launch_refine_dense(c->q.ds(), c->q.N, c->d.ds(), c->d.N, step, c->cand.as<uint32_t>(), c->W, c->st));
+  CK(cudaEventRecord(c->ev[EV_FILTER], c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->stats.ms_refine = elapsed(c, EV_SIG, EV_FILTER);
+  c->mapped = c->have_qidx = c->have_results = false;
+  return BMS_OK;
+}
+
+int bms_map(bms_ctx* c, uint64_t* n_pairs) {
+  GUARD(c);
+  if (!c->have_cand) return fail(c, BMS_ESTATE, "run bms_filter first");
+  const uint32_t D = c->d.G;
+  c->QW = (c->q.G + 31) / 32;
+  CK(c->valid.ensure(sizeof(uint32_t) * (uint64_t(D) * c->QW + 1)));
+  CK(c->vcounts.ensure(sizeof(uint32_t) * (D + 1)));
+  CK(c->gmcr_off.ensure(sizeof(uint32_t) * (D + 1)));
+  CK(c->scan_scratch.ensure(sizeof(uint32_t) * scan_scratch_words(D)));
+  CK(cudaEventRecord(c->ev[EV_FILTER], c->st));
+  CK(launch_gmcr_dense(c->q.dg(), c->d.dg(), c->cand.as<uint32_t>(), c->W, c->valid.as<uint32_t>(), c->QW,
+                       c->vcounts.as<uint32_t>(), c->st));
+  CK(launch_scan_u32(c->vcounts.as<uint32_t>(), c->gmcr_off.as<uint32_t>(), D, c->scan_scratch.as<uint32_t>(), c->st));
+  CK(cudaMemcpyAsync(c->h_T, c->gmcr_off.as<uint32_t>() + D, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->T = *c->h_T;
+  CK(c->qidx.ensure(sizeof(uint32_t) * (c->T ? c->T : 1)));
+  CK(launch_gmcr_indices(c->valid.as<uint32_t>(), c->QW, c->q.G, D, c->gmcr_off.as<uint32_t>(), c->qidx.as<uint32_t>(), c->st));
+  CK(cudaEventRecord(c->ev[EV_MAP], c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->stats.ms_map = elapsed(c, EV_FILTER, EV_MAP);
+  c->mapped = true;
+  c->have_qidx = true;
+  c->have_results = false;
+  c->stats.n_valid_pairs = c->T;
+  if (n_pairs) *n_pairs = c->T;
+  return BMS_OK;
+}
+
+int bms_join(bms_ctx* c, int mode, int order, int sem, uint64_t* total) {
+  GUARD(c);
+  if (!c->mapped) return fail(c, BMS_ESTATE, "run bms_map first");
+  int r = validate_modes(c, mode, order, sem);
+  if (r) return r;
+  const uint64_t T = c->T;
+  // one record per GMCR pair, candidate rows gathered from the dense matrix
+  CK(c->pair_nodes.ensure(sizeof(uint32_t) * (T + 1)));
+  CK(c->row_off.ensure(sizeof(uint32_t) * (T + 1)));
+  CK(c->tmp.ensure(sizeof(uint32_t) * scan_scratch_words(T)));
+  CK(launch_pair_nodes(c->q.dg(), c->qidx.as<uint32_t>(), T, c->pair_nodes.as<uint32_t>(), c->st));
+  CK(launch_scan_u32(c->pair_nodes.as<uint32_t>(), c->row_off.as<uint32_t>(), T, c->tmp.as<uint32_t>(), c->st));
+  uint32_t rows = 0;
+  CK(cudaMemcpyAsync(c->h_T, c->row_off.as<uint32_t>() + T, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  rows = *c->h_T;
+  c->rec_cap = std::max<uint64_t>(T, 1);
+  c->row_cap = std::max<uint64_t>(rows, 1);
+  c->task_cap = std::max<uint64_t>(uint64_t(rows) * 2, 1024);
+  // tasks <= roots <= 128 per record; grown below if the first attempt overflows
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    r = ensure_join_buffers(c);
+    if (r) return r;
+    CK(cudaMemsetAsync(c->ctr.p, 0, sizeof(Counters), c->st));
+    CK(cudaMemsetAsync(c->errflag.as<uint32_t>() + 2, 0, sizeof(uint32_t), c->st));
+    CK(cudaEventRecord(c->ev[EV_MAP], c->st));
+    CK(launch_gather_pairs(c->q.dg(), c->d.dg(), c->cand.as<uint32_t>(), c->W, c->gmcr_off.as<uint32_t>(),
+                           c->qidx.as<uint32_t>(), c->row_off.as<uint32_t>(), c->recs.as<PairRec>(),
+                           c->arena.as<uint64_t>(), c->st));
+    CK(launch_set_counter(&c->ctr.as<Counters>()->recs, T, c->st));
+    r = join_records(c, mode, order, sem, mode == BMS_COUNT_ALL && order == BMS_ORDER_GMCR && sem == BMS_SEM_EXACT);
+    if (r) return r;
+    CK(cudaMemcpyAsync(c->h_T, c->gmcr_off.as<uint32_t>() + c->d.G, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->st));
+    r = finish_run(c, total);
+    if (r) return r;
+    if (!(c->h_err[2] & kErrOverflow)) break;
+    c->task_cap = std::max<uint64_t>(c->h_ctr->tasks + 1, c->task_cap * 2);
+  }
+  if (c->h_err[2] & kErrOverflow) return fail(c, BMS_ENOMEM, "join task buffer overflow");
+  c->have_results = true;
+  c->have_vexp = mode == BMS_COUNT_ALL && order == BMS_ORDER_GMCR && sem == BMS_SEM_EXACT;
+  c->stats.ms_order = elapsed(c, EV_MAP, EV_ORDER);
+  c->stats.ms_join = elapsed(c, EV_ORDER, EV_JOIN);
+  c->stats.total_matches = c->h_ctr->total;
+  c->stats.expansions = c->h_ctr->expansions;
+  c->stats.n_incomplete = c->h_ctr->incomplete;
+  if (total) *total = c->h_ctr->total;
+  return c->h_ctr->incomplete ? fail(c, BMS_EINCOMPLETE, "some pairs hit the expansion budget") : BMS_OK;
+}
+
+int bms_run(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total) {
+  GUARD(c);
+  try {
+    const bool log = c->log_vertices && mode == BMS_COUNT_ALL && order == BMS_ORDER_GMCR && sem == BMS_SEM_EXACT;
+    return run_fused(c, R, mode, order, sem, total, log, 0);
+  } catch (...) {
+    return fail(c, BMS_ENOMEM, "host exception in bms_run");
+  }
+}
+
+}  // extern "C"
+
+namespace {
+
+int run_fused(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total, bool log_vertices, int attempt) {
+  if (!c->q.loaded || !c->d.loaded) return fail(c, BMS_ESTATE, "load query and data graphs first");
+  const unsigned long long launches0 = g_launches;
+  if (R < 0 || R > BMS_MAX_REFINE_STEPS) return fail(c, BMS_EINVAL, "refine_steps must be in [0, 8]");
+  int r = validate_modes(c, mode, order, sem);
+  if (r) return r;
+  invalidate_downstream(c);
+  const uint32_t D = c->d.G, Q = c->q.G;
+  c->QW = (Q + 31) / 32;
+  CK(c->valid.ensure(sizeof(uint32_t) * (uint64_t(D) * c->QW + 1)));
+  CK(c->vcounts.ensure(sizeof(uint32_t) * (D + 1)));
+  CK(c->gmcr_off.ensure(sizeof(uint32_t) * (D + 1)));
+  CK(c->scan_scratch.ensure(sizeof(uint32_t) * scan_scratch_words(D)));
+  CK(c->filter_order.ensure(uint64_t(Q ? Q : 1) * kMaxQueryNodes));
+  CK(c->label_count.ensure(256 * sizeof(unsigned long long)));
+  if (c->rec_cap == 0) {
+    c->rec_cap = std::max<uint64_t>(1 << 16, std::min<uint64_t>(uint64_t(Q) * D, uint64_t(1) << 22));
+    c->row_cap = c->rec_cap * 24;
+    c->task_cap = c->rec_cap * 8;
+  }
+  r = ensure_join_buffers(c);
+  if (r) return r;
+  const bool learned = order == BMS_ORDER_LEARNED;
+  if (learned) {
+    CK(c->cand_sum.ensure(sizeof(unsigned int) * (c->q.N ? c->q.N : 1)));
+    CK(cudaMemsetAsync(c->cand_sum.p, 0, sizeof(unsigned int) * (c->q.N ? c->q.N : 1), c->st));
+  }
+  CK(cudaMemsetAsync(c->ctr.p, 0, sizeof(Counters), c->st));
+  CK(cudaEventRecord(c->ev[EV_START], c->st));
+  r = run_signatures(c, R);
+  if (r) return r;
+  CK(launch_label_count(c->d.dg(), c->label_count.as<unsigned long long>(), c->st));
+  CK(launch_query_prep(c->q.dg(), c->q.ds(), c->label_count.as<unsigned long long>(), c->filter_order.as<uint8_t>(), c->st));
+  CK(cudaEventRecord(c->ev[EV_SIG], c->st));
+  PairFilterArgs pa{};
+  pa.q = c->q.dg();
+  pa.d = c->d.dg();
+  pa.qs = c->q.ds();
+  pa.ds = c->d.ds();
+  pa.filter_order = c->filter_order.as<uint8_t>();
+  pa.dperm = c->dperm.as<uint32_t>();
+  pa.valid = c->valid.as<uint32_t>();
+  pa.QW = c->QW;
+  pa.vcounts = c->vcounts.as<uint32_t>();
+  pa.recs = c->recs.as<PairRec>();
+  pa.rec_cap = c->rec_cap;
+  pa.arena = c->arena.as<uint64_t>();
+  pa.row_cap = c->row_cap;
+  pa.ctr = c->ctr.as<Counters>();
+  pa.err = c->errflag.as<uint32_t>() + 2;
+  pa.skip_by_labels = sem == BMS_SEM_EXACT;
+  pa.cand_sum = learned ? c->cand_sum.as<unsigned int>() : nullptr;
+  const int rounds[3] = {1, 2, 4};
+  for (int k = 2; k >= 0; --k) {
+    pa.class_begin = c->class_begin[k];
+    pa.class_end = c->class_end[k];
+    pa.class_id = k;
+    CK(launch_pair_filter(pa, rounds[k], c->st));
+  }
+  CK(cudaEventRecord(c->ev[EV_FILTER], c->st));
+  CK(launch_scan_u32(c->vcounts.as<uint32_t>(), c->gmcr_off.as<uint32_t>(), D, c->scan_scratch.as<uint32_t>(), c->st));
+  CK(launch_pair_positions(c->recs.as<PairRec>(), c->ctr.as<Counters>(), c->rec_cap, c->valid.as<uint32_t>(), c->QW,
+                           c->gmcr_off.as<uint32_t>(), c->st));
+  CK(cudaEventRecord(c->ev[EV_MAP], c->st));
+  r = join_records(c, mode, order, sem, log_vertices);
+  if (r) return r;
+  r = finish_run(c, total);
+  if (r) return r;
+  r = check_side_errors(c, "data", c->h_err[0]);
+  if (r) {
+    c->d.sig_steps = -1;
+    return r;
+  }
+  r = check_side_errors(c, "query", c->h_err[1]);
+  if (r) {
+    c->q.sig_steps = -1;
+    return r;
+  }
+  c->d.asymmetric = (c->h_err[0] & kErrAsym) != 0;
+  c->q.asymmetric = (c->h_err[1] & kErrAsym) != 0;
+  if (order == BMS_ORDER_LEARNED && (c->d.asymmetric || c->q.asymmetric))
+    return fail(c, BMS_EINVAL, "the learned order requires symmetric adjacency");
+  if (c->h_err[2] & kErrOverflow) {
+    if (attempt >= 2) return fail(c, BMS_ENOMEM, "result buffers overflow");
+    const Counters& h = *c->h_ctr;
+    c->rec_cap = std::max<uint64_t>(c->rec_cap, h.recs + h.recs / 8 + 1024);
+    c->row_cap = std::max<uint64_t>(c->row_cap, h.rows + h.rows / 8 + 16384);
+    c->task_cap = std::max<uint64_t>(c->task_cap, h.tasks + h.tasks / 8 + 16384);
+    if (h.recs <= c->rec_cap && h.rows <= c->row_cap && h.tasks < c->task_cap / 2) c->task_cap *= 2;
+    return run_fused(c, R, mode, order, sem, total, log_vertices, attempt + 1);
+  }
+  c->T = *c->h_T;
+  c->mapped = true;
+  c->have_qidx = false;
+  c->have_results = true;
+  c->have_vexp = log_vertices;
+  c->stats.refine_steps = uint32_t(R);
+  c->stats.ms_signatures = elapsed(c, EV_START, EV_SIG);
+  c->stats.ms_filter = elapsed(c, EV_SIG, EV_FILTER);
+  c->stats.ms_refine = 0.f;
+  c->stats.ms_map = elapsed(c, EV_FILTER, EV_MAP);
+  c->stats.kernel_launches = g_launches - launches0;
+  c->stats.ms_order = elapsed(c, EV_MAP, EV_ORDER);
+  c->stats.ms_join = elapsed(c, EV_ORDER, EV_JOIN);
+  c->stats.ms_total = elapsed(c, EV_START, EV_END);
+  c->stats.n_valid_pairs = c->T;
+  c->stats.total_matches = c->h_ctr->total;
+  c->stats.expansions = c->h_ctr->expansions;
+  c->stats.n_incomplete = c->h_ctr->incomplete;
+  if (total) *total = c->h_ctr->total;
+  return c->h_ctr->incomplete ? fail(c, BMS_EINCOMPLETE, "some pairs hit the expansion budget") : BMS_OK;
+}
+
+}  // namespace
+
+int bms::rejoin_timed(bms_ctx* c, int bps, int wpb, int steps, float* ms) {
+  if (!c->have_results) return fail(c, BMS_ESTATE, "run the pipeline first");
+  Counters* ctr = c->ctr.as<Counters>();
+  CK(cudaMemsetAsync(&ctr->task_fetch, 0, sizeof(unsigned long long), c->st));
+  CK(cudaMemsetAsync(c->pair_count.p, 0, sizeof(unsigned long long) * c->rec_cap, c->st));
+  CK(cudaMemsetAsync(c->pair_exp.p, 0, sizeof(unsigned long long) * c->rec_cap, c->st));
+  CK(cudaMemsetAsync(c->pair_flag.p, 0, sizeof(uint32_t) * c->rec_cap, c->st));
+  JoinArgs ja{};
+  ja.q = c->q.dg();
+  ja.d = c->d.dg();
+  ja.ds = c->d.ds();
+  ja.o = order_of(c);
+  ja.recs = c->recs.as<PairRec>();
+  ja.arena = c->arena.as<uint64_t>();
+  ja.tasks = c->tasks.as<Task>();
+  ja.task_cap = c->task_cap;
+  ja.ctr = ctr;
+  ja.pair_count = c->pair_count.as<unsigned long long>();
+  ja.pair_exp = c->pair_exp.as<unsigned long long>();
+  ja.pair_flag = c->pair_flag.as<uint32_t>();
+  ja.budget = c->budget;
+  ja.find_first = c->last_mode == BMS_FIND_FIRST;
+  ja.literal = c->last_sem == BMS_SEM_REFERENCE_DFS;
+  ja.steps = steps;
+  CK(cudaEventRecord(c->ev[EV_ORDER], c->st));
+  CK(launch_join(ja, sm_count() * bps, wpb * 32, c->st));
+  CK(cudaEventRecord(c->ev[EV_JOIN], c->st));
+  CK(cudaEventSynchronize(c->ev[EV_JOIN]));
+  *ms = elapsed(c, EV_ORDER, EV_JOIN);
+  return BMS_OK;
+}
+
+namespace {
+
+int scatter_results(bms_ctx* c, uint64_t* counts, uint64_t* exps, uint8_t* status) {
+  CK(launch_scatter(c->recs.as<PairRec>(), c->ctr.as<Counters>(), c->rec_cap, c->pair_count.as<unsigned long long>(),
+                    c->pair_exp.as<unsigned long long>(), c->pair_flag.as<uint32_t>(), c->last_mode == BMS_FIND_FIRST,
+                    counts, exps, status, c->st));
+  return BMS_OK;
+}
+
+int ensure_qidx(bms_ctx* c) {
+  if (c->have_qidx) return BMS_OK;
+  CK(c->qidx.ensure(sizeof(uint32_t) * (c->T ? c->T : 1)));
+  CK(launch_gmcr_indices(c->valid.as<uint32_t>(), c->QW, c->q.G, c->d.G, c->gmcr_off.as<uint32_t>(),
+                         c->qidx.as<uint32_t>(), c->st));
+  c->have_qidx = true;
+  return BMS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bms_get_stats(bms_ctx* c, bms_stats* out) {
+  GUARD(c);
+  if (!out) return fail(c, BMS_EINVAL, "out is null");
+  c->stats.n_query_graphs = c->q.G;
+  c->stats.n_data_graphs = c->d.G;
+  c->stats.n_query_nodes = c->q.N;
+  c->stats.n_data_nodes = c->d.N;
+  c->stats.n_pairs = uint64_t(c->q.G) * c->d.G;
+  c->stats.last_mode = uint32_t(c->last_mode);
+  c->stats.last_order = uint32_t(c->last_order);
+  c->stats.last_semantics = uint32_t(c->last_sem);
+  *out = c->stats;
+  return BMS_OK;
+}
+
+int bms_get_gmcr(bms_ctx* c, uint32_t* offsets, uint32_t* qidx, uint64_t cap) {
+  GUARD(c);
+  if (!c->mapped) return fail(c, BMS_ESTATE, "no mapping: run bms_map or bms_run");
+  if (offsets)
+    CK(cudaMemcpyAsync(offsets, c->gmcr_off.p, sizeof(uint32_t) * (c->d.G + 1), cudaMemcpyDeviceToHost, c->st));
+  if (qidx) {
+    if (cap < c->T) return fail(c, BMS_EINVAL, "capacity below the number of mapped pairs");
+    int r = ensure_qidx(c);
+    if (r) return r;
+    if (c->T) CK(cudaMemcpyAsync(qidx, c->qidx.p, sizeof(uint32_t) * c->T, cudaMemcpyDeviceToHost, c->st));
+  }
+  CK(cudaStreamSynchronize(c->st));
+  return BMS_OK;
+}
+
+static int get_pair_array(bms_ctx* c, int which, void* out, uint64_t cap) {
+  if (!c->have_results) return fail(c, BMS_ESTATE, "no join results");
+  if (!out) return fail(c, BMS_EINVAL, "out is null");
+  if (cap < c->T) return fail(c, BMS_EINVAL, "capacity below the number of mapped pairs");
+  const size_t elem = which == 2 ? 1 : 8;
+  CK(c->tmp.ensure(elem * (c->T ? c->T : 1)));
+  if (c->T) CK(cudaMemsetAsync(c->tmp.p, 0, elem * c->T, c->st));
+  int r = scatter_results(c, which == 0 ? c->tmp.as<uint64_t>() : nullptr, which == 1 ? c->tmp.as<uint64_t>() : nullptr,
+                          which == 2 ? c->tmp.as<uint8_t>() : nullptr);
+  if (r) return r;
+  if (c->T) CK(cudaMemcpyAsync(out, c->tmp.p, elem * c->T, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return BMS_OK;
+}
+
+int bms_get_pair_counts(bms_ctx* c, uint64_t* counts, uint64_t cap) {
+  GUARD(c);
+  return get_pair_array(c, 0, counts, cap);
+}
+int bms_get_pair_expansions(bms_ctx* c, uint64_t* e, uint64_t cap) {
+  GUARD(c);
+  return get_pair_array(c, 1, e, cap);
+}
+int bms_get_pair_status(bms_ctx* c, uint8_t* s, uint64_t cap) {
+  GUARD(c);
+  return get_pair_array(c, 2, s, cap);
+}
+
+int bms_get_candidates(bms_ctx* c, uint32_t* words, uint64_t cap) {
+  GUARD(c);
+  if (!c->have_cand) return fail(c, BMS_ESTATE, "no dense candidate matrix: run bms_filter");
+  const uint64_t n = c->q.N * c->W;
+  if (!words || cap < n) return fail(c, BMS_EINVAL, "capacity below n_query_nodes * ceil(n_data_nodes/32)");
+  if (n) CK(cudaMemcpyAsync(words, c->cand.p, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return BMS_OK;
+}
+
+int bms_get_signatures(bms_ctx* c, int kind, uint64_t* label_gen, uint64_t* path, uint16_t* cycle, uint64_t* shells) {
+  GUARD(c);
+  if (kind != BMS_QUERY && kind != BMS_DATA) return fail(c, BMS_EINVAL, "invalid kind");
+  Side& s = kind == BMS_QUERY ? c->q : c->d;
+  if (s.sig_steps < 0) return fail(c, BMS_ESTATE, "no signatures: run bms_signatures or bms_run");
+  std::vector<uint64_t> rec;
+  try {
+    rec.resize(s.N * kRecWords);
+  } catch (const std::bad_alloc&) {
+    return fail(c, BMS_ENOMEM, "out of host memory");
+  }
+  if (s.N) CK(cudaMemcpyAsync(rec.data(), s.frec.p, sizeof(uint64_t) * kRecWords * s.N, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  const int R = s.sig_steps;
+  for (uint64_t v = 0; v < s.N; ++v) {
+    const uint64_t* r = rec.data() + kRecWords * v;
+    if (label_gen) label_gen[v] = r[14];
+    if (path)
+      for (int i = 0; i < 4; ++i) path[4 * v + i] = r[2 + i];
+    if (cycle)
+      for (int i = 0; i < 4; ++i) cycle[4 * v + i] = uint16_t(r[1] >> (16 * i));
+    if (shells)
+      for (int k = 0; k < R; ++k) shells[uint64_t(k) * s.N + v] = r[6 + k];
+  }
+  return BMS_OK;
+}
+
+int bms_get_schedule(bms_ctx* c, bms_schedule* out) {
+  GUARD(c);
+  if (!out) return fail(c, BMS_EINVAL, "out is null");
+  *out = c->sched;
+  return BMS_OK;
+}
+
+int bms_set_schedule(bms_ctx* c, const bms_schedule* s) {
+  GUARD(c);
+  if (!s) return fail(c, BMS_EINVAL, "schedule is null");
+  for (int i = 0; i < BMS_SCHED_BUCKETS; ++i)
+    if (s->blocks_per_sm[i] > 32 || s->warps_per_block[i] == 0 || s->warps_per_block[i] > 32 ||
+        (s->split_depth[i] != 1 && s->split_depth[i] != 2))
+      return fail(c, BMS_EINVAL, "schedule entry out of range");
+  c->sched = *s;
+  return BMS_OK;
+}
+
+}  // extern "C"

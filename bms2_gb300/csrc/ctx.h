@@ -1,0 +1,126 @@
+// Context of libbms shared by the API translation units (not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/bms.h"
+#include "graphs.h"
+#include "internal.h"
+
+namespace bms {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  cudaError_t ensure(size_t b) {
+    if (b <= bytes && p) return cudaSuccess;
+    release();
+    if (b == 0) b = 16;
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e == cudaSuccess) bytes = b;
+    else p = nullptr;
+    return e;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+struct Side {
+  bool loaded = false;
+  uint32_t G = 0;
+  uint64_t N = 0, E = 0;
+  uint32_t max_nodes = 0;
+  std::vector<uint32_t> h_goff;
+  DevBuf goff, rowp, col, lab, elab;
+  DevBuf frec, adj, ghist, glabset;
+  int sig_steps = -1;
+  bool asymmetric = false;
+  DGraphs dg() const { return DGraphs{goff.as<uint32_t>(), rowp.as<uint32_t>(), col.as<uint32_t>(), lab.as<uint8_t>(), G, N, E}; }
+  DSigs ds() const {
+    return DSigs{frec.as<uint64_t>(), adj.as<uint64_t>(), ghist.as<uint64_t>(), glabset.as<uint32_t>(), sig_steps < 0 ? 0 : sig_steps};
+  }
+};
+
+enum Ev { EV_START, EV_SIG, EV_FILTER, EV_MAP, EV_ORDER, EV_JOIN, EV_END, EV_COUNT };
+
+}  // namespace bms
+
+using bms::Counters;
+using bms::DevBuf;
+using bms::Side;
+using bms::EV_COUNT;
+
+struct bms_ctx {
+  int device = 0;
+  cudaStream_t own = nullptr, st = nullptr;
+  std::string err;
+  Side q, d;
+  DevBuf errflag;  // [0] data side, [1] query side, [2] run
+  uint32_t* h_err = nullptr;
+  DevBuf ctr;
+  Counters* h_ctr = nullptr;
+  uint32_t* h_T = nullptr;
+  // staged dense matrix
+  DevBuf cand;
+  uint64_t W = 0;
+  bool have_cand = false;
+  // mapping
+  DevBuf valid, vcounts, gmcr_off, qidx, scan_scratch, row_off, pair_nodes;
+  uint32_t QW = 0;
+  bool mapped = false, have_qidx = false;
+  uint64_t T = 0;
+  // records and join
+  DevBuf recs, arena, tasks, pair_count, pair_exp, pair_flag;
+  uint64_t rec_cap = 0, row_cap = 0, task_cap = 0;
+  DevBuf dperm;
+  uint32_t class_begin[3] = {0, 0, 0}, class_end[3] = {0, 0, 0};
+  DevBuf filter_order, label_count, perm, dadj, vertex_exp, cand_sum, recs_per_query, features, cost;
+  bool have_results = false, have_vexp = false;
+  int last_mode = 0, last_order = 0, last_sem = 0;
+  DevBuf tmp;
+  // cost model
+  DevBuf model_master, model_bf16, adam_m, adam_v, grad, grad_partial, loss_buf, train_x, train_y, pred;
+  bool model_set = false;
+  bool log_vertices = false;
+  int join_steps = 32;
+  uint64_t budget = 0;
+  bms_schedule sched{};
+  cudaEvent_t ev[EV_COUNT] = {};
+  bms_stats stats{};
+};
+
+
+namespace bms {
+int fail(bms_ctx* c, int code, const std::string& msg);
+int fail_cuda(bms_ctx* c, cudaError_t e, const char* what);
+// learned order of every query from the current records (needs a model);
+// fills c->perm (the caller derives the depth adjacency)
+int learned_order(bms_ctx* c);
+// per-vertex features of the current records into c->features
+int compute_features(bms_ctx* c);
+// re-run the join over the tasks of the last run with a given launch shape
+int rejoin_timed(bms_ctx* c, int blocks_per_sm, int warps_per_block, int steps, float* ms);
+}  // namespace bms
+
+#define CK(call)                                                   \
+  do {                                                             \
+    cudaError_t e_ = (call);                                       \
+    if (e_ != cudaSuccess) return bms::fail_cuda(c, e_, #call);    \
+  } while (0)
+
+#define GUARD(c)                                                        \
+  if (!(c)) return bms::fail(nullptr, BMS_EINVAL, "null context");      \
+  if (cudaSetDevice((c)->device) != cudaSuccess) return bms::fail(c, BMS_ECUDA, "cudaSetDevice failed");

@@ -1,0 +1,394 @@
+// Host graph batches: text parsing and writing in the reference format, CSR
+// construction, size filtering.  Follows library/include/graph.hpp:147-310 and
+// io.hpp:43-52 of the reference.
+#include "graphs.h"
+
+#include <algorithm>
+#include <cerrno>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <new>
+#include <sstream>
+
+namespace bms {
+
+static thread_local std::string g_thread_error;
+void set_thread_error(const std::string& msg) { g_thread_error = msg; }
+const char* thread_error() { return g_thread_error.c_str(); }
+
+void append_graph(bms_graphs& g, const std::vector<uint8_t>& labels, const std::vector<Edge>& edges) {
+  const uint32_t n = uint32_t(labels.size());
+  const uint32_t node_base = uint32_t(g.lab.size());
+  const uint32_t entry_base = uint32_t(g.col.size());
+  std::vector<uint32_t> rows(n + 1, 0);
+  for (const Edge& e : edges) {
+    rows[std::get<0>(e) + 1]++;
+    rows[std::get<1>(e) + 1]++;
+  }
+  for (uint32_t i = 1; i <= n; ++i) rows[i] += rows[i - 1];
+  const uint32_t entries = rows[n];
+  std::vector<uint32_t> col(entries, 0);
+  std::vector<uint8_t> el(entries, 0);
+  std::vector<uint32_t> pos(n + 1, 0);
+  for (const Edge& e : edges) {
+    const uint32_t a = std::get<0>(e), b = std::get<1>(e);
+    const uint8_t l = std::get<2>(e);
+    col[rows[a] + pos[a]] = b;
+    el[rows[a] + pos[a]] = l;
+    col[rows[b] + pos[b]] = a;
+    el[rows[b] + pos[b]] = l;
+    pos[a]++;
+    pos[b]++;
+  }
+  for (uint32_t i = 0; i < n; ++i) g.rowp.push_back(entry_base + rows[i + 1]);
+  for (uint32_t i = 0; i < entries; ++i) {
+    g.col.push_back(node_base + col[i]);
+    g.elab.push_back(el[i]);
+  }
+  g.lab.insert(g.lab.end(), labels.begin(), labels.end());
+  g.goff.push_back(node_base + n);
+  g.max_nodes = std::max(g.max_nodes, n);
+}
+
+namespace {
+
+// whitespace tokenizer over one line
+struct Tok {
+  const char* p;
+  const char* e;
+  bool next(const char*& b, size_t& n) {
+    while (p < e && (*p == ' ' || *p == '\t' || *p == '\r' || *p == '\n' || *p == '\f' || *p == '\v')) ++p;
+    if (p >= e) return false;
+    b = p;
+    while (p < e && !(*p == ' ' || *p == '\t' || *p == '\r' || *p == '\n' || *p == '\f' || *p == '\v')) ++p;
+    n = size_t(p - b);
+    return true;
+  }
+};
+
+bool to_u64(const char* b, size_t n, uint64_t& out) {
+  if (n == 0 || n > 20) return false;
+  uint64_t v = 0;
+  for (size_t i = 0; i < n; ++i) {
+    if (b[i] < '0' || b[i] > '9') return false;
+    v = v * 10 + uint64_t(b[i] - '0');
+  }
+  out = v;
+  return true;
+}
+
+bool to_i64(const char* b, size_t n, int64_t& out) {
+  bool neg = false;
+  if (n > 0 && (b[0] == '-' || b[0] == '+')) {
+    neg = b[0] == '-';
+    ++b;
+    --n;
+  }
+  uint64_t u;
+  if (!to_u64(b, n, u)) return false;
+  out = neg ? -int64_t(u) : int64_t(u);
+  return true;
+}
+
+// "n#12": the reference drops the first two characters (token.substr(2)).
+bool header(Tok& t, uint64_t& v) {
+  const char* b;
+  size_t n;
+  if (!t.next(b, n) || n < 3) return false;
+  return to_u64(b + 2, n - 2, v);
+}
+
+}  // namespace
+
+bool parse_line(const char* s, size_t len, std::vector<uint8_t>& labels, std::vector<Edge>& edges, std::string& err) {
+  Tok t{s, s + len};
+  uint64_t n = 0, nl = 0, ne = 0;
+  if (!header(t, n)) {
+    err = "expected n#<nodes>";
+    return false;
+  }
+  if (!header(t, nl)) {
+    err = "expected l#<labels>";
+    return false;
+  }
+  if (n > (uint64_t(1) << 31)) {
+    err = "node count too large";
+    return false;
+  }
+  labels.assign(n, 0);
+  for (uint64_t i = 0; i < n; ++i) {
+    const char *b1, *b2;
+    size_t n1, n2;
+    uint64_t id;
+    int64_t lab;
+    if (!t.next(b1, n1) || !t.next(b2, n2) || !to_u64(b1, n1, id) || !to_i64(b2, n2, lab)) {
+      err = "malformed node entry";
+      return false;
+    }
+    if (id >= n) {
+      err = "node id out of range";
+      return false;
+    }
+    labels[id] = uint8_t(lab);  // label_t = uint8 (types.hpp:12), int truncated
+  }
+  if (!header(t, ne)) {
+    err = "expected e#<edges>";
+    return false;
+  }
+  std::vector<std::pair<const char*, size_t>> toks;
+  const char* b;
+  size_t k;
+  while (t.next(b, k)) toks.emplace_back(b, k);
+  edges.clear();
+  size_t per;
+  if (toks.size() == ne * 3) per = 3;
+  else if (toks.size() == ne * 2) per = 2;
+  else {
+    err = "Invalid graph format";  // graph.hpp:200
+    return false;
+  }
+  edges.reserve(ne);
+  for (uint64_t i = 0; i < ne; ++i) {
+    uint64_t u, v;
+    int64_t l = 0;
+    if (!to_u64(toks[i * per].first, toks[i * per].second, u) ||
+        !to_u64(toks[i * per + 1].first, toks[i * per + 1].second, v) ||
+        (per == 3 && !to_i64(toks[i * per + 2].first, toks[i * per + 2].second, l))) {
+      err = "malformed edge entry";
+      return false;
+    }
+    if (u >= n || v >= n) {
+      err = "edge endpoint out of range";
+      return false;
+    }
+    edges.emplace_back(uint32_t(u), uint32_t(v), uint8_t(l));
+  }
+  return true;
+}
+
+}  // namespace bms
+
+using bms::set_thread_error;
+
+namespace {
+
+int parse_buffer(const char* text, size_t len, uint32_t max_graphs, int skip_invalid, bms_graphs** out) {
+  if (!out) return BMS_EINVAL;
+  *out = nullptr;
+  bms_graphs* g = new (std::nothrow) bms_graphs();
+  if (!g) return BMS_ENOMEM;
+  std::vector<uint8_t> labels;
+  std::vector<bms::Edge> edges;
+  std::string err;
+  size_t line_no = 0;
+  const char* p = text;
+  const char* end = text + len;
+  try {
+    while (p < end) {
+      const char* nl = static_cast<const char*>(std::memchr(p, '\n', size_t(end - p)));
+      const char* le = nl ? nl : end;
+      ++line_no;
+      bool blank = true;
+      for (const char* q = p; q < le; ++q)
+        if (!(*q == ' ' || *q == '\t' || *q == '\r')) {
+          blank = false;
+          break;
+        }
+      if (!blank) {
+        if (max_graphs && g->n_graphs() >= max_graphs) break;
+        if (bms::parse_line(p, size_t(le - p), labels, edges, err)) {
+          if (g->lab.size() + labels.size() > 0xFFFFFFF0ull || g->col.size() + 2 * edges.size() > 0xFFFFFFF0ull) {
+            delete g;
+            set_thread_error("batch exceeds 32-bit node or entry ids");
+            return BMS_EUNSUPPORTED;
+          }
+          bms::append_graph(*g, labels, edges);
+        } else if (!skip_invalid) {
+          delete g;
+          set_thread_error("line " + std::to_string(line_no) + ": " + err);
+          return BMS_EINVAL;
+        }
+      }
+      p = nl ? nl + 1 : end;
+    }
+  } catch (const std::bad_alloc&) {
+    delete g;
+    set_thread_error("out of host memory while parsing");
+    return BMS_ENOMEM;
+  }
+  *out = g;
+  return BMS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* bms_status_name(int s) {
+  switch (s) {
+    case BMS_OK: return "BMS_OK";
+    case BMS_EINVAL: return "BMS_EINVAL";
+    case BMS_ENOMEM: return "BMS_ENOMEM";
+    case BMS_ECUDA: return "BMS_ECUDA";
+    case BMS_EIO: return "BMS_EIO";
+    case BMS_ESTATE: return "BMS_ESTATE";
+    case BMS_EUNSUPPORTED: return "BMS_EUNSUPPORTED";
+    case BMS_ETIMEDOUT: return "BMS_ETIMEDOUT";
+    case BMS_EINCOMPLETE: return "BMS_EINCOMPLETE";
+    case BMS_ENODEV: return "BMS_ENODEV";
+    default: return "BMS_E?";
+  }
+}
+
+int bms_abi_version(void) { return BMS_ABI_VERSION; }
+
+int bms_graphs_parse_text(const char* text, size_t len, uint32_t max_graphs, int skip_invalid, bms_graphs** out) {
+  if (!text && len) return BMS_EINVAL;
+  return parse_buffer(text ? text : "", len, max_graphs, skip_invalid, out);
+}
+
+int bms_graphs_parse_file(const char* path, uint32_t max_graphs, int skip_invalid, bms_graphs** out) {
+  if (!path || !out) return BMS_EINVAL;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) {
+    set_thread_error(std::string("cannot open ") + path + ": " + std::strerror(errno));
+    return BMS_EIO;
+  }
+  std::string buf;
+  char chunk[1 << 16];
+  size_t k;
+  while ((k = std::fread(chunk, 1, sizeof chunk, f)) > 0) buf.append(chunk, k);
+  bool bad = std::ferror(f) != 0;
+  std::fclose(f);
+  if (bad) {
+    set_thread_error(std::string("read error on ") + path);
+    return BMS_EIO;
+  }
+  return parse_buffer(buf.data(), buf.size(), max_graphs, skip_invalid, out);
+}
+
+int bms_graphs_from_csr(uint32_t G, const uint32_t* goff, const uint32_t* rowp, const uint32_t* col,
+                        const uint8_t* lab, const uint8_t* elab, bms_graphs** out) {
+  if (!out || !goff || (G && (!rowp || !lab))) return BMS_EINVAL;
+  *out = nullptr;
+  if (goff[0] != 0) {
+    set_thread_error("graph_offsets[0] must be 0");
+    return BMS_EINVAL;
+  }
+  for (uint32_t i = 0; i < G; ++i)
+    if (goff[i + 1] < goff[i]) {
+      set_thread_error("graph_offsets must be non-decreasing");
+      return BMS_EINVAL;
+    }
+  const uint64_t N = goff[G];
+  if (N && rowp[0] != 0) {
+    set_thread_error("row_offsets[0] must be 0");
+    return BMS_EINVAL;
+  }
+  for (uint64_t v = 0; v < N; ++v)
+    if (rowp[v + 1] < rowp[v]) {
+      set_thread_error("row_offsets must be non-decreasing");
+      return BMS_EINVAL;
+    }
+  const uint64_t E = N ? rowp[N] : 0;
+  if (E && !col) return BMS_EINVAL;
+  bms_graphs* g = new (std::nothrow) bms_graphs();
+  if (!g) return BMS_ENOMEM;
+  try {
+    g->goff.assign(goff, goff + G + 1);
+    g->rowp.assign(rowp, rowp + N + 1);
+    if (!N) g->rowp.assign(1, 0);
+    g->col.assign(col, col + E);
+    g->lab.assign(lab, lab + N);
+    if (elab) g->elab.assign(elab, elab + E);
+    else g->elab.assign(E, 0);
+  } catch (const std::bad_alloc&) {
+    delete g;
+    return BMS_ENOMEM;
+  }
+  for (uint32_t i = 0; i < G; ++i) g->max_nodes = std::max(g->max_nodes, goff[i + 1] - goff[i]);
+  *out = g;
+  return BMS_OK;
+}
+
+int bms_graphs_view_of(const bms_graphs* g, bms_graphs_view* v) {
+  if (!g || !v) return BMS_EINVAL;
+  v->n_graphs = g->n_graphs();
+  v->max_nodes = g->max_nodes;
+  v->n_nodes = g->lab.size();
+  v->n_entries = g->col.size();
+  v->graph_offsets = g->goff.data();
+  v->row_offsets = g->rowp.data();
+  v->column_indices = g->col.data();
+  v->node_labels = g->lab.data();
+  v->edge_labels = g->elab.data();
+  return BMS_OK;
+}
+
+// One line per graph: "n#N l#11 0 L0 1 L1 ... e#E u v l ...".  Each undirected
+// edge is written once, taken from the CSR entries with u <= v in row order;
+// a CSR built by append_graph from such a line reproduces the same batch when
+// the graph has no self-loops.
+int bms_graphs_write_file(const bms_graphs* g, const char* path) {
+  if (!g || !path) return BMS_EINVAL;
+  FILE* f = std::fopen(path, "wb");
+  if (!f) {
+    set_thread_error(std::string("cannot open ") + path + ": " + std::strerror(errno));
+    return BMS_EIO;
+  }
+  std::string line;
+  bool ok = true;
+  for (uint32_t gi = 0; gi < g->n_graphs() && ok; ++gi) {
+    const uint32_t b = g->goff[gi], e = g->goff[gi + 1];
+    line.clear();
+    line += "n#" + std::to_string(e - b) + " l#11";
+    for (uint32_t v = b; v < e; ++v) line += " " + std::to_string(v - b) + " " + std::to_string(unsigned(g->lab[v]));
+    std::string el;
+    uint64_t ne = 0;
+    for (uint32_t v = b; v < e; ++v)
+      for (uint32_t i = g->rowp[v]; i < g->rowp[v + 1]; ++i) {
+        const uint32_t w = g->col[i];
+        if (w < v) continue;
+        el += " " + std::to_string(v - b) + " " + std::to_string(w - b) + " " + std::to_string(unsigned(g->elab[i]));
+        ++ne;
+      }
+    line += " e#" + std::to_string(ne) + el + "\n";
+    ok = std::fwrite(line.data(), 1, line.size(), f) == line.size();
+  }
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok) {
+    set_thread_error(std::string("write error on ") + path);
+    return BMS_EIO;
+  }
+  return BMS_OK;
+}
+
+int bms_graphs_filter_size(const bms_graphs* g, uint32_t min_nodes, uint32_t max_nodes, bms_graphs** out) {
+  if (!g || !out) return BMS_EINVAL;
+  bms_graphs* r = new (std::nothrow) bms_graphs();
+  if (!r) return BMS_ENOMEM;
+  for (uint32_t gi = 0; gi < g->n_graphs(); ++gi) {
+    const uint32_t b = g->goff[gi], e = g->goff[gi + 1], n = e - b;
+    if (n < min_nodes || n > max_nodes) continue;
+    const uint32_t node_base = uint32_t(r->lab.size());
+    const uint32_t entry_base = uint32_t(r->col.size());
+    for (uint32_t v = b; v < e; ++v) {
+      r->lab.push_back(g->lab[v]);
+      r->rowp.push_back(entry_base + (g->rowp[v + 1] - g->rowp[b]));
+    }
+    for (uint32_t i = g->rowp[b]; i < g->rowp[e]; ++i) {
+      r->col.push_back(g->col[i] - b + node_base);
+      r->elab.push_back(g->elab[i]);
+    }
+    r->goff.push_back(node_base + n);
+    r->max_nodes = std::max(r->max_nodes, n);
+  }
+  *out = r;
+  return BMS_OK;
+}
+
+void bms_graphs_free(bms_graphs* g) { delete g; }
+
+}  // extern "C"

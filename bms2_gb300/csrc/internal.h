@@ -1,0 +1,220 @@
+// Internal interfaces between the host runtime (api.cpp) and the CUDA kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace bms {
+
+constexpr uint32_t kMaxDataNodes = 128;  // two 64-bit words per bitset row
+constexpr uint32_t kMaxQueryNodes = 64;
+constexpr int kMaxSteps = 8;
+constexpr uint8_t kWildcard = 255;
+
+// validation bits raised by the signature kernel
+constexpr uint32_t kErrColumn = 1u;     // a column id outside its graph
+constexpr uint32_t kErrAsym = 2u;       // adjacency is not symmetric (as a set)
+constexpr uint32_t kErrTooLarge = 4u;   // graph exceeds the side's node limit
+constexpr uint32_t kErrOverflow = 8u;   // an output buffer was too small
+constexpr uint32_t kErrBudget = 16u;    // some task hit its expansion budget
+constexpr uint32_t kErrRows = 32u;      // row offsets decrease or exceed the entry count
+
+// A batched CSR on the device (DeviceBatchedCSRGraph, graph.hpp:58-66).
+struct DGraphs {
+  const uint32_t* goff;
+  const uint32_t* rowp;
+  const uint32_t* col;
+  const uint8_t* lab;
+  uint32_t G;
+  uint64_t N;
+  uint64_t E;  // CSR entries; row offsets beyond it are rejected
+};
+
+// Signatures of one side.  Each node has a 128-byte filter record, one cache
+// line, holding everything the filter and refine stages compare:
+//   w0  label | degree << 32        w1  cycle: 4 x uint16 (5-same, 5-diff, 6-same, 6-diff)
+//   w2..w5  256-bit path filter     w6..w13  distance shells 1..8 (16 nibbles each)
+//   w14 label signature (neighbour label counts)   w15 zero
+// adj holds two 64-bit words per node: the set of local ids in the node's CSR row.
+constexpr int kRecWords = 16;
+struct DSigs {
+  uint64_t* frec;       // [N*16]
+  uint64_t* adj;        // [N*2]
+  uint64_t* ghist;      // [G]   per-graph nibble histogram of labels < 16
+  uint32_t* glabset;    // [G]   bit l: some node has label l (< 16)
+  int R;
+};
+
+// One mapped (query, data graph) pair whose join is still to run.
+struct PairRec {
+  uint32_t q;
+  uint32_t d;
+  uint32_t gpos;   // position in GMCR order
+  uint32_t c_row;  // first candidate row in the arena (rows of 2 x uint64)
+};
+
+// A join task: a pair and the local id of the root (first vertex of the order).
+struct Task {
+  uint32_t pair;
+  uint32_t root;
+};
+
+// Per-query search order: perm[q*64 + t] is the vertex at depth t; dadj[q*64 + t]
+// has bit i (i < t) set iff the vertex at depth i is in the CSR row of the
+// vertex at depth t (the reference's query_adj_masks, isomorphism.hpp:383-390).
+struct DOrder {
+  uint8_t* perm;
+  uint64_t* dadj;
+};
+
+// Device counters of one run, zeroed at its start.  The pipeline reads its
+// sizes from here, so no stage waits for the host between launches.
+struct Counters {
+  unsigned long long recs;        // PairRecs written
+  unsigned long long rows;        // candidate rows allocated in the arena
+  unsigned long long tasks;       // join tasks emitted
+  unsigned long long task_fetch;  // join work-stealing head
+  unsigned int work[4];           // pair-filter work heads, one per size class
+  unsigned long long total;       // sum of per-pair counts
+  unsigned long long expansions;  // sum of per-pair expansions
+  unsigned long long incomplete;  // pairs that hit the expansion budget
+  unsigned long long pad;
+};
+
+// ----------------------------------------------------------------- launchers
+// All return cudaSuccess or the launch error.
+int sm_count();
+// kernels launched by this host thread (every launcher counts its launches)
+extern thread_local unsigned long long g_launches;
+inline void note_launch() { ++g_launches; }
+
+cudaError_t launch_signatures(const DGraphs& g, DSigs s, uint32_t max_nodes, uint32_t* err, cudaStream_t st);
+
+// Staged (reference-shaped) stages on the dense query-major candidate matrix.
+cudaError_t launch_filter_dense(const DGraphs& q, const DSigs& qs, const DGraphs& d, const DSigs& ds, uint32_t* cand,
+                                uint64_t W, cudaStream_t st);
+cudaError_t launch_refine_dense(const DSigs& qs, uint64_t Qn, const DSigs& ds, uint64_t Dn, int step, uint32_t* cand,
+                                uint64_t W, cudaStream_t st);
+// GMCR validity from the dense matrix: valid bits [D][QW] and per-data-graph counts.
+cudaError_t launch_gmcr_dense(const DGraphs& q, const DGraphs& d, const uint32_t* cand, uint64_t W, uint32_t* valid,
+                              uint32_t QW, uint32_t* vcounts, cudaStream_t st);
+// Staged path: number of query nodes of every GMCR pair, then one PairRec per
+// pair with its candidate rows gathered from the dense matrix.
+cudaError_t launch_pair_nodes(const DGraphs& q, const uint32_t* qidx, uint64_t T, uint32_t* nodes, cudaStream_t st);
+cudaError_t launch_gather_pairs(const DGraphs& q, const DGraphs& d, const uint32_t* cand, uint64_t W,
+                                const uint32_t* offsets, const uint32_t* qidx, const uint32_t* row_off, PairRec* recs,
+                                uint64_t* arena, cudaStream_t st);
+cudaError_t launch_set_counter(unsigned long long* dst, unsigned long long value, cudaStream_t st);
+
+// Label totals over all data nodes (labels 0..255).
+cudaError_t launch_label_count(const DGraphs& d, unsigned long long* counts, cudaStream_t st);
+// Per query: vertex order of the validity test (rarest label first, then
+// highest degree), its label set and its label histogram.
+cudaError_t launch_query_prep(const DGraphs& q, const DSigs& qs, const unsigned long long* label_count,
+                              uint8_t* filter_order, cudaStream_t st);
+
+// Fused filter + refine + GMCR validity for every (query, data graph) pair.
+struct PairFilterArgs {
+  DGraphs q, d;
+  DSigs qs, ds;
+  const uint8_t* filter_order;  // [Q*64]
+  const uint32_t* dperm;        // data graph ids grouped by size class
+  uint32_t class_begin, class_end;
+  int class_id;
+  uint32_t* valid;              // [D][QW] GMCR validity bits
+  uint32_t QW;
+  uint32_t* vcounts;            // [D] valid pairs per data graph
+  PairRec* recs;                // appended join-eligible pairs
+  uint64_t rec_cap;
+  uint64_t* arena;              // candidate rows, 2 words each
+  uint64_t row_cap;
+  Counters* ctr;
+  uint32_t* err;
+  int skip_by_labels;           // skip pairs whose label multiset cannot embed (EXACT only)
+  unsigned int* cand_sum;       // nullable: per query node, sum of candidate-set sizes over records
+};
+cudaError_t launch_pair_filter(const PairFilterArgs& a, int rounds, cudaStream_t st);
+
+// exclusive scan of n uint32 values into out[0..n] (out[n] = total); scratch
+// must hold scan_scratch_words(n) words.
+size_t scan_scratch_words(uint64_t n);
+cudaError_t launch_scan_u32(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* scratch, cudaStream_t st);
+
+// GMCR query indices from the valid bits and offsets.
+cudaError_t launch_gmcr_indices(const uint32_t* valid, uint32_t QW, uint32_t Q, uint32_t D, const uint32_t* offsets,
+                                uint32_t* qidx, cudaStream_t st);
+// Fill in PairRec::gpos of records produced by the fused filter.
+cudaError_t launch_pair_positions(PairRec* recs, const Counters* ctr, uint64_t rec_cap, const uint32_t* valid,
+                                  uint32_t QW, const uint32_t* offsets, cudaStream_t st);
+
+// Plain (query-index) order; depth adjacency of any order whose perm is set.
+cudaError_t launch_plain_order(const DGraphs& q, DOrder o, cudaStream_t st);
+cudaError_t launch_order_adjacency(const DGraphs& q, const DSigs& qs, DOrder o, cudaStream_t st);
+
+// One task per root of every record under the order (atomic append).
+cudaError_t launch_task_emit(const PairRec* recs, uint64_t rec_cap, const DGraphs& q, DOrder o, const uint64_t* arena,
+                             Task* tasks, uint64_t task_cap, Counters* ctr, uint32_t* err, cudaStream_t st);
+
+struct JoinArgs {
+  DGraphs q, d;
+  DSigs ds;  // adjacency rows of the data side
+  DOrder o;
+  const PairRec* recs;
+  const uint64_t* arena;
+  const Task* tasks;
+  uint64_t task_cap;
+  Counters* ctr;
+  unsigned long long* pair_count;  // per record
+  unsigned long long* pair_exp;    // per record
+  uint32_t* pair_flag;             // per record: bit0 found (find-first), bit1 incomplete
+  unsigned long long* vertex_exp;  // nullable: per query node expansions (plain-order logging)
+  uint64_t budget;                 // 0 = unlimited
+  int find_first;
+  int literal;                     // REFERENCE_DFS semantics
+  int steps;                       // DFS steps between refills
+};
+cudaError_t launch_join(const JoinArgs& a, int blocks, int threads, cudaStream_t st);
+
+// Totals over the records (count, expansions, incomplete pairs) into ctr.
+cudaError_t launch_totals(const Counters* ctr_in, uint64_t rec_cap, const unsigned long long* pair_count,
+                          const unsigned long long* pair_exp, const uint32_t* pair_flag, int find_first, Counters* ctr,
+                          cudaStream_t st);
+// Per-record results into GMCR order (arrays of T entries, zero-filled first).
+cudaError_t launch_scatter(const PairRec* recs, const Counters* ctr, uint64_t rec_cap,
+                           const unsigned long long* pair_count, const unsigned long long* pair_exp,
+                           const uint32_t* pair_flag, int find_first, uint64_t* counts, uint64_t* exps,
+                           uint8_t* status, cudaStream_t st);
+
+// ------------------------------------------------------------- learned order
+constexpr int kFeatures = 12;
+constexpr int kHidden = 64;
+constexpr int kParams = kHidden * kFeatures + kHidden + kHidden * kHidden + kHidden + kHidden + 1;
+struct DFeatureArgs {
+  DGraphs q;
+  DSigs qs;
+  const unsigned long long* label_count;  // [256] data nodes per label
+  uint64_t data_nodes;
+  const unsigned int* cand_sum;           // [Qn] sum over records of candidate-set sizes
+  const unsigned int* recs_per_query;     // [Q]
+  float* features;                        // [Qn * 12]
+};
+// Per query: number of records; per query node: sum of candidate-set sizes.
+cudaError_t launch_record_stats(const PairRec* recs, const Counters* ctr, uint64_t rec_cap, const DGraphs& q,
+                                const uint64_t* arena, unsigned int* per_query, unsigned int* cand_sum,
+                                cudaStream_t st);
+cudaError_t launch_features(const DFeatureArgs& a, cudaStream_t st);
+// Inference: cost per query node, then a per-query greedy connected order.
+cudaError_t launch_mlp_predict(const float* features, uint64_t n, const uint16_t* wbf16, float* cost, cudaStream_t st);
+cudaError_t launch_learned_order(const DGraphs& q, const DSigs& qs, const float* cost, DOrder o, cudaStream_t st);
+// Training: forward + backward per 32-sample block into partial gradients,
+// then a fixed-order reduction (deterministic).  n_total scales the MSE.
+int mlp_grad_blocks(uint32_t n);
+cudaError_t launch_mlp_grad(const float* x, const float* y, uint32_t n, uint32_t n_total, const uint16_t* wbf16,
+                            float* grad_partial, float* pred, float* loss_partial, cudaStream_t st);
+cudaError_t launch_mlp_reduce(const float* grad_partial, int blocks, float* grad, const float* loss_partial, float* loss,
+                              uint32_t n, cudaStream_t st);
+cudaError_t launch_adam(float* master, uint16_t* wbf16, const float* grad, float* m, float* v, float lr, float b1,
+                        float b2, float eps, int step, cudaStream_t st);
+cudaError_t launch_to_bf16(const float* master, uint16_t* wbf16, int n, cudaStream_t st);
+
+}  // namespace bms

@@ -1,0 +1,328 @@
+// Mapping and bookkeeping kernels: GMCR offsets and query indices (gmcr.hpp:
+// 92-127, with a parallel scan in place of the reference's single-work-item
+// prefix sum), query preparation, search orders, task emission, totals and the
+// scatter of per-pair results into GMCR order.
+#include "device_common.cuh"
+
+namespace bms {
+namespace {
+
+unsigned grid_for(uint64_t work, unsigned threads, unsigned per_sm = 8) {
+  uint64_t want = (work + threads - 1) / threads;
+  uint64_t cap = uint64_t(sm_count()) * per_sm;
+  if (want < 1) want = 1;
+  return unsigned(want < cap ? want : cap);
+}
+
+// ------------------------------------------------------------------ labels
+__global__ void label_count_kernel(DGraphs d, unsigned long long* counts) {
+  __shared__ unsigned int h[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  for (uint64_t v = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; v < d.N; v += uint64_t(gridDim.x) * blockDim.x)
+    atomicAdd(&h[d.lab[v]], 1u);
+  __syncthreads();
+  for (int i = threadIdx.x; i < 256; i += blockDim.x)
+    if (h[i]) atomicAdd(&counts[i], (unsigned long long)h[i]);
+}
+
+// One thread per query: validity-test order, rarest label first (wildcards
+// last), ties by higher degree, then by index.
+__global__ void query_prep_kernel(DGraphs q, DSigs qs, const unsigned long long* label_count, uint8_t* order) {
+  for (uint32_t qg = blockIdx.x * blockDim.x + threadIdx.x; qg < q.G; qg += gridDim.x * blockDim.x) {
+    const uint32_t qoff = q.goff[qg], n = q.goff[qg + 1] - qoff;
+    uint8_t* o = order + uint64_t(qg) * kMaxQueryNodes;
+    unsigned long long key[kMaxQueryNodes];
+    for (uint32_t i = 0; i < n && i < kMaxQueryNodes; ++i) {
+      const uint64_t w0 = qs.frec[uint64_t(kRecWords) * (qoff + i)];
+      const uint32_t l = uint32_t(w0 & 0xFFu), deg = uint32_t(w0 >> 32);
+      const unsigned long long freq = l == kWildcard ? 0xFFFFFFFFFFull : (label_count[l] & 0xFFFFFFFFFFull);
+      const uint32_t dk = 0xFFFFu - (deg > 0xFFFFu ? 0xFFFFu : deg);
+      key[i] = (freq << 22) | (uint64_t(dk) << 6) | i;
+      o[i] = uint8_t(i);
+    }
+    for (uint32_t i = 1; i < n && i < kMaxQueryNodes; ++i) {
+      const unsigned long long k = key[i];
+      const uint8_t v = o[i];
+      int j = int(i) - 1;
+      while (j >= 0 && key[j] > k) {
+        key[j + 1] = key[j];
+        o[j + 1] = o[j];
+        --j;
+      }
+      key[j + 1] = k;
+      o[j + 1] = v;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ scan
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr uint64_t kScanBlock = kScanThreads * kScanItems;
+
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t x, uint32_t* s_warp, uint32_t& total) {
+  const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+  uint32_t inc = x;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= uint32_t(o)) inc += y;
+  }
+  if (lane == 31) s_warp[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < (blockDim.x >> 5) ? s_warp[lane] : 0u;
+    uint32_t wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= uint32_t(o)) wi += y;
+    }
+    if (lane < (blockDim.x >> 5)) s_warp[lane] = wi - w;
+    if (lane == 31) s_warp[32] = wi;
+  }
+  __syncthreads();
+  const uint32_t r = s_warp[warp] + inc - x;
+  total = s_warp[32];
+  __syncthreads();
+  return r;
+}
+
+// out[i] = exclusive prefix within the block chunk; sums[b] = chunk total
+__global__ void __launch_bounds__(kScanThreads) scan_chunks(const uint32_t* in, uint32_t* out, uint64_t n,
+                                                            uint32_t* sums) {
+  __shared__ uint32_t s_warp[33];
+  const uint64_t base = uint64_t(blockIdx.x) * kScanBlock + uint64_t(threadIdx.x) * kScanItems;
+  uint32_t v[kScanItems];
+  uint32_t local = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    v[i] = base + i < n ? in[base + i] : 0u;
+    local += v[i];
+  }
+  uint32_t total;
+  uint32_t pre = block_exclusive_scan(local, s_warp, total);
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    if (base + i < n) out[base + i] = pre;
+    pre += v[i];
+  }
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+__global__ void scan_add(uint32_t* out, uint64_t n, const uint32_t* offs) {
+  const uint64_t base = uint64_t(blockIdx.x) * kScanBlock;
+  const uint32_t add = offs[blockIdx.x];
+  for (uint64_t i = base + threadIdx.x; i < base + kScanBlock && i < n; i += blockDim.x) out[i] += add;
+}
+
+__global__ void scan_total(const uint32_t* in, const uint32_t* out, uint64_t n, uint32_t* last) {
+  *last = n ? out[n - 1] + in[n - 1] : 0u;
+}
+
+// ------------------------------------------------------------------ GMCR
+__global__ void gmcr_indices_kernel(const uint32_t* valid, uint32_t QW, uint32_t Q, uint32_t D, const uint32_t* offsets,
+                                    uint32_t* qidx) {
+  for (uint32_t dg = blockIdx.x * blockDim.x + threadIdx.x; dg < D; dg += gridDim.x * blockDim.x) {
+    uint32_t pos = offsets[dg];
+    const uint32_t* row = valid + uint64_t(dg) * QW;
+    for (uint32_t w = 0; w < QW; ++w)
+      for (uint32_t bits = row[w]; bits; bits &= bits - 1) qidx[pos++] = w * 32 + uint32_t(__ffs(bits) - 1);
+  }
+}
+
+__global__ void pair_positions_kernel(PairRec* recs, const Counters* ctr, uint64_t rec_cap, const uint32_t* valid,
+                                      uint32_t QW, const uint32_t* offsets) {
+  const uint64_t n = min((unsigned long long)rec_cap, ctr->recs);
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+    const PairRec r = recs[i];
+    const uint32_t* row = valid + uint64_t(r.d) * QW;
+    uint32_t rank = 0;
+    for (uint32_t w = 0; w < (r.q >> 5); ++w) rank += __popc(row[w]);
+    rank += __popc(row[r.q >> 5] & ((1u << (r.q & 31u)) - 1u));
+    recs[i].gpos = offsets[r.d] + rank;
+  }
+}
+
+// ------------------------------------------------------------------ orders
+__global__ void plain_order_kernel(DGraphs q, DOrder o) {
+  for (uint32_t qg = blockIdx.x * blockDim.x + threadIdx.x; qg < q.G; qg += gridDim.x * blockDim.x) {
+    const uint32_t n = q.goff[qg + 1] - q.goff[qg];
+    for (uint32_t t = 0; t < n && t < kMaxQueryNodes; ++t) o.perm[uint64_t(qg) * kMaxQueryNodes + t] = uint8_t(t);
+  }
+}
+
+// dadj[t] bit i  <=>  perm[i] is in the CSR row of perm[t]
+__global__ void order_adjacency_kernel(DGraphs q, DSigs qs, DOrder o) {
+  const uint64_t total = uint64_t(q.G) * kMaxQueryNodes;
+  for (uint64_t k = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < total; k += uint64_t(gridDim.x) * blockDim.x) {
+    const uint32_t qg = uint32_t(k / kMaxQueryNodes), t = uint32_t(k % kMaxQueryNodes);
+    const uint32_t qoff = q.goff[qg], n = q.goff[qg + 1] - qoff;
+    if (t >= n) continue;
+    const uint8_t* perm = o.perm + uint64_t(qg) * kMaxQueryNodes;
+    const uint64_t row = qs.adj[2 * (uint64_t(qoff) + perm[t])];  // queries have at most 64 nodes
+    uint64_t m = 0;
+    for (uint32_t i = 0; i < t; ++i) m |= ((row >> perm[i]) & 1ull) << i;
+    o.dadj[k] = m;
+  }
+}
+
+// ------------------------------------------------------------------ tasks
+__global__ void task_emit_kernel(const PairRec* recs, uint64_t rec_cap, DGraphs q, DOrder o, const uint64_t* arena,
+                                 Task* tasks, uint64_t task_cap, Counters* ctr, uint32_t* err) {
+  const uint64_t n = min((unsigned long long)rec_cap, ctr->recs);
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+    const PairRec r = recs[i];
+    const uint32_t root = o.perm[uint64_t(r.q) * kMaxQueryNodes];
+    B128 c = ld_b128(arena + 2 * (uint64_t(r.c_row) + root));
+    const uint32_t k = b_pop(c);
+    if (!k) continue;
+    const unsigned long long base = atomicAdd(&ctr->tasks, (unsigned long long)k);
+    if (base + k > task_cap) {
+      atomicOr(err, kErrOverflow);
+      continue;
+    }
+    for (uint32_t j = 0; j < k; ++j) {
+      tasks[base + j] = Task{uint32_t(i), b_low(c)};
+      c = b_clear_low(c);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ totals
+__global__ void totals_kernel(const Counters* ctr_in, uint64_t rec_cap, const unsigned long long* pair_count,
+                              const unsigned long long* pair_exp, const uint32_t* pair_flag, int find_first,
+                              Counters* ctr) {
+  const uint64_t n = min((unsigned long long)rec_cap, ctr_in->recs);
+  unsigned long long c = 0, e = 0, inc = 0;
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+    const unsigned long long k = pair_count[i];
+    c += find_first ? (k ? 1ull : 0ull) : k;
+    e += pair_exp[i];
+    inc += (pair_flag[i] >> 1) & 1u;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    c += __shfl_down_sync(0xffffffffu, c, o);
+    e += __shfl_down_sync(0xffffffffu, e, o);
+    inc += __shfl_down_sync(0xffffffffu, inc, o);
+  }
+  if (lane_id() == 0) {
+    if (c) atomicAdd(&ctr->total, c);
+    if (e) atomicAdd(&ctr->expansions, e);
+    if (inc) atomicAdd(&ctr->incomplete, inc);
+  }
+}
+
+__global__ void scatter_kernel(const PairRec* recs, const Counters* ctr, uint64_t rec_cap,
+                               const unsigned long long* pair_count, const unsigned long long* pair_exp,
+                               const uint32_t* pair_flag, int find_first, uint64_t* counts, uint64_t* exps,
+                               uint8_t* status) {
+  const uint64_t n = min((unsigned long long)rec_cap, ctr->recs);
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+    const uint32_t g = recs[i].gpos;
+    const unsigned long long k = pair_count[i];
+    if (counts) counts[g] = find_first ? (k ? 1ull : 0ull) : k;
+    if (exps) exps[g] = pair_exp[i];
+    if (status) status[g] = uint8_t((pair_flag[i] >> 1) & 1u);
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_label_count(const DGraphs& d, unsigned long long* counts, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(counts, 0, 256 * sizeof(unsigned long long), st);
+  if (e != cudaSuccess || d.N == 0) return e;
+  label_count_kernel<<<grid_for(d.N, 256, 4), 256, 0, st>>>(d, counts); note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_query_prep(const DGraphs& q, const DSigs& qs, const unsigned long long* label_count,
+                              uint8_t* filter_order, cudaStream_t st) {
+  if (q.G == 0) return cudaSuccess;
+  query_prep_kernel<<<grid_for(q.G, 64), 64, 0, st>>>(q, qs, label_count, filter_order); note_launch();
+  return cudaGetLastError();
+}
+
+size_t scan_scratch_words(uint64_t n) {
+  size_t w = 0;
+  while (n > kScanBlock) {
+    n = (n + kScanBlock - 1) / kScanBlock;
+    w += 2 * n + 1;
+  }
+  return w + 2;
+}
+
+cudaError_t launch_scan_u32(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* scratch, cudaStream_t st) {
+  if (n == 0) return cudaMemsetAsync(out, 0, sizeof(uint32_t), st);
+  const uint64_t blocks = (n + kScanBlock - 1) / kScanBlock;
+  if (blocks > 0x7FFFFFFFull) return cudaErrorInvalidValue;
+  uint32_t* sums = scratch;
+  uint32_t* sums_scan = scratch + blocks;
+  scan_chunks<<<unsigned(blocks), kScanThreads, 0, st>>>(in, out, n, sums); note_launch();
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  if (blocks > 1) {
+    e = launch_scan_u32(sums, sums_scan, blocks, scratch + 2 * blocks + 1, st);
+    if (e != cudaSuccess) return e;
+    scan_add<<<unsigned(blocks), 256, 0, st>>>(out, n, sums_scan); note_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  scan_total<<<1, 1, 0, st>>>(in, out, n, out + n); note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gmcr_indices(const uint32_t* valid, uint32_t QW, uint32_t Q, uint32_t D, const uint32_t* offsets,
+                                uint32_t* qidx, cudaStream_t st) {
+  if (D == 0) return cudaSuccess;
+  gmcr_indices_kernel<<<grid_for(D, 128, 16), 128, 0, st>>>(valid, QW, Q, D, offsets, qidx); note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pair_positions(PairRec* recs, const Counters* ctr, uint64_t rec_cap, const uint32_t* valid,
+                                  uint32_t QW, const uint32_t* offsets, cudaStream_t st) {
+  if (rec_cap == 0) return cudaSuccess;
+  pair_positions_kernel<<<grid_for(rec_cap, 256, 4), 256, 0, st>>>(recs, ctr, rec_cap, valid, QW, offsets); note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_plain_order(const DGraphs& q, DOrder o, cudaStream_t st) {
+  if (q.G == 0) return cudaSuccess;
+  plain_order_kernel<<<grid_for(q.G, 128), 128, 0, st>>>(q, o); note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_order_adjacency(const DGraphs& q, const DSigs& qs, DOrder o, cudaStream_t st) {
+  if (q.G == 0) return cudaSuccess;
+  order_adjacency_kernel<<<grid_for(uint64_t(q.G) * kMaxQueryNodes, 256), 256, 0, st>>>(q, qs, o); note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_task_emit(const PairRec* recs, uint64_t rec_cap, const DGraphs& q, DOrder o, const uint64_t* arena,
+                             Task* tasks, uint64_t task_cap, Counters* ctr, uint32_t* err, cudaStream_t st) {
+  if (rec_cap == 0) return cudaSuccess;
+  task_emit_kernel<<<grid_for(rec_cap, 256, 4), 256, 0, st>>>(recs, rec_cap, q, o, arena, tasks, task_cap, ctr, err); note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_totals(const Counters* ctr_in, uint64_t rec_cap, const unsigned long long* pair_count,
+                          const unsigned long long* pair_exp, const uint32_t* pair_flag, int find_first, Counters* ctr,
+                          cudaStream_t st) {
+  if (rec_cap == 0) return cudaSuccess;
+  totals_kernel<<<grid_for(rec_cap, 256, 4), 256, 0, st>>>(ctr_in, rec_cap, pair_count, pair_exp, pair_flag,
+                                                            find_first, ctr); note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter(const PairRec* recs, const Counters* ctr, uint64_t rec_cap,
+                           const unsigned long long* pair_count, const unsigned long long* pair_exp,
+                           const uint32_t* pair_flag, int find_first, uint64_t* counts, uint64_t* exps,
+                           uint8_t* status, cudaStream_t st) {
+  if (rec_cap == 0) return cudaSuccess;
+  scatter_kernel<<<grid_for(rec_cap, 256, 4), 256, 0, st>>>(recs, ctr, rec_cap, pair_count, pair_exp, pair_flag,
+                                                             find_first, counts, exps, status); note_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace bms

@@ -1,0 +1,286 @@
+// Node signatures of a graph batch, one warp per graph.
+//
+// Replaces, for one side (data or queries), the reference kernels
+//   GenerateDataSignaturesKernel      signature.hpp:124-151   -> label_gen
+//   GenerateCSRPathSignaturesKernel   signature.hpp:472-519   -> path
+//   GenerateCSRCycleSignaturesKernel  signature.hpp:591-719   -> cycle
+//   RefineDataSignaturesKernel (x R)  signature.hpp:335-389   -> shells[k]
+// in a single pass.  The graph's adjacency is staged in shared memory as one
+// 128-bit set per node, so every walk, path and BFS runs on on-chip bitsets.
+// Semantics are the reference's with bitsets as wide as the graph (no 64-node
+// aliasing, no 128-entry stack cap, cycle signatures for every graph size).
+#include "device_common.cuh"
+
+namespace bms {
+namespace {
+
+constexpr int kWarps = 4;  // ~7.8 KB of shared memory per warp
+constexpr int kMaxEntries = 1024;  // CSR entries staged per graph; larger rows read global memory
+
+struct WarpSmem {
+  B128 adj[kMaxDataNodes];      // out-neighbour set of every node (row as a set)
+  B128 in[kMaxDataNodes];       // in-neighbour set
+  B128 same[kMaxDataNodes];     // nodes with the same label
+  uint8_t lab[kMaxDataNodes];
+  uint16_t row[kMaxDataNodes + 1];
+  uint8_t col[kMaxEntries];
+  B128 labmask[16];
+};
+
+// CSR row access of the current graph with local ids, from shared memory when
+// the graph fits, else from global memory.
+struct Rows {
+  const WarpSmem* s;
+  const uint32_t* rowp;
+  const uint32_t* col;
+  uint32_t start;
+  bool global;
+  __device__ uint32_t begin(uint32_t v) const { return global ? rowp[start + v] : s->row[v]; }
+  __device__ uint32_t end(uint32_t v) const { return global ? rowp[start + v + 1] : s->row[v + 1]; }
+  __device__ uint32_t at(uint32_t i) const { return global ? col[i] - start : s->col[i]; }
+};
+
+__device__ uint32_t mult(const Rows& r, uint32_t a, uint32_t target) {
+  uint32_t k = 0;
+  for (uint32_t i = r.begin(a); i < r.end(a); ++i) k += r.at(i) == target;
+  return k;
+}
+
+// Cycle closures through v following CSR entries (multi-edge graphs).
+__device__ void cycles_entries(const WarpSmem& s, const Rows& r, uint32_t v, uint32_t c[4]) {
+  const uint32_t lv = s.lab[v];
+  for (uint32_t i1 = r.begin(v); i1 < r.end(v); ++i1) {
+    const uint32_t a = r.at(i1);
+    const bool s1 = s.lab[a] == lv;
+    const B128 m1 = b_or(b_bit(v), b_bit(a));
+    for (uint32_t i2 = r.begin(a); i2 < r.end(a); ++i2) {
+      const uint32_t b = r.at(i2);
+      if (b == v || b_has(m1, b)) continue;
+      const bool s2 = s1 && s.lab[b] == lv;
+      const B128 m2 = b_or(m1, b_bit(b));
+      for (uint32_t i3 = r.begin(b); i3 < r.end(b); ++i3) {
+        const uint32_t cc = r.at(i3);
+        if (cc == v || b_has(m2, cc)) continue;
+        const bool s3 = s2 && s.lab[cc] == lv;
+        const B128 m3 = b_or(m2, b_bit(cc));
+        for (uint32_t i4 = r.begin(cc); i4 < r.end(cc); ++i4) {
+          const uint32_t d = r.at(i4);
+          if (d == v || b_has(m3, d)) continue;
+          const bool s4 = s3 && s.lab[d] == lv;
+          const uint32_t k4 = mult(r, d, v);
+          c[s4 ? 0 : 1] += k4;
+          const B128 m4 = b_or(m3, b_bit(d));
+          for (uint32_t i5 = r.begin(d); i5 < r.end(d); ++i5) {
+            const uint32_t e = r.at(i5);
+            if (e == v || b_has(m4, e)) continue;
+            const bool s5 = s4 && s.lab[e] == lv;
+            c[s5 ? 2 : 3] += mult(r, e, v);
+          }
+        }
+      }
+    }
+  }
+}
+
+// Cycle closures through v on adjacency sets (graphs without repeated entries).
+// At depth 5 the closing nodes are counted in one step: they are the unvisited
+// out-neighbours of the depth-4 node whose rows contain v.
+__device__ void cycles_sets(const WarpSmem& s, uint32_t v, uint32_t c[4]) {
+  const uint32_t lv = s.lab[v];
+  const B128 inv = s.in[v];
+  const B128 eq = s.same[v];
+  for (B128 r1 = s.adj[v]; b_any(r1); r1 = b_clear_low(r1)) {
+    const uint32_t a = b_low(r1);
+    const bool s1 = s.lab[a] == lv;
+    const B128 m1 = b_or(b_bit(v), b_bit(a));
+    for (B128 r2 = b_andn(s.adj[a], m1); b_any(r2); r2 = b_clear_low(r2)) {
+      const uint32_t b = b_low(r2);
+      const bool s2 = s1 && s.lab[b] == lv;
+      const B128 m2 = b_or(m1, b_bit(b));
+      for (B128 r3 = b_andn(s.adj[b], m2); b_any(r3); r3 = b_clear_low(r3)) {
+        const uint32_t cc = b_low(r3);
+        const bool s3 = s2 && s.lab[cc] == lv;
+        const B128 m3 = b_or(m2, b_bit(cc));
+        for (B128 r4 = b_andn(s.adj[cc], m3); b_any(r4); r4 = b_clear_low(r4)) {
+          const uint32_t d = b_low(r4);
+          const bool s4 = s3 && s.lab[d] == lv;
+          if (b_has(inv, d)) c[s4 ? 0 : 1] += 1;
+          const B128 close = b_and(b_andn(s.adj[d], b_or(m3, b_bit(d))), inv);
+          const uint32_t all = b_pop(close);
+          const uint32_t same = s4 ? b_pop(b_and(close, eq)) : 0u;
+          c[2] += same;
+          c[3] += all - same;
+        }
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kWarps * 32) signatures_kernel(DGraphs g, DSigs out, uint32_t max_nodes,
+                                                                uint32_t* err) {
+  __shared__ WarpSmem smem[kWarps];
+  const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
+  WarpSmem& s = smem[warp];
+  for (uint32_t gi = blockIdx.x * kWarps + warp; gi < g.G; gi += gridDim.x * kWarps) {
+    const uint32_t start = g.goff[gi];
+    const uint32_t m = g.goff[gi + 1] - start;
+    if (m > max_nodes) {
+      if (lane == 0) atomicOr(err, kErrTooLarge);
+      continue;
+    }
+    // row offsets of this graph must be non-decreasing and inside [0, E]
+    bool rows_ok = true;
+    for (uint32_t v = lane; v <= m; v += 32) {
+      const uint64_t r = g.rowp[start + v];
+      rows_ok = rows_ok && r <= g.E && (v == 0 || g.rowp[start + v - 1] <= r);
+    }
+    if (!__all_sync(0xffffffffu, rows_ok)) {
+      if (lane == 0) atomicOr(err, kErrRows);
+      continue;
+    }
+    const uint32_t e0 = g.rowp[start];
+    const uint32_t entries = g.rowp[start + m] - e0;
+    const bool global_rows = entries > uint32_t(kMaxEntries);
+    // stage labels, rows, entries; build adjacency sets
+    uint32_t bad = 0;
+    bool multi = false;
+    for (uint32_t v = lane; v < m; v += 32) {
+      s.lab[v] = g.lab[start + v];
+      const uint32_t rb = g.rowp[start + v], re = g.rowp[start + v + 1];
+      if (!global_rows) {
+        s.row[v] = uint16_t(rb - e0);
+        if (v == m - 1) s.row[m] = uint16_t(re - e0);
+      }
+      B128 a{0, 0};
+      for (uint32_t i = rb; i < re; ++i) {
+        const uint32_t c = g.col[i];
+        uint32_t lc = c - start;
+        if (c < start || lc >= m) {
+          bad |= kErrColumn;
+          lc = 0;  // keep the entry inside the graph; the batch is rejected
+        }
+        if (!global_rows) s.col[i - e0] = uint8_t(lc);
+        if (b_has(a, lc)) multi = true;
+        a = b_or(a, b_bit(lc));
+      }
+      s.adj[v] = a;
+      s.in[v] = B128{0, 0};
+    }
+    if (lane < 16) s.labmask[lane] = B128{0, 0};
+    multi = __any_sync(0xffffffffu, multi);
+    bad = __reduce_or_sync(0xffffffffu, bad);
+    __syncwarp();
+    // in-neighbour sets, label masks
+    for (uint32_t v = lane; v < m; v += 32) {
+      for (B128 r = s.adj[v]; b_any(r); r = b_clear_low(r)) {
+        const uint32_t w = b_low(r);
+        const B128 bv = b_bit(v);
+        atomicOr(reinterpret_cast<unsigned long long*>(&s.in[w].lo), (unsigned long long)bv.lo);
+        atomicOr(reinterpret_cast<unsigned long long*>(&s.in[w].hi), (unsigned long long)bv.hi);
+      }
+      const uint32_t l = s.lab[v];
+      if (l < 16) {
+        const B128 bv = b_bit(v);
+        atomicOr(reinterpret_cast<unsigned long long*>(&s.labmask[l].lo), (unsigned long long)bv.lo);
+        atomicOr(reinterpret_cast<unsigned long long*>(&s.labmask[l].hi), (unsigned long long)bv.hi);
+      }
+    }
+    __syncwarp();
+    for (uint32_t v = lane; v < m; v += 32) {
+      B128 eq{0, 0};
+      const uint8_t l = s.lab[v];
+      for (uint32_t y = 0; y < m; ++y)
+        if (s.lab[y] == l) eq = b_or(eq, b_bit(y));
+      s.same[v] = eq;
+      // symmetry as sets: out-set equals in-set
+      const B128 o = s.adj[v], i = s.in[v];
+      if (o.lo != i.lo || o.hi != i.hi) bad |= kErrAsym;
+    }
+    bad = __reduce_or_sync(0xffffffffu, bad);
+    if (bad && lane == 0) atomicOr(err, bad);
+    __syncwarp();
+    const Rows rows{&s, g.rowp, g.col, start, global_rows};
+    for (uint32_t v = lane; v < m; v += 32) {
+      const uint64_t u = uint64_t(start) + v;
+      const uint32_t lu = s.lab[v];
+      // label signature: +1 per CSR entry on the neighbour's label
+      uint64_t lg = 0;
+      for (uint32_t i = rows.begin(v); i < rows.end(v); ++i) nib_inc(lg, s.lab[rows.at(i)]);
+      // path signature: walks v-a-w (w != v) and v-a-w-x (x != a, x != v)
+      uint64_t p0 = 0, p1 = 0, p2 = 0, p3 = 0;
+      for (B128 ra = s.adj[v]; b_any(ra); ra = b_clear_low(ra)) {
+        const uint32_t a = b_low(ra);
+        const uint32_t la = s.lab[a];
+        for (B128 rw = b_andn(s.adj[a], b_bit(v)); b_any(rw); rw = b_clear_low(rw)) {
+          const uint32_t w = b_low(rw);
+          const uint32_t h2 = hcombine(lu, hcombine(la, s.lab[w]));
+          bloom_insert(p0, p1, p2, p3, fmix32(h2));
+          for (B128 rx = b_andn(s.adj[w], b_or(b_bit(a), b_bit(v))); b_any(rx); rx = b_clear_low(rx)) {
+            const uint32_t x = b_low(rx);
+            bloom_insert(p0, p1, p2, p3, fmix32(hcombine(h2, s.lab[x])));
+          }
+        }
+      }
+      // cycle signature
+      uint32_t c[4] = {0, 0, 0, 0};
+      if (multi) cycles_entries(s, rows, v, c);
+      else cycles_sets(s, v, c);
+      const uint64_t cyc = uint64_t((c[0] & 0xFFFFu) >> 1) | (uint64_t((c[1] & 0xFFFFu) >> 1) << 16) |
+                           (uint64_t((c[2] & 0xFFFFu) >> 1) << 32) | (uint64_t((c[3] & 0xFFFFu) >> 1) << 48);
+      // distance shells 1..R (exact BFS levels); unused steps stay zero
+      uint64_t sh[kMaxSteps];
+      B128 reached = b_bit(v), frontier = reached;
+#pragma unroll
+      for (int k = 0; k < kMaxSteps; ++k) {
+        sh[k] = 0;
+        if (k < out.R) {
+          B128 next{0, 0};
+          for (B128 f = frontier; b_any(f); f = b_clear_low(f)) next = b_or(next, s.adj[b_low(f)]);
+          next = b_andn(next, reached);
+          reached = b_or(reached, next);
+          for (B128 f = next; b_any(f); f = b_clear_low(f)) nib_inc(sh[k], s.lab[b_low(f)]);
+          frontier = next;
+        }
+      }
+      const uint32_t deg = rows.end(v) - rows.begin(v);
+      ulonglong2* rec = reinterpret_cast<ulonglong2*>(out.frec + uint64_t(kRecWords) * u);
+      rec[0] = make_ulonglong2(uint64_t(lu) | (uint64_t(deg) << 32), cyc);
+      rec[1] = make_ulonglong2(p0, p1);
+      rec[2] = make_ulonglong2(p2, p3);
+      rec[3] = make_ulonglong2(sh[0], sh[1]);
+      rec[4] = make_ulonglong2(sh[2], sh[3]);
+      rec[5] = make_ulonglong2(sh[4], sh[5]);
+      rec[6] = make_ulonglong2(sh[6], sh[7]);
+      rec[7] = make_ulonglong2(lg, 0ull);
+      st_b128(out.adj + 2 * u, s.adj[v]);
+    }
+    // per-graph label histogram (labels < 16) and label set
+    uint32_t cnt = 0;
+    if (lane < 16) cnt = b_pop(s.labmask[lane]);
+    const uint32_t nib = lane < 16 ? (cnt > 15 ? 15u : cnt) : 0u;
+    const uint32_t lo = __reduce_or_sync(0xffffffffu, lane < 8 ? nib << (4 * lane) : 0u);
+    const uint32_t hi = __reduce_or_sync(0xffffffffu, (lane >= 8 && lane < 16) ? nib << (4 * (lane - 8)) : 0u);
+    const uint32_t present = __ballot_sync(0xffffffffu, lane < 16 && cnt > 0);
+    if (lane == 0) {
+      out.ghist[gi] = uint64_t(lo) | (uint64_t(hi) << 32);
+      out.glabset[gi] = present & 0xFFFFu;
+    }
+    __syncwarp();
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_signatures(const DGraphs& g, DSigs s, uint32_t max_nodes, uint32_t* err, cudaStream_t st) {
+  if (g.G == 0) return cudaSuccess;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  uint64_t want = (uint64_t(g.G) + kWarps - 1) / kWarps;
+  uint64_t cap = uint64_t(sms > 0 ? sms : 152) * 16;
+  const unsigned blocks = unsigned(want < cap ? want : cap);
+  signatures_kernel<<<blocks, kWarps * 32, 0, st>>>(g, s, max_nodes, err); note_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace bms

@@ -1,0 +1,265 @@
+/*
+ * bms.h — C ABI of the GB300 batched subgraph-isomorphism engine (libbms.so).
+ *
+ * The entry points mirror the reference library's hot path, stage by stage
+ * (AnySparse/BMS2, namespace `sigmo`, header-only SYCL C++20).  The reference
+ * has no FFI of its own: its boundary is a set of C++ templates called from the
+ * driver's main() (library/src/BMS2.cpp:7-393).  Each function below names the
+ * reference interface it replaces.  Conventions:
+ *   - every call returns an int status: BMS_OK (0) or a negative BMS_E* code;
+ *     no C++ exception crosses this boundary; bms_last_error() gives a message;
+ *   - one context per host thread (contexts are independent, a context is not
+ *     re-entrant — the reference is single-threaded with one sycl::queue);
+ *   - input arrays are borrowed for the duration of the call and copied;
+ *   - node ids are global within a batch, as in DeviceBatchedCSRGraph
+ *     (library/include/graph.hpp:58-66).
+ */
+#ifndef BMS_H
+#define BMS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BMS_ABI_VERSION 1
+
+/* Limits of this implementation.  The reference itself is defined for data
+ * graphs of at most 64 nodes and queries of at most 30 nodes (64-bit bitsets,
+ * utils.hpp:90-120, signature.hpp:614; MAX_QUERY_NODES, isomorphism.hpp:248). */
+#define BMS_MAX_DATA_NODES 128u
+#define BMS_MAX_QUERY_NODES 64u
+#define BMS_MAX_REFINE_STEPS 8
+#define BMS_WILDCARD_LABEL 255u       /* types.hpp:18 */
+#define BMS_NULL_NODE 0xFFFFFFFFu     /* types.hpp:22 */
+
+typedef enum {
+  BMS_OK = 0,
+  BMS_EINVAL = -1,       /* bad argument or malformed input (graph.hpp:200 throws) */
+  BMS_ENOMEM = -2,       /* device or host allocation failed */
+  BMS_ECUDA = -3,        /* a CUDA runtime call failed */
+  BMS_EIO = -4,          /* file could not be opened or read */
+  BMS_ESTATE = -5,       /* call out of order (e.g. join before map) */
+  BMS_EUNSUPPORTED = -6, /* input exceeds BMS_MAX_* limits */
+  BMS_ETIMEDOUT = -7,    /* a bounded host wait expired */
+  BMS_EINCOMPLETE = -8,  /* some pairs hit the expansion budget (see status) */
+  BMS_ENODEV = -9        /* no usable CUDA device */
+} bms_status;
+
+typedef enum { BMS_QUERY = 0, BMS_DATA = 1 } bms_kind;
+/* join mode: find-first reports min(count,1) per pair (isomorphism.hpp:298,
+ * default of the reference driver); count-all is the driver's --find-all. */
+typedef enum { BMS_FIND_FIRST = 0, BMS_COUNT_ALL = 1 } bms_mode;
+/* search order: GMCR = query-index order 0..n-1, the only order of the
+ * reference (isomorphism.hpp:414-448); LEARNED = cost-model order. */
+typedef enum { BMS_ORDER_GMCR = 0, BMS_ORDER_LEARNED = 1 } bms_order;
+/* join semantics.  EXACT counts every injective, induced, label-preserving
+ * embedding inside the candidate sets.  REFERENCE_DFS restates the reference
+ * DFS literally, including the visited bit it never clears when a frame
+ * advances (isomorphism.hpp:414-448), with mapping[] reset to NULL per root;
+ * it requires BMS_ORDER_GMCR. */
+typedef enum { BMS_SEM_EXACT = 0, BMS_SEM_REFERENCE_DFS = 1 } bms_semantics;
+
+/* per-pair status codes (bms_get_pair_status) */
+#define BMS_PAIR_DONE 0u
+#define BMS_PAIR_INCOMPLETE 1u /* the expansion budget ran out */
+
+/* ------------------------------------------------------------------ errors */
+/* Last error message of `ctx`, or of the calling thread when ctx is NULL. */
+const char* bms_last_error(const void* ctx);
+const char* bms_status_name(int status);
+int bms_abi_version(void);
+
+/* ------------------------------------------------------- host graph batches */
+/* A host-side batched CSR, the reference's std::vector<CSRGraph> flattened
+ * the way createDeviceCSRGraph flattens it (graph.hpp:251-310). */
+typedef struct bms_graphs bms_graphs;
+typedef struct {
+  uint32_t n_graphs;
+  uint32_t max_nodes;             /* largest graph */
+  uint64_t n_nodes;
+  uint64_t n_entries;             /* CSR entries (two per undirected edge) */
+  const uint32_t* graph_offsets;  /* [n_graphs + 1] */
+  const uint32_t* row_offsets;    /* [n_nodes + 1], global */
+  const uint32_t* column_indices; /* [n_entries], global node ids */
+  const uint8_t* node_labels;     /* [n_nodes] */
+  const uint8_t* edge_labels;     /* [n_entries] */
+} bms_graphs_view;
+
+/* io::loadCSRGraphsFromFile (io.hpp:43-52) + IntermediateGraph(line) and
+ * toCSRGraph() (graph.hpp:147-243): one graph per line,
+ * "n#N l#L {id label}xN e#E {u v [elabel]}xE".  Empty lines are skipped;
+ * a malformed line fails with BMS_EINVAL unless skip_invalid is set, in which
+ * case it is dropped (the batch driver's behaviour, BMS2_batch.cpp:121-124).
+ * max_graphs = 0 means no limit (--max-data-graphs / --max-query-graphs). */
+int bms_graphs_parse_file(const char* path, uint32_t max_graphs, int skip_invalid, bms_graphs** out);
+int bms_graphs_parse_text(const char* text, size_t len, uint32_t max_graphs, int skip_invalid, bms_graphs** out);
+/* Wrap caller CSR arrays (copied).  edge_labels may be NULL (all zero). */
+int bms_graphs_from_csr(uint32_t n_graphs, const uint32_t* graph_offsets, const uint32_t* row_offsets,
+                        const uint32_t* column_indices, const uint8_t* node_labels, const uint8_t* edge_labels,
+                        bms_graphs** out);
+int bms_graphs_view_of(const bms_graphs* g, bms_graphs_view* out);
+/* Write in the reference text format (generate_data.py:74-92 layout). */
+int bms_graphs_write_file(const bms_graphs* g, const char* path);
+/* Keep graphs whose node count is in [min_nodes, max_nodes] (--query-filter,
+ * BMS2.cpp:27-34). */
+int bms_graphs_filter_size(const bms_graphs* g, uint32_t min_nodes, uint32_t max_nodes, bms_graphs** out);
+void bms_graphs_free(bms_graphs* g);
+
+/* ------------------------------------------- seeded synthetic molecular data */
+/* Not part of the reference (its datasets are converted from SMARTS with rdkit,
+ * generate_data.py).  Labels use the reference converter's ids
+ * (generate_data.py:8): N=0 Cl=1 Br=3 O=7 C=8 S=9 F=10. */
+typedef enum { BMS_SIZE_UNIFORM = 0, BMS_SIZE_NORMAL = 1, BMS_SIZE_LOGNORMAL = 2 } bms_size_dist;
+typedef struct {
+  uint32_t n_graphs;
+  uint32_t size_dist;   /* bms_size_dist */
+  double p0, p1;        /* uniform: unused; normal: mean, sd; lognormal: median, sigma */
+  uint32_t min_nodes, max_nodes;
+  uint32_t min_rings, max_rings;
+} bms_mol_params;
+int bms_synth_molecules(const bms_mol_params* p, uint64_t seed, bms_graphs** out);
+
+typedef struct {
+  uint32_t n_queries;
+  uint32_t min_nodes, max_nodes;
+  double frac_carbon;      /* pure-carbon chains and rings */
+  double frac_adversarial; /* fused carbon rings, long chains, halogen stars */
+} bms_query_params;
+/* Queries are connected induced subgraphs of random graphs of `source`,
+ * numbered in random depth-first discovery order. */
+int bms_synth_queries(const bms_query_params* p, const bms_graphs* source, uint64_t seed, bms_graphs** out);
+
+/* --------------------------------------------------------------- contexts */
+typedef struct bms_ctx bms_ctx;
+int bms_create(int device, bms_ctx** out);
+void bms_destroy(bms_ctx* ctx);
+/* Run all work of ctx on `stream` (a cudaStream_t; NULL restores the
+ * context's own stream). */
+int bms_set_stream(bms_ctx* ctx, void* stream);
+/* Per (pair, root) expansion budget of the join; 0 = unlimited (default). */
+int bms_set_expansion_budget(bms_ctx* ctx, uint64_t budget);
+/* Log per-query-vertex expansions in bms_run (count-all, GMCR order, EXACT
+ * semantics only) for bms_vertex_expansions; off by default. */
+int bms_set_logging(bms_ctx* ctx, int vertex_expansions);
+
+/* createDeviceCSRGraph (graph.hpp:251-310): upload a batch as the query or the
+ * data side.  The CSR must be symmetric with column ids inside each graph; the
+ * check runs on the device and is reported by the next stage call. */
+int bms_load_graphs(bms_ctx* ctx, int kind, const bms_graphs* g);
+int bms_load_csr(bms_ctx* ctx, int kind, uint32_t n_graphs, const uint32_t* graph_offsets,
+                 const uint32_t* row_offsets, const uint32_t* column_indices, const uint8_t* node_labels,
+                 const uint8_t* edge_labels);
+
+/* ------------------------------------------------------- staged pipeline */
+/* Signature<>::generate{Data,Query}Signatures (signature.hpp:56-73,124-151),
+ * PathSignature (:455-519), CycleSignature (:574-719) and the distance-shell
+ * refinement refine{Data,Query}Signatures(k) for k = 1..refine_steps
+ * (:335-389), for both sides. */
+int bms_signatures(bms_ctx* ctx, int refine_steps);
+/* filter::filterCandidates (isomorphism.hpp:30-104): dense query-major
+ * candidate bitset, uint32 words, ceil(data_nodes/32) words per query node
+ * (candidates.hpp:10-24). */
+int bms_filter(bms_ctx* ctx);
+/* filter::refineCandidates (isomorphism.hpp:106-203) with shell step k. */
+int bms_refine(bms_ctx* ctx, int step);
+/* mapping::GMCR::generateGMCR (gmcr.hpp:35-144).  Query ids within a data
+ * graph's row are ascending.  *n_pairs receives the number of valid pairs. */
+int bms_map(bms_ctx* ctx, uint64_t* n_pairs);
+/* join::joinCandidates (isomorphism.hpp:291-472) over the mapped pairs.
+ * *total receives the sum of per-pair counts (the driver's "# Matches"). */
+int bms_join(bms_ctx* ctx, int mode, int order, int semantics, uint64_t* total);
+
+/* ------------------------------------------------------- fused pipeline */
+/* Signatures, filter, refine 1..refine_steps, mapping and join in one pass
+ * that never materialises the dense candidate matrix.  Results are identical
+ * to the staged pipeline's.  The persistent join and the filter run as CUDA
+ * kernels on the context's stream. */
+int bms_run(bms_ctx* ctx, int refine_steps, int mode, int order, int semantics, uint64_t* total);
+
+/* ------------------------------------------------------------- results */
+typedef struct {
+  uint32_t n_query_graphs, n_data_graphs;
+  uint64_t n_query_nodes, n_data_nodes;
+  uint64_t n_pairs;          /* query graphs x data graphs */
+  uint64_t n_valid_pairs;    /* GMCR tasks */
+  uint64_t n_incomplete;     /* pairs that hit the expansion budget */
+  uint64_t total_matches;
+  uint64_t expansions;       /* successful assignments in the join, roots included */
+  uint32_t refine_steps;
+  uint32_t last_mode, last_order, last_semantics;
+  /* device time of the last stage calls, milliseconds (CUDA events) */
+  float ms_signatures, ms_filter, ms_refine, ms_map, ms_order, ms_join, ms_total;
+  uint64_t kernel_launches;  /* CUDA kernels launched by the last pipeline call */
+} bms_stats;
+int bms_get_stats(bms_ctx* ctx, bms_stats* out);
+
+/* GMCR as the reference stores it (gmcr.hpp:220-224): data_graph_offsets
+ * [n_data_graphs+1] and query_graph_indices [n_valid_pairs]. */
+int bms_get_gmcr(bms_ctx* ctx, uint32_t* data_graph_offsets, uint32_t* query_graph_indices, uint64_t cap);
+/* Per-pair counts in GMCR order (find-first: 0/1). */
+int bms_get_pair_counts(bms_ctx* ctx, uint64_t* counts, uint64_t cap);
+/* Per-pair expansion counts in GMCR order. */
+int bms_get_pair_expansions(bms_ctx* ctx, uint64_t* expansions, uint64_t cap);
+int bms_get_pair_status(bms_ctx* ctx, uint8_t* status, uint64_t cap);
+/* Candidates::getHostCandidates (candidates.hpp:181-186): the dense matrix,
+ * n_query_nodes x ceil(n_data_nodes/32) uint32 words (staged pipeline only). */
+int bms_get_candidates(bms_ctx* ctx, uint32_t* words, uint64_t cap);
+/* Node signatures of one side.  Any pointer may be NULL.  label_gen[n],
+ * path[4n], cycle[4n] (5-same, 5-diff, 6-same, 6-diff), shells[steps*n]
+ * step-major. */
+int bms_get_signatures(bms_ctx* ctx, int kind, uint64_t* label_gen, uint64_t* path, uint16_t* cycle,
+                       uint64_t* shells);
+
+/* ------------------------------------------------------ learned ordering */
+/* 12 features per query vertex (see bms_feature_names), computed from the
+ * loaded queries and the mapped pairs.  Requires bms_map or bms_run. */
+#define BMS_NUM_FEATURES 12
+#define BMS_MLP_HIDDEN 64
+#define BMS_MLP_PARAMS (64 * 12 + 64 + 64 * 64 + 64 + 64 + 1)
+const char* bms_feature_name(int i);
+int bms_query_features(bms_ctx* ctx, float* features /* [n_query_nodes*12] */);
+/* Per query vertex: total successful assignments at that vertex over all
+ * mapped pairs in the last plain-order (BMS_ORDER_GMCR, BMS_SEM_EXACT) join. */
+int bms_vertex_expansions(bms_ctx* ctx, uint64_t* expansions /* [n_query_nodes] */);
+/* Train the cost model on the GPU with the library's own forward/backward and
+ * Adam kernels: BF16 weights, FP32 accumulation, MSE loss.  x [n*12], y [n].
+ * *final_loss (nullable) receives the last epoch's mean loss. */
+int bms_model_train(bms_ctx* ctx, const float* x, const float* y, uint32_t n, uint32_t epochs, uint32_t batch,
+                    float lr, uint64_t seed, float* final_loss);
+/* One forward+backward on the GPU (for gradient checks): params in the
+ * BMS_MLP_PARAMS layout W1[64x12] b1 W2[64x64] b2 w3 b3; outputs y[n] and
+ * grad[BMS_MLP_PARAMS]. */
+int bms_model_grad(bms_ctx* ctx, const float* params, const float* x, const float* y_target, uint32_t n,
+                   float* y_out, float* grad, float* loss);
+int bms_model_get(bms_ctx* ctx, float* params);
+int bms_model_set(bms_ctx* ctx, const float* params);
+int bms_model_save(bms_ctx* ctx, const char* path);
+int bms_model_load(bms_ctx* ctx, const char* path);
+/* Predicted log2 expansion cost per query vertex and the resulting per-query
+ * order (order[n_query_nodes], local vertex ids, query by query). */
+int bms_model_predict(bms_ctx* ctx, float* cost, uint8_t* order);
+
+/* ------------------------------------------------------------ scheduling */
+/* Size-bucketed schedule of the persistent join.  Buckets are keyed by the
+ * query's node count class; each entry picks lanes cooperating per task and the
+ * DFS split depth.  bms_autotune times candidate schedules on the loaded
+ * workload and installs the fastest per bucket. */
+#define BMS_SCHED_BUCKETS 4
+typedef struct {
+  uint32_t max_query_nodes[BMS_SCHED_BUCKETS]; /* bucket upper bounds */
+  uint32_t split_depth[BMS_SCHED_BUCKETS];     /* 1 = (pair, root) tasks, 2 = (pair, root, second) */
+  uint32_t blocks_per_sm[BMS_SCHED_BUCKETS];
+  uint32_t warps_per_block[BMS_SCHED_BUCKETS];
+  float ms[BMS_SCHED_BUCKETS];                 /* measured by the autotuner */
+} bms_schedule;
+int bms_get_schedule(bms_ctx* ctx, bms_schedule* out);
+int bms_set_schedule(bms_ctx* ctx, const bms_schedule* s);
+int bms_autotune(bms_ctx* ctx, int refine_steps, int mode, int order, bms_schedule* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BMS_H */

@@ -1,0 +1,621 @@
+// CPU oracle for the bms2_gb300 subgraph-isomorphism path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the checker: the pytest suite,
+// __graft_entry__.smoke() and bench.py's CPU-baseline leg load it to compute the
+// expected results.  The product (libbms.so) never links, loads or calls it.
+//
+// What it restates: the reference AnySparse/BMS2 (namespace `sigmo`) hot path,
+// one plain C++ loop per reference kernel, following the reference's loops:
+//   - label signature generation     signature.hpp:124-151  (orc_signatures, label_gen)
+//   - path (Bloom) signature         signature.hpp:393-437, 472-519
+//   - cycle signature                signature.hpp:535-555, 591-719
+//   - distance-shell refinement      signature.hpp:335-389 (PowerGraph CSR)
+//   - filter                         isomorphism.hpp:30-104
+//   - refine                         isomorphism.hpp:106-203
+//   - candidate range count / select candidates.hpp:82-158
+//   - GMCR mapping                   gmcr.hpp:35-144
+//   - join                           isomorphism.hpp:268-288, 291-472
+//
+// Parity status: the reference cannot be built in this environment (SYCL
+// compiler and runtime, MPI and a network fetch of cxxopts are required; g++
+// rejects signature.hpp:212,249,297,335 and isomorphism.hpp:866 is a syntax
+// error) and it ships no tests, fixtures or golden vectors.  Parity is therefore
+// UNPINNED BY THE REFERENCE ITSELF.  This oracle is pinned instead by
+// hand-derived known-answer tests and by an independent networkx cross-check of
+// the exact embedding counts (tests/golden/).
+//
+// Two switches select how the reference's undefined or defective behaviour is read:
+//   x86      = 1 emulates what the reference computes on an x86 CPU device outside
+//              its 64-node domain: 64-bit bitsets indexed by (local id & 63), cycle
+//              signatures forced to zero for graphs above 64 nodes (signature.hpp:614)
+//              and the 128-entry cycle stack that drops pushes (signature.hpp:638,697).
+//              x86 = 0 ("generalized") uses bitsets wide enough for the graph and no
+//              size cut-offs.  Both readings agree on graphs of at most 64 nodes whose
+//              degree is at most 25.
+//   dfs_literal = 1 restates the reference join DFS verbatim, including its defect:
+//              a frame that advances to its next candidate never clears the visited
+//              bit of the previous one, and an exhausted frame clears the bit of
+//              mapping[k] even when it assigned nothing (isomorphism.hpp:414-448).
+//              mapping[] is reset to NULL_NODE per root (the reference leaves it
+//              uninitialised and carries it across roots and tasks, which depends on
+//              the work-item schedule; NULL is the only deterministic reading).
+//              dfs_literal = 0 ("exact") clears each candidate's bit when the frame
+//              moves on, which counts every injective induced embedding.
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+constexpr uint8_t kWildcard = 255;  // types.hpp:18
+constexpr uint32_t kNullNode = 0xFFFFFFFFu;  // types.hpp:22
+
+// ---------------------------------------------------------------- nibbles
+// Signature<PowerGraph,4>::SignatureDevice (signature.hpp:22-53): 16 saturating
+// 4-bit label counters in one uint64; labels >= 16 are ignored.
+inline unsigned nib_get(uint64_t s, unsigned l) { return l < 16 ? unsigned((s >> (4 * l)) & 15u) : 0u; }
+inline void nib_inc(uint64_t& s, unsigned l) {
+  if (l >= 16) return;
+  unsigned c = nib_get(s, l);
+  if (c < 15) s = (s & ~(uint64_t(15) << (4 * l))) | (uint64_t(c + 1) << (4 * l));
+}
+
+// ---------------------------------------------------------------- hashes
+// signature.hpp:393-404: MurmurHash3 fmix32 finalizer and a boost-style combine.
+inline uint32_t fmix32(uint32_t h) {
+  h ^= h >> 16;
+  h *= 0x85ebca6bu;
+  h ^= h >> 13;
+  h *= 0xc2b2ae35u;
+  h ^= h >> 16;
+  return h;
+}
+inline uint32_t hcombine(uint32_t a, uint32_t b) { return a ^ (b + 0x9e3779b9u + (a << 6) + (a >> 2)); }
+// PathSignatureDevice::insert (signature.hpp:418-430): three bits of a 256-bit filter.
+inline void bloom_insert(uint64_t* bits, uint32_t v) {
+  uint32_t h1 = v, h2 = fmix32(h1), h3 = fmix32(h2);
+  bits[(h1 & 255u) >> 6] |= uint64_t(1) << (h1 & 63u);
+  bits[(h2 & 255u) >> 6] |= uint64_t(1) << (h2 & 63u);
+  bits[(h3 & 255u) >> 6] |= uint64_t(1) << (h3 & 63u);
+}
+
+struct Batch {
+  uint32_t G;
+  const uint32_t* goff;
+  const uint32_t* rowp;
+  const uint32_t* col;
+  const uint8_t* lab;
+  uint64_t nodes() const { return goff[G]; }
+};
+
+// graph id of every node (DeviceBatchedCSRGraph::getGraphID, graph.hpp:96-107)
+std::vector<uint32_t> graph_of_nodes(const Batch& b) {
+  std::vector<uint32_t> g(b.nodes());
+  for (uint32_t i = 0; i < b.G; ++i)
+    for (uint32_t v = b.goff[i]; v < b.goff[i + 1]; ++v) g[v] = i;
+  return g;
+}
+
+// Simple growable bitset over local node ids.
+struct Bits {
+  std::vector<uint64_t> w;
+  explicit Bits(size_t n = 64) : w((n + 63) / 64 ? (n + 63) / 64 : 1, 0) {}
+  bool get(size_t i) const { return (w[i >> 6] >> (i & 63)) & 1u; }
+  void set(size_t i) { w[i >> 6] |= uint64_t(1) << (i & 63); }
+  void clr(size_t i) { w[i >> 6] &= ~(uint64_t(1) << (i & 63)); }
+};
+
+// ---------------------------------------------------------------- label signature
+// signature.hpp:124-151: +1 per CSR entry on the neighbour's label.
+uint64_t label_gen_one(const Batch& b, uint32_t u) {
+  uint64_t s = 0;
+  for (uint32_t i = b.rowp[u]; i < b.rowp[u + 1]; ++i) nib_inc(s, b.lab[b.col[i]]);
+  return s;
+}
+
+// ---------------------------------------------------------------- path signature
+// signature.hpp:472-519: label walks u-v-w (w != u) and u-v-w-x (x != v, x != u).
+void path_one(const Batch& b, uint32_t u, uint64_t* out) {
+  out[0] = out[1] = out[2] = out[3] = 0;
+  uint32_t lu = b.lab[u];
+  for (uint32_t i = b.rowp[u]; i < b.rowp[u + 1]; ++i) {
+    uint32_t v = b.col[i];
+    uint32_t lv = b.lab[v];
+    for (uint32_t j = b.rowp[v]; j < b.rowp[v + 1]; ++j) {
+      uint32_t w = b.col[j];
+      if (w == u) continue;
+      uint32_t lw = b.lab[w];
+      uint32_t h2 = hcombine(lu, hcombine(lv, lw));
+      bloom_insert(out, fmix32(h2));
+      for (uint32_t k = b.rowp[w]; k < b.rowp[w + 1]; ++k) {
+        uint32_t x = b.col[k];
+        if (x == v || x == u) continue;
+        bloom_insert(out, fmix32(hcombine(h2, b.lab[x])));
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- cycle signature
+// signature.hpp:591-719: LIFO DFS over simple paths from u; at depth 4 (5) every
+// CSR entry of the current node equal to u adds a 5-ring (6-ring) closure,
+// "same" iff every node after u on the path carries u's label.  Counters are
+// uint16 and halved at the end.
+void cycle_one(const Batch& b, uint32_t u, uint32_t gstart, uint32_t m, bool x86, uint16_t* out) {
+  out[0] = out[1] = out[2] = out[3] = 0;
+  if (x86 && m > 64) return;  // signature.hpp:614
+  struct Frame {
+    uint32_t node, depth, same;
+    Bits mask;
+  };
+  std::vector<Frame> st;
+  const size_t cap = x86 ? 128 : SIZE_MAX;
+  uint32_t lu = b.lab[u];
+  uint32_t ul = u - gstart;
+  uint16_t c5s = 0, c5d = 0, c6s = 0, c6d = 0;
+  for (uint32_t i = b.rowp[u]; i < b.rowp[u + 1]; ++i) {
+    uint32_t nb = b.col[i];
+    if (st.size() < cap) {
+      Frame f{nb - gstart, 1, b.lab[nb] == lu ? 1u : 0u, Bits(m)};
+      f.mask.set(ul);
+      f.mask.set(nb - gstart);
+      st.push_back(std::move(f));
+    }
+  }
+  while (!st.empty()) {
+    Frame f = std::move(st.back());
+    st.pop_back();
+    uint32_t cur = f.node + gstart;
+    if (f.depth == 4 || f.depth == 5) {
+      for (uint32_t i = b.rowp[cur]; i < b.rowp[cur + 1]; ++i) {
+        if (b.col[i] == u) {
+          if (f.depth == 4) {
+            if (f.same) ++c5s; else ++c5d;
+          } else {
+            if (f.same) ++c6s; else ++c6d;
+          }
+        }
+      }
+    }
+    if (f.depth < 5) {
+      for (uint32_t i = b.rowp[cur]; i < b.rowp[cur + 1]; ++i) {
+        uint32_t nb = b.col[i];
+        if (nb == u) continue;
+        uint32_t nl = nb - gstart;
+        if (!f.mask.get(nl)) {
+          if (st.size() < cap) {
+            Frame g{nl, f.depth + 1, (f.same && b.lab[nb] == lu) ? 1u : 0u, f.mask};
+            g.mask.set(nl);
+            st.push_back(std::move(g));
+          }
+        }
+      }
+    }
+  }
+  out[0] = uint16_t(c5s / 2);
+  out[1] = uint16_t(c5d / 2);
+  out[2] = uint16_t(c6s / 2);
+  out[3] = uint16_t(c6d / 2);
+}
+
+// ---------------------------------------------------------------- shell signatures
+// signature.hpp:335-389 applied for k = 1..R: S_k(u) = saturating label histogram
+// of the nodes at exact BFS distance k.  `old` (the reference's reachables) starts
+// at zero.  With x86 = 1 the bitsets are a single uint64 indexed by (local & 63)
+// and set bits are read back as local ids 0..63, as on x86 where a 64-bit shift
+// count is taken modulo 64 (utils.hpp:95-97).
+void shells_one(const Batch& b, uint32_t u, uint32_t gstart, uint32_t m, int R, bool x86, uint64_t* out, uint64_t stride) {
+  if (x86) {
+    uint64_t old = 0;
+    const uint32_t ul = (u - gstart) & 63u;
+    for (int k = 1; k <= R; ++k) {
+      uint64_t frontier = uint64_t(1) << ul, reach = frontier;
+      for (int it = 0; it < k && frontier; ++it) {
+        uint64_t next = 0;
+        for (uint64_t f = frontier; f; f &= f - 1) {
+          uint32_t node = uint32_t(__builtin_ctzll(f)) + gstart;
+          for (uint32_t i = b.rowp[node]; i < b.rowp[node + 1]; ++i) {
+            uint32_t nl = (b.col[i] - gstart) & 63u;
+            if (!((reach >> nl) & 1u)) {
+              reach |= uint64_t(1) << nl;
+              next |= uint64_t(1) << nl;
+            }
+          }
+        }
+        frontier = next;
+      }
+      reach &= ~(uint64_t(1) << ul);
+      reach &= ~old;
+      uint64_t s = 0;
+      for (uint64_t r = reach; r; r &= r - 1) nib_inc(s, b.lab[uint32_t(__builtin_ctzll(r)) + gstart]);
+      out[uint64_t(k - 1) * stride] = s;
+      old |= reach;
+    }
+    return;
+  }
+  // generalized: one BFS, level k is the exact-distance-k shell.
+  std::vector<int> dist(m, -1);
+  std::vector<uint32_t> frontier{u - gstart}, next;
+  dist[u - gstart] = 0;
+  for (int k = 1; k <= R; ++k) {
+    next.clear();
+    uint64_t s = 0;
+    for (uint32_t fl : frontier) {
+      uint32_t node = fl + gstart;
+      for (uint32_t i = b.rowp[node]; i < b.rowp[node + 1]; ++i) {
+        uint32_t nl = b.col[i] - gstart;
+        if (dist[nl] < 0) {
+          dist[nl] = k;
+          next.push_back(nl);
+          nib_inc(s, b.lab[b.col[i]]);
+        }
+      }
+    }
+    out[uint64_t(k - 1) * stride] = s;
+    frontier.swap(next);
+  }
+}
+
+// ---------------------------------------------------------------- candidates
+inline uint64_t words_per_row(uint64_t dn) { return (dn + 31) / 32; }
+
+// Candidates::getCandidatesCount(source, start, end) (candidates.hpp:82-100),
+// read as the exact popcount of bits [start, end).
+uint32_t range_count(const uint32_t* row, uint32_t start, uint32_t end) {
+  uint32_t c = 0;
+  for (uint32_t v = start; v < end;) {
+    uint32_t w = v >> 5, lo = v & 31u;
+    uint32_t hi = std::min<uint32_t>(32u, lo + (end - v));
+    uint32_t word = row[w] >> lo;
+    if (hi - lo < 32) word &= (1u << (hi - lo)) - 1u;
+    c += uint32_t(__builtin_popcount(word));
+    v += hi - lo;
+  }
+  return c;
+}
+// Candidates::getCandidateAt(source, idx, start, end) (candidates.hpp:128-158):
+// the idx-th candidate of the range in ascending node order, or NULL_NODE.
+uint32_t range_select(const uint32_t* row, uint32_t idx, uint32_t start, uint32_t end) {
+  uint32_t c = 0;
+  for (uint32_t v = start; v < end; ++v)
+    if ((row[v >> 5] >> (v & 31u)) & 1u) {
+      if (c == idx) return v;
+      ++c;
+    }
+  return kNullNode;
+}
+
+// DeviceBatchedCSRGraph::isNeighbor (graph.hpp:68-73): linear CSR scan.
+inline bool csr_has(const uint32_t* rowp, const uint32_t* col, uint32_t u, uint32_t v) {
+  for (uint32_t i = rowp[u]; i < rowp[u + 1]; ++i)
+    if (col[i] == v) return true;
+  return false;
+}
+
+int nthreads_or_default(int t) {
+#ifdef _OPENMP
+  return t > 0 ? t : omp_get_max_threads();
+#else
+  (void)t;
+  return 1;
+#endif
+}
+
+}  // namespace
+
+extern "C" {
+
+// Number of uint32 candidate words per query-node row (Candidates::single_node_size).
+uint64_t orc_words_per_row(uint64_t data_nodes) { return words_per_row(data_nodes); }
+
+// All node signatures of one batch (data or query graphs).  Any output may be
+// null.  shells is laid out step-major: shells[(k-1)*N + v].
+int orc_signatures(uint32_t G, const uint32_t* goff, const uint32_t* rowp, const uint32_t* col, const uint8_t* lab,
+                   int R, int x86, int threads, uint64_t* label_gen, uint64_t* path, uint16_t* cycle, uint64_t* shells) {
+  Batch b{G, goff, rowp, col, lab};
+  const uint64_t N = b.nodes();
+  std::vector<uint32_t> gid = graph_of_nodes(b);
+  const int nt = nthreads_or_default(threads);
+  (void)nt;
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nt)
+  for (int64_t vi = 0; vi < int64_t(N); ++vi) {
+    uint32_t v = uint32_t(vi);
+    uint32_t g = gid[v];
+    uint32_t gs = goff[g], m = goff[g + 1] - goff[g];
+    if (label_gen) label_gen[v] = label_gen_one(b, v);
+    if (path) path_one(b, v, path + 4 * uint64_t(v));
+    if (cycle) cycle_one(b, v, gs, m, x86 != 0, cycle + 4 * uint64_t(v));
+    if (shells && R > 0) shells_one(b, v, gs, m, R, x86 != 0, shells + v, N);
+  }
+  return 0;
+}
+
+// filter::filterCandidates (isomorphism.hpp:30-104).  cand is Qn x W uint32,
+// query-major, and is fully overwritten.
+int orc_filter(uint64_t Qn, const uint32_t* q_rowp, const uint8_t* q_lab, const uint64_t* q_path, const uint16_t* q_cyc,
+               uint64_t Dn, const uint32_t* d_rowp, const uint8_t* d_lab, const uint64_t* d_path, const uint16_t* d_cyc,
+               int threads, uint32_t* cand) {
+  const uint64_t W = words_per_row(Dn);
+  const int nt = nthreads_or_default(threads);
+  (void)nt;
+#pragma omp parallel for schedule(static) num_threads(nt)
+  for (int64_t ui = 0; ui < int64_t(Qn); ++ui) {
+    uint64_t u = uint64_t(ui);
+    uint32_t* row = cand + u * W;
+    std::memset(row, 0, W * 4);
+    const uint32_t qdeg = q_rowp[u + 1] - q_rowp[u];
+    const uint64_t* qp = q_path + 4 * u;
+    const uint16_t* qc = q_cyc + 4 * u;
+    for (uint64_t v = 0; v < Dn; ++v) {
+      if (q_lab[u] != d_lab[v] && q_lab[u] != kWildcard) continue;
+      if (qdeg > d_rowp[v + 1] - d_rowp[v]) continue;
+      const uint64_t* dp = d_path + 4 * v;
+      bool ok = true;
+      for (int i = 0; i < 4; ++i) ok = ok && ((dp[i] & qp[i]) == qp[i]);
+      if (!ok) continue;
+      const uint16_t* dc = d_cyc + 4 * v;
+      if (!(dc[0] >= qc[0] && dc[1] >= qc[1] && dc[2] >= qc[2] && dc[3] >= qc[3])) continue;
+      row[v >> 5] |= 1u << (v & 31u);
+    }
+  }
+  return 0;
+}
+
+// filter::refineCandidates (isomorphism.hpp:106-203) for one step: keep bit (u,v)
+// iff every nibble of S_k(u) is <= the same nibble of S_k(v).
+int orc_refine(uint64_t Qn, const uint64_t* q_shell, uint64_t Dn, const uint64_t* d_shell, int threads, uint32_t* cand) {
+  const uint64_t W = words_per_row(Dn);
+  const int nt = nthreads_or_default(threads);
+  (void)nt;
+#pragma omp parallel for schedule(static) num_threads(nt)
+  for (int64_t ui = 0; ui < int64_t(Qn); ++ui) {
+    uint64_t u = uint64_t(ui);
+    const uint64_t qs = q_shell[u];
+    for (uint64_t w = 0; w < W; ++w) {
+      uint32_t blk = cand[u * W + w];
+      uint32_t nb = blk;
+      for (uint32_t bits = blk; bits; bits &= bits - 1) {
+        uint32_t bit = uint32_t(__builtin_ctz(bits));
+        uint64_t v = w * 32 + bit;
+        bool keep = v < Dn;
+        if (keep) {
+          const uint64_t ds = d_shell[v];
+          for (unsigned l = 0; l < 16 && keep; ++l) keep = nib_get(qs, l) <= nib_get(ds, l);
+        }
+        if (!keep) nb &= ~(1u << bit);
+      }
+      cand[u * W + w] = nb;
+    }
+  }
+  return 0;
+}
+
+// mapping::GMCR::generateGMCR (gmcr.hpp:35-144).  Valid iff the query has more
+// than one node and every query node has a candidate inside the data graph.
+// Rows list query ids in ascending order (the reference's atomic scatter leaves
+// the order unspecified).  Returns the pair total in *total; qidx may be null to
+// only count, otherwise it must hold `cap` entries.
+int orc_gmcr(uint32_t Qg, const uint32_t* q_goff, uint32_t Dg, const uint32_t* d_goff, uint64_t Dn, const uint32_t* cand,
+             int threads, uint32_t* offsets, uint32_t* qidx, uint64_t cap, uint64_t* total) {
+  const uint64_t W = words_per_row(Dn);
+  std::vector<uint8_t> valid(uint64_t(Qg) * Dg, 0);
+  const int nt = nthreads_or_default(threads);
+  (void)nt;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nt)
+  for (int64_t di = 0; di < int64_t(Dg); ++di) {
+    uint32_t d = uint32_t(di);
+    for (uint32_t q = 0; q < Qg; ++q) {
+      uint32_t n = q_goff[q + 1] - q_goff[q];
+      bool ok = n > 1;
+      for (uint32_t i = 0; i < n && ok; ++i) ok = range_count(cand + (q_goff[q] + i) * W, d_goff[d], d_goff[d + 1]) > 0;
+      valid[uint64_t(q) * Dg + d] = ok;
+    }
+  }
+  uint64_t t = 0;
+  offsets[0] = 0;
+  for (uint32_t d = 0; d < Dg; ++d) {
+    for (uint32_t q = 0; q < Qg; ++q)
+      if (valid[uint64_t(q) * Dg + d]) {
+        if (qidx) {
+          if (t >= cap) return -1;
+          qidx[t] = q;
+        }
+        ++t;
+      }
+    offsets[d + 1] = uint32_t(t);
+  }
+  *total = t;
+  return 0;
+}
+
+// join::joinCandidates (isomorphism.hpp:291-472) per GMCR task.  counts[t] is the
+// embedding count of task t (find_first: 0 or 1).  expansions (nullable) receives
+// the number of successful assignments per task, root included.
+int orc_join(uint32_t Qg, const uint32_t* q_goff, const uint32_t* q_rowp, const uint32_t* q_col,
+             uint32_t Dg, const uint32_t* d_goff, const uint32_t* d_rowp, const uint32_t* d_col,
+             uint64_t Dn, const uint32_t* cand, const uint32_t* offsets, const uint32_t* qidx,
+             int find_first, int x86, int dfs_literal, int threads, uint64_t* counts, uint64_t* expansions) {
+  (void)Qg;
+  const uint64_t W = words_per_row(Dn);
+  const uint64_t T = offsets[Dg];
+  const int nt = nthreads_or_default(threads);
+  (void)nt;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+  for (uint32_t d = 0; d < Dg; ++d) {
+    const uint32_t start = d_goff[d], end = d_goff[d + 1], m = end - start;
+    for (uint32_t t = offsets[d]; t < offsets[d + 1]; ++t) {
+      const uint32_t q = qidx[t];
+      const uint32_t qoff = q_goff[q], n = q_goff[q + 1] - qoff;
+      std::vector<uint32_t> cnt(n);
+      std::vector<uint64_t> mask(n, 0);
+      bool possible = true;
+      for (uint32_t i = 0; i < n; ++i) {
+        cnt[i] = range_count(cand + (qoff + i) * W, start, end);
+        if (cnt[i] == 0) {
+          possible = false;
+          break;
+        }
+        for (uint32_t j = 0; j < i; ++j)
+          if (csr_has(q_rowp, q_col, qoff + i, qoff + j)) mask[i] |= uint64_t(1) << j;
+      }
+      uint64_t total = 0, exps = 0;
+      if (possible) {
+        struct Fr {
+          uint32_t depth, idx;
+        };
+        std::vector<uint32_t> map(n);
+        std::vector<Fr> st(n + 1);
+        for (uint32_t c = 0; c < cnt[0]; ++c) {
+          // visited bitset (utils.hpp:90-120, offset = start of the data graph)
+          Bits vis(x86 ? 64 : m);
+          auto vbit = [&](uint32_t node) -> int64_t {
+            if (node == kNullNode) return -1;
+            if (x86) return int64_t((node - start) & 63u);
+            if (node < start || node >= end) return -1;
+            return int64_t(node - start);
+          };
+          std::fill(map.begin(), map.end(), kNullNode);
+          map[0] = range_select(cand + qoff * W, c, start, end);
+          vis.set(size_t(vbit(map[0])));
+          ++exps;
+          uint32_t top = 0;
+          st[top++] = {1, 0};
+          uint64_t found = 0;
+          while (top > 0) {
+            Fr fr = st[top - 1];
+            const uint32_t qn = fr.depth;
+            if (qn == n) {
+              ++found;
+              --top;
+              if (!dfs_literal) {
+                int64_t bb = vbit(map[n - 1]);
+                if (bb >= 0) vis.clr(size_t(bb));
+              }
+              if (find_first) break;
+              continue;
+            }
+            if (fr.idx >= cnt[qn]) {
+              --top;
+              if (dfs_literal) {
+                int64_t bb = vbit(map[qn]);
+                if (bb >= 0) vis.clr(size_t(bb));
+              }
+              // exact: the frame below clears its own candidate on advance
+              if (!dfs_literal && top > 0) {
+                int64_t bb = vbit(map[qn - 1]);
+                if (bb >= 0 && qn - 1 > 0) vis.clr(size_t(bb));
+              }
+              continue;
+            }
+            const uint32_t v = range_select(cand + (qoff + qn) * W, fr.idx, start, end);
+            st[top - 1].idx++;
+            if (vis.get(size_t(vbit(v)))) continue;
+            bool ok = true;
+            for (uint32_t i = 0; i < qn && ok; ++i) {
+              bool qa = (mask[qn] >> i) & 1u;
+              ok = (qa == csr_has(d_rowp, d_col, map[i], v));
+            }
+            if (ok) {
+              map[qn] = v;
+              vis.set(size_t(vbit(v)));
+              ++exps;
+              st[top++] = {qn + 1, 0};
+            }
+          }
+          total += found;
+          if (find_first && found) break;
+        }
+      }
+      counts[t] = find_first ? (total ? 1 : 0) : total;
+      if (expansions) expansions[t] = exps;
+    }
+  }
+  (void)T;
+  return 0;
+}
+
+// ---------------------------------------------------------------- MLP oracle
+// Learned-order cost model (no reference counterpart): 12 -> 64 -> 64 -> 1, ReLU,
+// weights rounded to bfloat16 (round-to-nearest-even), fp32 accumulation.
+static inline float bf16_round(float x) {
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  if ((u & 0x7f800000u) == 0x7f800000u) return x;
+  uint32_t lsb = (u >> 16) & 1u;
+  u += 0x7fffu + lsb;
+  u &= 0xffff0000u;
+  float r;
+  std::memcpy(&r, &u, 4);
+  return r;
+}
+
+// Forward + backward of mean-squared error over a batch.  Weights are fp32
+// masters (W1[64x12], b1[64], W2[64x64], b2[64], w3[64], b3[1]); the forward and
+// backward use their bf16-rounded values.  Gradients are written to g_* (same
+// shapes), predictions to y (nullable).  Returns the loss.
+float orc_mlp_grad(int B, const float* X, const float* target, const float* W1, const float* b1, const float* W2,
+                   const float* b2, const float* w3, const float* b3, float* y, float* gW1, float* gb1, float* gW2,
+                   float* gb2, float* gw3, float* gb3) {
+  float rW1[64 * 12], rW2[64 * 64], rw3[64], rb1[64], rb2[64], rb3 = bf16_round(b3[0]);
+  for (int i = 0; i < 64 * 12; ++i) rW1[i] = bf16_round(W1[i]);
+  for (int i = 0; i < 64 * 64; ++i) rW2[i] = bf16_round(W2[i]);
+  for (int i = 0; i < 64; ++i) {
+    rw3[i] = bf16_round(w3[i]);
+    rb1[i] = bf16_round(b1[i]);
+    rb2[i] = bf16_round(b2[i]);
+  }
+  std::memset(gW1, 0, sizeof(float) * 64 * 12);
+  std::memset(gW2, 0, sizeof(float) * 64 * 64);
+  std::memset(gb1, 0, sizeof(float) * 64);
+  std::memset(gb2, 0, sizeof(float) * 64);
+  std::memset(gw3, 0, sizeof(float) * 64);
+  gb3[0] = 0.f;
+  double loss = 0.0;
+  for (int s = 0; s < B; ++s) {
+    const float* x = X + 12 * s;
+    float h1[64], h2[64];
+    for (int j = 0; j < 64; ++j) {
+      float a = rb1[j];
+      for (int i = 0; i < 12; ++i) a += rW1[j * 12 + i] * x[i];
+      h1[j] = a > 0.f ? a : 0.f;
+    }
+    for (int j = 0; j < 64; ++j) {
+      float a = rb2[j];
+      for (int i = 0; i < 64; ++i) a += rW2[j * 64 + i] * h1[i];
+      h2[j] = a > 0.f ? a : 0.f;
+    }
+    float o = rb3;
+    for (int i = 0; i < 64; ++i) o += rw3[i] * h2[i];
+    if (y) y[s] = o;
+    float e = o - target[s];
+    loss += double(e) * e;
+    float dy = 2.f * e / float(B);
+    gb3[0] += dy;
+    float dh2[64], dh1[64];
+    for (int i = 0; i < 64; ++i) {
+      gw3[i] += dy * h2[i];
+      dh2[i] = h2[i] > 0.f ? dy * rw3[i] : 0.f;
+    }
+    for (int i = 0; i < 64; ++i) dh1[i] = 0.f;
+    for (int j = 0; j < 64; ++j) {
+      gb2[j] += dh2[j];
+      for (int i = 0; i < 64; ++i) {
+        gW2[j * 64 + i] += dh2[j] * h1[i];
+        dh1[i] += dh2[j] * rW2[j * 64 + i];
+      }
+    }
+    for (int j = 0; j < 64; ++j) {
+      float g = h1[j] > 0.f ? dh1[j] : 0.f;
+      gb1[j] += g;
+      for (int i = 0; i < 12; ++i) gW1[j * 12 + i] += g * x[i];
+    }
+  }
+  return float(loss / B);
+}
+
+}  // extern "C"

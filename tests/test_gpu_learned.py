@@ -1,0 +1,112 @@
+"""Learned query-vertex order: GPU MLP kernels against the CPU oracle, training,
+and bit-exact counts under the learned order."""
+import numpy as np
+import pytest
+
+import oracle
+from bms2_gb300 import COUNT_ALL, DATA, FIND_FIRST, ORDER_GMCR, ORDER_LEARNED, QUERY, SEM_EXACT, BmsError, workloads
+from bms2_gb300.native import MLP_PARAMS
+from bms2_gb300.train import collect, train
+
+pytestmark = pytest.mark.gpu
+
+
+def rand_params(seed):
+    r = np.random.default_rng(seed)
+    p = np.zeros(MLP_PARAMS, np.float32)
+    p[:768] = r.uniform(-0.7, 0.7, 768)
+    p[768:832] = r.uniform(-0.1, 0.1, 64)
+    p[832:4928] = r.uniform(-0.3, 0.3, 4096)
+    p[4928:4992] = r.uniform(-0.1, 0.1, 64)
+    p[4992:5056] = r.uniform(-0.3, 0.3, 64)
+    p[5056] = 0.25
+    return p
+
+
+@pytest.mark.parametrize("n", [1, 31, 32, 100, 257])
+def test_mlp_forward_backward_match_cpu_oracle(ctx, n):
+    # bf16-rounded weights, fp32 accumulation: only the summation order differs
+    r = np.random.default_rng(n)
+    p = rand_params(n)
+    x = r.uniform(0, 2, (n, 12)).astype(np.float32)
+    y = r.uniform(0, 8, n).astype(np.float32)
+    yg, gg, lg = ctx.model_grad(p, x, y)
+    yo, go, lo = oracle.mlp_grad(p, x, y)
+    np.testing.assert_allclose(yg, yo, rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(lg, lo, rtol=1e-4)
+    np.testing.assert_allclose(gg, go, rtol=1e-3, atol=2e-5)
+
+
+def test_training_fits_a_smooth_target(ctx):
+    r = np.random.default_rng(7)
+    x = r.uniform(0, 1, (2048, 12)).astype(np.float32)
+    y = (2.0 * x[:, 0] + np.sin(3 * x[:, 1]) + x[:, 2] * x[:, 3] + 1.0).astype(np.float32)
+    from bms2_gb300 import Context
+
+    c = Context(0)
+    base = float(np.mean((y - y.mean()) ** 2))
+    loss = c.model_train(x, y, epochs=60, batch=128, lr=3e-3, seed=3)
+    assert loss < 0.1 * base
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def trained(ctx):
+    q, d = workloads.make("mol100k", 11, n_data=4000, n_queries=80)
+    ctx.load(QUERY, q)
+    ctx.load(DATA, d)
+    x, y = collect(ctx, 6)
+    assert len(y) > 100 and np.isfinite(x).all() and np.isfinite(y).all()
+    loss = train(ctx, x, y, seed=5, epochs=80)
+    return ctx.model_get(), loss, float(np.var(y))
+
+
+def test_trained_model_beats_constant_predictor(trained):
+    _, loss, var = trained
+    assert loss < 0.8 * var
+
+
+def test_learned_order_keeps_counts_bit_exact(ctx, trained):
+    q, d = workloads.make("mol100k", 12, n_data=3000, n_queries=60)
+    ctx.load(QUERY, q)
+    ctx.load(DATA, d)
+    for mode in (COUNT_ALL, FIND_FIRST):
+        plain = ctx.run(6, mode, ORDER_GMCR, SEM_EXACT)
+        pc = ctx.pair_counts().copy()
+        learned = ctx.run(6, mode, ORDER_LEARNED, SEM_EXACT)
+        assert learned == plain
+        assert np.array_equal(ctx.pair_counts(), pc)
+    want = oracle.run_pipeline(q, d, 6, keep_steps=False)
+    assert ctx.run(6, COUNT_ALL, ORDER_LEARNED, SEM_EXACT) == want.total
+
+
+def test_learned_orders_are_permutations(ctx, trained):
+    q, d = workloads.make("mol1k", 13, n_data=300, n_queries=30)
+    ctx.load(QUERY, q)
+    ctx.load(DATA, d)
+    ctx.run(2, COUNT_ALL, ORDER_GMCR, SEM_EXACT)
+    cost, order = ctx.model_predict()
+    goff = q.arrays()["graph_offsets"]
+    for g in range(len(goff) - 1):
+        s, e = goff[g], goff[g + 1]
+        assert sorted(order[s:e].tolist()) == list(range(e - s))
+    assert np.isfinite(cost).all()
+
+
+def test_model_save_load_round_trip(ctx, trained, tmp_path):
+    p, _, _ = trained
+    ctx.model_save(tmp_path / "m.bin")
+    ctx.model_set(np.zeros_like(p))
+    ctx.model_load(tmp_path / "m.bin")
+    assert np.array_equal(ctx.model_get(), p)
+    (tmp_path / "bad.bin").write_bytes(b"nope")
+    with pytest.raises(BmsError):
+        ctx.model_load(tmp_path / "bad.bin")
+
+
+def test_learned_order_requires_exact_semantics(ctx, trained):
+    q, d = workloads.make("mol1k", 14, n_data=50, n_queries=5)
+    ctx.load(QUERY, q)
+    ctx.load(DATA, d)
+    with pytest.raises(BmsError):
+        ctx.run(2, COUNT_ALL, ORDER_LEARNED, 1)

@@ -1,0 +1,269 @@
+"""CUDA path against the oracle, through the C ABI (libbms.so), bit for bit.
+
+Every stage of the staged pipeline (signatures, filter, each refine step, GMCR,
+join) and the fused pipeline are compared with the CPU oracle on the same seeded
+inputs; EXACT counts are also compared with the networkx answer key.
+"""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+from bms2_gb300 import (COUNT_ALL, DATA, FIND_FIRST, ORDER_GMCR, QUERY, SEM_EXACT, SEM_REFERENCE_DFS, BmsError,
+                        Graphs, workloads)
+from tests.kat_graphs import C, N, O, WILD, chain, line, ring, star
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = Path(__file__).with_name("golden") / "nx_small.json"
+
+
+def graphs(*gs) -> Graphs:
+    return Graphs.parse_text("\n".join(line(*g) for g in gs) + "\n")
+
+
+def mixed_workload(seed=3, n_data=300, n_queries=24):
+    """Seeded molecules plus hand-built edge cases appended to both sides."""
+    q, d = workloads.make("mol1k", seed, n_data=n_data, n_queries=n_queries)
+    extra_q = [ring(6), star(2), ([WILD, C], [(0, 1)]), ([20, C], [(0, 1)]), ([C], []), chain(4)]
+    extra_d = [ring(6), star(3), ([O, C], [(0, 1)]), ([20, C, C], [(0, 1), (1, 2)]), ring(5),
+               (ring(5)[0], ring(5)[1] + [(0, 1)]),  # repeated CSR entries
+               ([C] * 0, [])]  # an empty data graph
+    tmp = []
+    for g, extra in ((q, extra_q), (d, extra_d)):
+        a = g.arrays()
+        txt = _text(a) + "".join(line(*x) + "\n" for x in extra)
+        tmp.append(Graphs.parse_text(txt))
+    return tmp[0], tmp[1]
+
+
+def _text(a) -> str:
+    go, ro, ci, nl, el = (a["graph_offsets"], a["row_offsets"], a["column_indices"], a["node_labels"],
+                          a["edge_labels"])
+    out = []
+    for g in range(len(go) - 1):
+        s, e = int(go[g]), int(go[g + 1])
+        labels = [int(x) for x in nl[s:e]]
+        edges = [(v - s, int(ci[i]) - s) for v in range(s, e) for i in range(int(ro[v]), int(ro[v + 1]))
+                 if int(ci[i]) >= v]
+        out.append(line(labels, edges) + "\n")
+    return "".join(out)
+
+
+@pytest.fixture(scope="module")
+def wl():
+    return mixed_workload()
+
+
+def load(ctx, q, d):
+    ctx.load(QUERY, q)
+    ctx.load(DATA, d)
+
+
+@pytest.mark.parametrize("R", [0, 6])
+def test_signatures_bit_exact(ctx, wl, R):
+    q, d = wl
+    load(ctx, q, d)
+    ctx.signatures(R)
+    for kind, g in ((QUERY, q), (DATA, d)):
+        want = oracle.signatures(g.arrays(), R)
+        got = ctx.signatures_of(kind, R)
+        assert np.array_equal(got["label_gen"], want.label_gen)
+        assert np.array_equal(got["path"], want.path)
+        assert np.array_equal(got["cycle"], want.cycle)
+        assert np.array_equal(got["shells"], want.shells)
+
+
+@pytest.mark.parametrize("R", [0, 3, 6])
+def test_staged_filter_refine_map_bit_exact(ctx, wl, R):
+    q, d = wl
+    want = oracle.run_pipeline(q, d, R, join=False)
+    load(ctx, q, d)
+    ctx.signatures(R)
+    ctx.filter()
+    assert np.array_equal(ctx.candidates(), want.cand_filter)
+    for k in range(1, R + 1):
+        ctx.refine(k)
+        assert np.array_equal(ctx.candidates(), want.cand_steps[k - 1]), f"refine step {k}"
+    T = ctx.map()
+    off, qidx = ctx.gmcr()
+    assert T == len(want.qidx)
+    assert np.array_equal(off, want.offsets)
+    assert np.array_equal(qidx, want.qidx)
+
+
+MODES = [(COUNT_ALL, SEM_EXACT), (FIND_FIRST, SEM_EXACT), (COUNT_ALL, SEM_REFERENCE_DFS),
+         (FIND_FIRST, SEM_REFERENCE_DFS)]
+
+
+@pytest.mark.parametrize("mode,sem", MODES)
+def test_staged_join_counts_bit_exact(ctx, wl, mode, sem):
+    q, d = wl
+    R = 2
+    want = oracle.run_pipeline(q, d, R, find_first=mode == FIND_FIRST, dfs_literal=sem == SEM_REFERENCE_DFS)
+    load(ctx, q, d)
+    ctx.signatures(R)
+    ctx.filter()
+    for k in range(1, R + 1):
+        ctx.refine(k)
+    ctx.map()
+    total = ctx.join(mode, ORDER_GMCR, sem)
+    assert np.array_equal(ctx.pair_counts(), want.counts)
+    assert total == want.total
+
+
+@pytest.mark.parametrize("R", [0, 2, 6])
+@pytest.mark.parametrize("mode,sem", MODES)
+def test_fused_run_bit_exact(ctx, wl, R, mode, sem):
+    q, d = wl
+    want = oracle.run_pipeline(q, d, R, find_first=mode == FIND_FIRST, dfs_literal=sem == SEM_REFERENCE_DFS)
+    load(ctx, q, d)
+    total = ctx.run(R, mode, ORDER_GMCR, sem)
+    off, qidx = ctx.gmcr()
+    assert np.array_equal(off, want.offsets)
+    assert np.array_equal(qidx, want.qidx)
+    assert np.array_equal(ctx.pair_counts(), want.counts)
+    assert total == want.total
+    st = ctx.stats()
+    assert st["n_valid_pairs"] == len(want.qidx)
+    assert st["n_pairs"] == q.n_graphs * d.n_graphs
+
+
+def test_fused_expansions_match_oracle_exact_plain_order(ctx, wl):
+    # oracle expansions count the reference DFS's successful pushes per pair;
+    # the engine's bitset DFS makes the same assignments in EXACT mode
+    q, d = wl
+    want = oracle.run_pipeline(q, d, 2)
+    load(ctx, q, d)
+    ctx.run(2, COUNT_ALL, ORDER_GMCR, SEM_EXACT)
+    got = ctx.pair_expansions()
+    counted = want.counts > 0
+    assert np.array_equal(got[counted], want.expansions[counted])
+
+
+@pytest.mark.parametrize("R", [0, 2])
+def test_fused_matches_networkx_answer_key(ctx, R):
+    g = json.loads(GOLDEN.read_text())
+    q = Graphs.parse_text(g["query_text"])
+    d = Graphs.parse_text(g["data_text"])
+    load(ctx, q, d)
+    ctx.run(R, COUNT_ALL, ORDER_GMCR, SEM_EXACT)
+    off, qidx = ctx.gmcr()
+    counts = ctx.pair_counts()
+    dense = np.zeros((g["n_queries"], g["n_data"]), np.uint64)
+    for di in range(g["n_data"]):
+        for t in range(off[di], off[di + 1]):
+            dense[qidx[t], di] = counts[t]
+    want = np.zeros_like(dense)
+    for qi, di, c in g["counts"]:
+        want[qi, di] = c
+    assert np.array_equal(dense, want)
+
+
+def test_large_graphs_two_word_bitsets(ctx):
+    # data graphs of 65-128 nodes and queries of 31-64 nodes (beyond the
+    # reference's 64/30 domain: generalized semantics, same in the oracle)
+    d = Graphs.synth_molecules(60, 5, 0, 0, 0, 65, 128, 1, 4)
+    q = Graphs.synth_queries(d, 10, 6, 31, 40)
+    q2 = Graphs.synth_queries(d, 10, 7, 3, 10)
+    for qq in (q, q2):
+        for R in (0, 4):
+            want = oracle.run_pipeline(qq, d, R)
+            load(ctx, qq, d)
+            ctx.run(R, COUNT_ALL, ORDER_GMCR, SEM_EXACT)
+            assert np.array_equal(ctx.pair_counts(), want.counts)
+            ctx.signatures(R)
+            got = ctx.signatures_of(DATA, R)
+            assert np.array_equal(got["cycle"], want.d_sigs.cycle)
+            assert np.array_equal(got["shells"], want.d_sigs.shells)
+
+
+def test_many_entries_graph_reads_rows_from_global_memory(ctx):
+    # a 127-leaf star with every edge listed 5 times: 1270 CSR entries (more
+    # than the 1024 staged in shared memory), repeated entries, 128 nodes
+    labels = [C] + [C if i % 4 else N for i in range(127)]
+    edges = [(0, i + 1) for i in range(127) for _ in range(5)]
+    d = graphs((labels, edges), ring(6))
+    q = graphs(star(2), chain(3), ([N, C], [(0, 1)]), ([C, N, C], [(0, 1), (0, 2)]))
+    for R in (0, 2):
+        want = oracle.run_pipeline(q, d, R)
+        load(ctx, q, d)
+        ctx.run(R, COUNT_ALL, ORDER_GMCR, SEM_EXACT)
+        assert np.array_equal(ctx.pair_counts(), want.counts)
+        ctx.signatures(R)
+        got = ctx.signatures_of(DATA, R)
+        for k in ("label_gen", "path", "cycle", "shells"):
+            assert np.array_equal(got[k], getattr(want.d_sigs, k)), k
+    assert want.counts.max() == 95 * 94  # ordered pairs of the 95 carbon leaves
+
+
+def test_mol100k_sample_fused_equals_staged_equals_oracle(ctx):
+    q, d = workloads.make("mol100k", 1, n_data=3000, n_queries=60)
+    R = 6
+    want = oracle.run_pipeline(q, d, R, keep_steps=False)
+    load(ctx, q, d)
+    total = ctx.run(R, COUNT_ALL, ORDER_GMCR, SEM_EXACT)
+    assert np.array_equal(ctx.pair_counts(), want.counts)
+    assert total == want.total
+    ctx.signatures(R)
+    ctx.filter()
+    for k in range(1, R + 1):
+        ctx.refine(k)
+    ctx.map()
+    assert ctx.join(COUNT_ALL, ORDER_GMCR, SEM_EXACT) == total
+
+
+def test_runs_are_deterministic(ctx, wl):
+    q, d = wl
+    load(ctx, q, d)
+    a = ctx.run(6, COUNT_ALL, ORDER_GMCR, SEM_EXACT)
+    ca = ctx.pair_counts().copy()
+    b = ctx.run(6, COUNT_ALL, ORDER_GMCR, SEM_EXACT)
+    assert a == b and np.array_equal(ca, ctx.pair_counts())
+
+
+def test_invalid_column_is_reported(ctx):
+    q = graphs(chain(2))
+    ctx.load(QUERY, q)
+    ctx.load_csr(DATA, [0, 2], [0, 1, 2], [1, 5], [8, 8])
+    with pytest.raises(BmsError) as e:
+        ctx.run(1)
+    assert e.value.status == -1
+
+
+def test_oversized_graph_is_rejected_at_load(ctx):
+    big = graphs(chain(129))
+    with pytest.raises(BmsError) as e:
+        ctx.load(DATA, big)
+    assert e.value.status == -6
+    with pytest.raises(BmsError):
+        ctx.load(QUERY, graphs(chain(65)))
+
+
+def test_stage_order_is_enforced(ctx, wl):
+    q, d = wl
+    load(ctx, q, d)
+    with pytest.raises(BmsError) as e:
+        ctx.filter()
+    assert e.value.status == -5
+    with pytest.raises(BmsError):
+        ctx.map()
+
+
+def test_expansion_budget_marks_pairs_incomplete(ctx):
+    q = graphs(chain(8))
+    d = graphs(*[chain(40) for _ in range(4)])
+    load(ctx, q, d)
+    ctx.set_expansion_budget(5)
+    try:
+        with pytest.raises(BmsError) as e:
+            ctx.run(0, COUNT_ALL, ORDER_GMCR, SEM_EXACT)
+        assert e.value.status == -8
+        assert ctx.stats()["n_incomplete"] > 0
+        assert ctx.pair_status().max() == 1
+    finally:
+        ctx.set_expansion_budget(0)
+    full = ctx.run(0, COUNT_ALL, ORDER_GMCR, SEM_EXACT)
+    assert full == oracle.run_pipeline(q, d, 0).total

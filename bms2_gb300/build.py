@@ -17,6 +17,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_build"
 LIB = OUT / "libbms.so"
+CLI = OUT / "bms2"
 ORACLE_DIR = ROOT / "oracle"
 ORACLE_OUT = ORACLE_DIR / "_build"
 ORACLE_LIB = ORACLE_OUT / "liboracle.so"
@@ -69,6 +70,11 @@ def build_library(force: bool = False, jobs: int | None = None) -> Path:
     if force or jobs_ or _stale(LIB, objs):
         _run([nvcc, "-shared", *ARCH, "-cudart", "static", "-o", str(LIB), *map(str, objs), "-lpthread", "-ldl",
               "-lrt"])
+    cli_src = CSRC / "tools" / "bms2_main.cpp"
+    if force or _stale(CLI, [cli_src, LIB, ROOT / "include" / "bms.hpp", ROOT / "include" / "bms.h"]):
+        cxx = shutil.which("g++") or "g++"
+        _run([cxx, "-std=c++17", "-O2", "-I", str(ROOT / "include"), str(cli_src), "-o", str(CLI), "-L", str(OUT),
+              "-lbms", "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 

@@ -374,7 +374,9 @@ int bms_signatures(bms_ctx* c, int R) {
   GUARD(c);
   if (!c->q.loaded || !c->d.loaded) return fail(c, BMS_ESTATE, "load query and data graphs first");
   if (R < 0 || R > BMS_MAX_REFINE_STEPS) return fail(c, BMS_EINVAL, "refine_steps must be in [0, 8]");
-  invalidate_downstream(c);
+  // signatures are a pure function of the loaded graphs: steps 1..k do not
+  // change when more steps are requested, so an existing candidate matrix
+  // stays valid (uploads invalidate it)
   CK(cudaEventRecord(c->ev[EV_START], c->st));
   int r = run_signatures(c, R);
   if (r) return r;

@@ -166,7 +166,7 @@ def run_ours(args) -> None:
     if order == ORDER_LEARNED:
         extra.update(train_cost_model(ctx, seed=101, n_data=args.train_graphs))
     # evaluation workload (seed B; each rank its own shard)
-    q, d = workloads.make(WORKLOAD, 202 + rank)
+    q, d = workloads.make(WORKLOAD, 202 + rank, n_data=args.data_graphs)
     Q, D = q.n_graphs, d.n_graphs
     qa, da = q.arrays(), d.arrays()
     ctx.load(QUERY, q)
@@ -176,6 +176,11 @@ def run_ours(args) -> None:
     def step():
         return ctx.run(REFINE_STEPS, COUNT_ALL, order, SEM_EXACT)
 
+    if args.once:  # one pipeline run, for profilers
+        total = step()
+        print(json.dumps({"once": True, "order": args.order, "total": int(total), **ctx.stats()}), flush=True)
+        ctx.close()
+        return
     for _ in range(args.warmup):
         step()
     plain_total = None
@@ -329,6 +334,8 @@ def main() -> None:
     ap.add_argument("--train-graphs", type=int, default=20000)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--data-graphs", type=int, default=None, help="shrink the workload (profiling)")
+    ap.add_argument("--once", action="store_true", help="one untimed pipeline run (profiling)")
     args = ap.parse_args()
     from bms2_gb300 import build
 

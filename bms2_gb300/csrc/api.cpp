@@ -86,6 +86,7 @@ int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const 
   }
   CK(s.frec.ensure(sizeof(uint64_t) * kRecWords * (N ? N : 1)));
   CK(s.adj.ensure(sizeof(uint64_t) * 2 * (N ? N : 1)));
+  CK(s.adjin.ensure(sizeof(uint64_t) * 2 * (N ? N : 1)));
   CK(s.ghist.ensure(sizeof(uint64_t) * (G ? G : 1)));
   CK(s.glabset.ensure(sizeof(uint32_t) * (G ? G : 1)));
   s.loaded = true;
@@ -526,6 +527,7 @@ int run_fused(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total, 
   CK(c->gmcr_off.ensure(sizeof(uint32_t) * (D + 1)));
   CK(c->scan_scratch.ensure(sizeof(uint32_t) * scan_scratch_words(D)));
   CK(c->filter_order.ensure(uint64_t(Q ? Q : 1) * kMaxQueryNodes));
+  CK(c->filter_dup.ensure(uint64_t(Q ? Q : 1) * kMaxQueryNodes));
   CK(c->label_count.ensure(256 * sizeof(unsigned long long)));
   if (c->rec_cap == 0) {
     c->rec_cap = std::max<uint64_t>(1 << 16, std::min<uint64_t>(uint64_t(Q) * D, uint64_t(1) << 22));
@@ -544,7 +546,8 @@ int run_fused(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total, 
   r = run_signatures(c, R);
   if (r) return r;
   CK(launch_label_count(c->d.dg(), c->label_count.as<unsigned long long>(), c->st));
-  CK(launch_query_prep(c->q.dg(), c->q.ds(), c->label_count.as<unsigned long long>(), c->filter_order.as<uint8_t>(), c->st));
+  CK(launch_query_prep(c->q.dg(), c->q.ds(), c->label_count.as<unsigned long long>(), c->filter_order.as<uint8_t>(),
+                       c->filter_dup.as<uint8_t>(), c->st));
   CK(cudaEventRecord(c->ev[EV_SIG], c->st));
   PairFilterArgs pa{};
   pa.q = c->q.dg();
@@ -552,6 +555,7 @@ int run_fused(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total, 
   pa.qs = c->q.ds();
   pa.ds = c->d.ds();
   pa.filter_order = c->filter_order.as<uint8_t>();
+  pa.dup = c->filter_dup.as<uint8_t>();
   pa.dperm = c->dperm.as<uint32_t>();
   pa.valid = c->valid.as<uint32_t>();
   pa.QW = c->QW;

@@ -45,12 +45,13 @@ struct Side {
   uint32_t max_nodes = 0;
   std::vector<uint32_t> h_goff;
   DevBuf goff, rowp, col, lab, elab;
-  DevBuf frec, adj, ghist, glabset;
+  DevBuf frec, adj, adjin, ghist, glabset;
   int sig_steps = -1;
   bool asymmetric = false;
   DGraphs dg() const { return DGraphs{goff.as<uint32_t>(), rowp.as<uint32_t>(), col.as<uint32_t>(), lab.as<uint8_t>(), G, N, E}; }
   DSigs ds() const {
-    return DSigs{frec.as<uint64_t>(), adj.as<uint64_t>(), ghist.as<uint64_t>(), glabset.as<uint32_t>(), sig_steps < 0 ? 0 : sig_steps};
+    return DSigs{frec.as<uint64_t>(), adj.as<uint64_t>(), adjin.as<uint64_t>(), ghist.as<uint64_t>(),
+                 glabset.as<uint32_t>(), sig_steps < 0 ? 0 : sig_steps};
   }
 };
 
@@ -87,7 +88,7 @@ struct bms_ctx {
   uint64_t rec_cap = 0, row_cap = 0, task_cap = 0;
   DevBuf dperm;
   uint32_t class_begin[3] = {0, 0, 0}, class_end[3] = {0, 0, 0};
-  DevBuf filter_order, label_count, perm, dadj, vertex_exp, cand_sum, recs_per_query, features, cost;
+  DevBuf filter_order, filter_dup, label_count, perm, dadj, vertex_exp, cand_sum, recs_per_query, features, cost;
   bool have_results = false, have_vexp = false;
   int last_mode = 0, last_order = 0, last_sem = 0;
   DevBuf tmp;

@@ -35,11 +35,14 @@ struct DGraphs {
 //   w0  label | degree << 32        w1  cycle: 4 x uint16 (5-same, 5-diff, 6-same, 6-diff)
 //   w2..w5  256-bit path filter     w6..w13  distance shells 1..8 (16 nibbles each)
 //   w14 label signature (neighbour label counts)   w15 zero
-// adj holds two 64-bit words per node: the set of local ids in the node's CSR row.
+// adj holds two 64-bit words per node: the set of local ids in the node's CSR
+// row; adjin the set of local ids whose rows contain the node (equal to adj
+// when the graph is symmetric).
 constexpr int kRecWords = 16;
 struct DSigs {
   uint64_t* frec;       // [N*16]
   uint64_t* adj;        // [N*2]
+  uint64_t* adjin;      // [N*2]
   uint64_t* ghist;      // [G]   per-graph nibble histogram of labels < 16
   uint32_t* glabset;    // [G]   bit l: some node has label l (< 16)
   int R;
@@ -109,15 +112,17 @@ cudaError_t launch_set_counter(unsigned long long* dst, unsigned long long value
 // Label totals over all data nodes (labels 0..255).
 cudaError_t launch_label_count(const DGraphs& d, unsigned long long* counts, cudaStream_t st);
 // Per query: vertex order of the validity test (rarest label first, then
-// highest degree), its label set and its label histogram.
+// highest degree) and, per vertex, an earlier vertex with an identical filter
+// record (0xFF if none).
 cudaError_t launch_query_prep(const DGraphs& q, const DSigs& qs, const unsigned long long* label_count,
-                              uint8_t* filter_order, cudaStream_t st);
+                              uint8_t* filter_order, uint8_t* dup, cudaStream_t st);
 
 // Fused filter + refine + GMCR validity for every (query, data graph) pair.
 struct PairFilterArgs {
   DGraphs q, d;
   DSigs qs, ds;
   const uint8_t* filter_order;  // [Q*64]
+  const uint8_t* dup;           // [Q*64] vertex with an identical record, earlier in the order, or 0xFF
   const uint32_t* dperm;        // data graph ids grouped by size class
   uint32_t class_begin, class_end;
   int class_id;

@@ -9,11 +9,16 @@
 // task with one warp-aggregated atomic on a global head, so there is no
 // per-workgroup chunking and long tasks never hold idle neighbours hostage.
 // The search state is bitsets over the data graph's local ids (<= 128 nodes):
-//   F[t]   candidates left at depth t = C[order[t]] minus visited, intersected
-//          with the neighbourhood (or its complement) of every earlier mapped
-//          node, as the induced test of isValidMapping_fast_bitwise demands
-//          (isomorphism.hpp:268-288);
-//   As[t]  the CSR-row set of the node mapped at depth t.
+//   F[t]   candidates left at depth t: the vertices v of C[order[t]] not yet
+//          mapped that satisfy the induced test of isValidMapping_fast_bitwise
+//          (isomorphism.hpp:268-288) against every earlier depth i, i.e.
+//          v in row(f_i) iff query vertex order[i] is in the row of order[t].
+// The test is evaluated in two parts: C is intersected with the rows of the
+// nodes mapped at the query-adjacent earlier depths (usually one or two), and
+// each surviving candidate v is kept iff every mapped node whose row contains
+// v (v's in-row, intersected with the mapped set) sits at one of those
+// depths.  On molecular graphs (degree <= 4) that is a handful of independent
+// 16-byte loads per level instead of one dependent load per earlier depth.
 // The last depth is never expanded: its candidates are counted with one
 // popcount.  Stacks live in per-thread local memory, interleaved per lane.
 //
@@ -34,21 +39,33 @@ struct Lane {
   bool done_fetching;
   uint32_t rec, n, qoff;
   const uint64_t* crow;
-  const uint64_t* arow;
+  const uint64_t* arow;  // out-rows of the data graph
+  const uint64_t* irow;  // in-rows of the data graph
   const uint8_t* perm;
   const uint64_t* dadj;
   int t;
-  B128 vis;
+  B128 mapped;  // nodes mapped at depths 0..t-1 of the current path
+  B128 vis;     // REFERENCE_DFS: the reference's visited bitset
   unsigned long long cnt, exps;
   uint32_t since_check;
 };
 
-__device__ __forceinline__ B128 compute_level(const Lane& L, uint32_t j, const B128* As, bool literal) {
+__device__ __forceinline__ B128 compute_level(const Lane& L, uint32_t j, const uint8_t* f, bool literal) {
   B128 c = ld_b128(L.crow + 2 * uint64_t(L.perm[j]));
-  if (!literal) c = b_andn(c, L.vis);
-  const uint64_t m = L.dadj[j];
-  for (uint32_t i = 0; i < j; ++i) c = ((m >> i) & 1ull) ? b_and(c, As[i]) : b_andn(c, As[i]);
-  return c;
+  if (!literal) c = b_andn(c, L.mapped);
+  B128 pset{0, 0};
+  for (uint64_t pm = L.dadj[j]; pm; pm &= pm - 1) {
+    const uint32_t x = f[__ffsll((long long)pm) - 1];
+    c = b_and(c, ld_b128(L.arow + 2 * uint64_t(x)));
+    pset = b_or(pset, b_bit(x));
+  }
+  B128 res{0, 0};
+  for (B128 r = c; b_any(r); r = b_clear_low(r)) {
+    const uint32_t v = b_low(r);
+    const B128 bad = b_andn(b_and(ld_b128(L.irow + 2 * uint64_t(v)), L.mapped), pset);
+    if (!b_any(bad)) res = b_or(res, b_bit(v));
+  }
+  return res;
 }
 
 __device__ __forceinline__ void finish(Lane& L, const JoinArgs& a, const uint32_t* expd) {
@@ -95,7 +112,7 @@ __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
   L.done_fetching = false;
   L.cnt = L.exps = 0;
   uint8_t f[kMaxQueryNodes], mp[kMaxQueryNodes];
-  B128 F[kMaxQueryNodes], As[kMaxQueryNodes];
+  B128 F[kMaxQueryNodes];
   uint32_t expd[kMaxQueryNodes];
   for (;;) {
     const uint32_t need = __ballot_sync(0xffffffffu, !L.active && !L.done_fetching);
@@ -116,6 +133,7 @@ __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
           L.n = a.q.goff[r.q + 1] - L.qoff;
           L.crow = a.arena + 2 * uint64_t(r.c_row);
           L.arow = a.ds.adj + 2 * uint64_t(a.d.goff[r.d]);
+          L.irow = a.ds.adjin + 2 * uint64_t(a.d.goff[r.d]);
           L.perm = a.o.perm + uint64_t(r.q) * kMaxQueryNodes;
           L.dadj = a.o.dadj + uint64_t(r.q) * kMaxQueryNodes;
           L.cnt = 0;
@@ -133,9 +151,9 @@ __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
             f[0] = uint8_t(root);
             mp[0] = uint8_t(root);
             for (uint32_t t = 1; t < L.n; ++t) mp[t] = kNull8;
-            As[0] = ld_b128(L.arow + 2 * uint64_t(root));
             L.vis = b_bit(root);
-            const B128 nf = compute_level(L, 1, As, a.literal);
+            L.mapped = L.vis;
+            const B128 nf = compute_level(L, 1, f, a.literal);
             if (L.n == 2) {
               leaf(L, a, nf, mp, expd);
               finish(L, a, expd);
@@ -152,32 +170,34 @@ __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
       const int t = L.t;
       const B128 cur = F[t];
       if (!b_any(cur)) {
-        if (a.literal) {
-          if (mp[t] != kNull8) L.vis = b_andn(L.vis, b_bit(mp[t]));
-          L.t = t - 1;
-        } else {
-          L.t = t - 1;
-          if (L.t > 0) L.vis = b_andn(L.vis, b_bit(f[L.t]));
+        // frame t exhausted; back in frame t-1, whose node leaves the path
+        if (a.literal && mp[t] != kNull8) L.vis = b_andn(L.vis, b_bit(mp[t]));
+        L.t = t - 1;
+        if (L.t == 0) {
+          finish(L, a, expd);
+          continue;
         }
-        if (L.t == 0) finish(L, a, expd);
+        L.mapped = b_andn(L.mapped, b_bit(f[L.t]));
         continue;
       }
       const uint32_t v = b_low(cur);
       F[t] = b_clear_low(cur);
-      if (a.literal && b_has(L.vis, v)) continue;
+      if (a.literal) {
+        if (b_has(L.vis, v)) continue;
+        mp[t] = uint8_t(v);
+        L.vis = b_or(L.vis, b_bit(v));
+      }
       f[t] = uint8_t(v);
-      mp[t] = uint8_t(v);
-      L.vis = b_or(L.vis, b_bit(v));
-      As[t] = ld_b128(L.arow + 2 * uint64_t(v));
+      L.mapped = b_or(L.mapped, b_bit(v));
       L.exps += 1;
       if (a.vertex_exp) expd[t] += 1;
-      const B128 nf = compute_level(L, uint32_t(t) + 1, As, a.literal);
+      const B128 nf = compute_level(L, uint32_t(t) + 1, f, a.literal);
       if (uint32_t(t) + 1 == L.n - 1) {
         if (leaf(L, a, nf, mp, expd)) {
           finish(L, a, expd);
           continue;
         }
-        if (!a.literal) L.vis = b_andn(L.vis, b_bit(v));
+        L.mapped = b_andn(L.mapped, b_bit(v));  // frame t moves on
       } else {
         L.t = t + 1;
         F[t + 1] = nf;

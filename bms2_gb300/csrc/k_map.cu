@@ -26,32 +26,68 @@ __global__ void label_count_kernel(DGraphs d, unsigned long long* counts) {
     if (h[i]) atomicAdd(&counts[i], (unsigned long long)h[i]);
 }
 
-// One thread per query: validity-test order, rarest label first (wildcards
-// last), ties by higher degree, then by index.
-__global__ void query_prep_kernel(DGraphs q, DSigs qs, const unsigned long long* label_count, uint8_t* order) {
-  for (uint32_t qg = blockIdx.x * blockDim.x + threadIdx.x; qg < q.G; qg += gridDim.x * blockDim.x) {
+// One warp per query, lane i owning vertices i and i + 32.
+//  - order: the vertex order of the validity test, rarest data label first
+//    (wildcards last), then higher degree, then lower index;
+//  - dup[v]: the vertex earliest in that order whose filter record (label,
+//    degree, cycle, path and the first R shells) equals v's, 0xFF if none or
+//    if v is itself the earliest.  Equal records give equal candidate rows.
+__global__ void query_prep_kernel(DGraphs q, DSigs qs, const unsigned long long* label_count, uint8_t* order,
+                                  uint8_t* dup) {
+  const uint32_t lane = lane_id();
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  const int R = qs.R;
+  for (uint32_t qg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; qg < q.G; qg += warps) {
     const uint32_t qoff = q.goff[qg], n = q.goff[qg + 1] - qoff;
-    uint8_t* o = order + uint64_t(qg) * kMaxQueryNodes;
-    unsigned long long key[kMaxQueryNodes];
-    for (uint32_t i = 0; i < n && i < kMaxQueryNodes; ++i) {
-      const uint64_t w0 = qs.frec[uint64_t(kRecWords) * (qoff + i)];
-      const uint32_t l = uint32_t(w0 & 0xFFu), deg = uint32_t(w0 >> 32);
-      const unsigned long long freq = l == kWildcard ? 0xFFFFFFFFFFull : (label_count[l] & 0xFFFFFFFFFFull);
-      const uint32_t dk = 0xFFFFu - (deg > 0xFFFFu ? 0xFFFFu : deg);
-      key[i] = (freq << 22) | (uint64_t(dk) << 6) | i;
-      o[i] = uint8_t(i);
-    }
-    for (uint32_t i = 1; i < n && i < kMaxQueryNodes; ++i) {
-      const unsigned long long k = key[i];
-      const uint8_t v = o[i];
-      int j = int(i) - 1;
-      while (j >= 0 && key[j] > k) {
-        key[j + 1] = key[j];
-        o[j + 1] = o[j];
-        --j;
+    unsigned long long key[2];
+    uint64_t h[2];
+    for (int r = 0; r < 2; ++r) {
+      const uint32_t i = lane + 32 * r;
+      key[r] = ~0ull;
+      h[r] = 0;
+      if (i < n) {
+        const uint64_t* rec = qs.frec + uint64_t(kRecWords) * (qoff + i);
+        const uint64_t w0 = rec[0];
+        const uint32_t l = uint32_t(w0 & 0xFFu), deg = uint32_t(w0 >> 32);
+        const unsigned long long freq = l == kWildcard ? 0xFFFFFFFFFFull : (label_count[l] & 0xFFFFFFFFFFull);
+        const uint32_t dk = 0xFFFFu - (deg > 0xFFFFu ? 0xFFFFu : deg);
+        key[r] = (freq << 22) | (uint64_t(dk) << 6) | i;
+        uint64_t x = 0x9e3779b97f4a7c15ull;
+        for (int w = 0; w < 6 + R; ++w) x = (x ^ rec[w]) * 0x100000001b3ull + (x >> 29);
+        h[r] = x;
       }
-      key[j + 1] = k;
-      o[j + 1] = v;
+    }
+    // rank of each vertex in the order
+    uint32_t rank[2] = {0, 0};
+    for (uint32_t j = 0; j < n; ++j) {
+      const unsigned long long kj = __shfl_sync(0xffffffffu, key[j >> 5], j & 31);
+      for (int r = 0; r < 2; ++r) rank[r] += kj < key[r];
+    }
+    uint8_t* o = order + uint64_t(qg) * kMaxQueryNodes;
+    uint8_t* dd = dup + uint64_t(qg) * kMaxQueryNodes;
+    for (int r = 0; r < 2; ++r) {
+      const uint32_t i = lane + 32 * r;
+      if (i < n) o[rank[r]] = uint8_t(i);
+    }
+    // duplicate records: earliest-ranked vertex with an equal record
+    for (int r = 0; r < 2; ++r) {
+      const uint32_t i = lane + 32 * r;
+      uint32_t best = 0xFFu, best_rank = rank[r];
+      for (uint32_t j = 0; j < n; ++j) {
+        const uint64_t hj = __shfl_sync(0xffffffffu, h[j >> 5], j & 31);
+        const uint32_t rj = __shfl_sync(0xffffffffu, rank[j >> 5], j & 31);
+        if (i < n && j != i && hj == h[r] && rj < best_rank) {
+          const uint64_t* a = qs.frec + uint64_t(kRecWords) * (qoff + i);
+          const uint64_t* b = qs.frec + uint64_t(kRecWords) * (qoff + j);
+          bool same = true;
+          for (int w = 0; w < 6 + R && same; ++w) same = a[w] == b[w];
+          if (same) {
+            best = j;
+            best_rank = rj;
+          }
+        }
+      }
+      if (i < n) dd[i] = uint8_t(best);
     }
   }
 }
@@ -238,9 +274,9 @@ cudaError_t launch_label_count(const DGraphs& d, unsigned long long* counts, cud
 }
 
 cudaError_t launch_query_prep(const DGraphs& q, const DSigs& qs, const unsigned long long* label_count,
-                              uint8_t* filter_order, cudaStream_t st) {
+                              uint8_t* filter_order, uint8_t* dup, cudaStream_t st) {
   if (q.G == 0) return cudaSuccess;
-  query_prep_kernel<<<grid_for(q.G, 64), 64, 0, st>>>(q, qs, label_count, filter_order); note_launch();
+  query_prep_kernel<<<grid_for(uint64_t(q.G) * 32, 128), 128, 0, st>>>(q, qs, label_count, filter_order, dup); note_launch();
   return cudaGetLastError();
 }
 

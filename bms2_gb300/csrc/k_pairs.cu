@@ -137,13 +137,21 @@ __global__ void __launch_bounds__(ROUNDS <= 2 ? 256 : 128) pair_filter_kernel(Pa
         const bool join = (m2 >> i) & 1u;
         const uint32_t qoff = a.q.goff[q], n = a.q.goff[q + 1] - qoff;
         const uint8_t* ord = a.filter_order + uint64_t(q) * kMaxQueryNodes;
+        const uint8_t* dup = a.dup + uint64_t(q) * kMaxQueryNodes;
         bool valid = true;
         for (uint32_t t = 0; t < n; ++t) {
           const uint32_t ul = ord[t];
-          const B128 c = eval_rows<ROUNDS>(dn, a.qs.frec + uint64_t(kRecWords) * (qoff + ul), R);
-          if (!b_any(c)) {
-            valid = false;
-            break;
+          const uint32_t src = dup[ul];
+          B128 c;
+          if (src != 0xFFu) {
+            __syncwarp();
+            c = rows[src];  // identical record, evaluated earlier in this pair
+          } else {
+            c = eval_rows<ROUNDS>(dn, a.qs.frec + uint64_t(kRecWords) * (qoff + ul), R);
+            if (!b_any(c)) {
+              valid = false;
+              break;
+            }
           }
           if (lane == 0) rows[ul] = c;
         }

@@ -253,6 +253,7 @@ __global__ void __launch_bounds__(kWarps * 32) signatures_kernel(DGraphs g, DSig
       rec[6] = make_ulonglong2(sh[6], sh[7]);
       rec[7] = make_ulonglong2(lg, 0ull);
       st_b128(out.adj + 2 * u, s.adj[v]);
+      st_b128(out.adjin + 2 * u, s.in[v]);
     }
     // per-graph label histogram (labels < 16) and label set
     uint32_t cnt = 0;

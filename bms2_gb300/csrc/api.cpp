@@ -66,6 +66,9 @@ int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const 
   s.E = E;
   s.max_nodes = mx;
   s.h_goff.assign(v.graph_offsets, v.graph_offsets + G + 1);
+  s.labels_lt16 = 0;
+  for (uint64_t i = 0; i < N; ++i)
+    if (v.node_labels[i] < 16) s.labels_lt16 |= 1u << v.node_labels[i];
   if (!G) s.h_goff.assign(1, 0);
   CK(s.goff.ensure(sizeof(uint32_t) * (G + 1)));
   CK(s.rowp.ensure(sizeof(uint32_t) * (N + 1)));
@@ -548,8 +551,16 @@ int run_fused(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total, 
   CK(launch_label_count(c->d.dg(), c->label_count.as<unsigned long long>(), c->st));
   CK(launch_query_prep(c->q.dg(), c->q.ds(), c->label_count.as<unsigned long long>(), c->filter_order.as<uint8_t>(),
                        c->filter_dup.as<uint8_t>(), c->st));
+  ShellPack sp{};
+  for (uint32_t l = 0; l < 16; ++l)
+    if ((c->q.labels_lt16 >> l) & 1u) sp.pos[sp.K++] = uint8_t(l);
+  sp.PW = sp.K == 0 ? 0u : (sp.K <= 8 ? uint32_t(R + 1) / 2 : uint32_t(R));
+  CK(c->qpack.ensure(sizeof(uint64_t) * 8 * (c->q.N ? c->q.N : 1)));
+  CK(launch_pack_query_shells(c->q.dg(), c->q.ds(), sp, c->qpack.as<uint64_t>(), c->st));
   CK(cudaEventRecord(c->ev[EV_SIG], c->st));
   PairFilterArgs pa{};
+  pa.qpack = c->qpack.as<uint64_t>();
+  pa.sp = sp;
   pa.q = c->q.dg();
   pa.d = c->d.dg();
   pa.qs = c->q.ds();

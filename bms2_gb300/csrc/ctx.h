@@ -48,6 +48,7 @@ struct Side {
   DevBuf frec, adj, adjin, ghist, glabset;
   int sig_steps = -1;
   bool asymmetric = false;
+  uint32_t labels_lt16 = 0;  // bit l: some node carries label l < 16
   DGraphs dg() const { return DGraphs{goff.as<uint32_t>(), rowp.as<uint32_t>(), col.as<uint32_t>(), lab.as<uint8_t>(), G, N, E}; }
   DSigs ds() const {
     return DSigs{frec.as<uint64_t>(), adj.as<uint64_t>(), adjin.as<uint64_t>(), ghist.as<uint64_t>(),
@@ -88,7 +89,7 @@ struct bms_ctx {
   uint64_t rec_cap = 0, row_cap = 0, task_cap = 0;
   DevBuf dperm;
   uint32_t class_begin[3] = {0, 0, 0}, class_end[3] = {0, 0, 0};
-  DevBuf filter_order, filter_dup, label_count, perm, dadj, vertex_exp, cand_sum, recs_per_query, features, cost;
+  DevBuf filter_order, filter_dup, qpack, label_count, perm, dadj, vertex_exp, cand_sum, recs_per_query, features, cost;
   bool have_results = false, have_vexp = false;
   int last_mode = 0, last_order = 0, last_sem = 0;
   DevBuf tmp;

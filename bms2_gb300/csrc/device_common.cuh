@@ -32,6 +32,24 @@ __device__ __forceinline__ uint64_t nib_le_bits(uint64_t q, uint64_t d) {
 }
 __device__ __forceinline__ bool nib_le(uint64_t q, uint64_t d) { return (nib_le_bits(q, d) & kHiBit) == kHiBit; }
 
+// Shell k projected onto ShellPack positions, packed two per word when K <= 8.
+__device__ __forceinline__ uint64_t project_shell(uint64_t s, const ShellPack& sp) {
+  uint64_t c = 0;
+#pragma unroll
+  for (int j = 0; j < 16; ++j)
+    if (uint32_t(j) < sp.K) c |= ((s >> (4 * sp.pos[j])) & 15ull) << (4 * j);
+  return c;
+}
+__device__ __forceinline__ uint64_t packed_word(const uint64_t* shells, int R, int w, const ShellPack& sp) {
+  if (sp.K <= 8) {
+    const int k0 = 2 * w, k1 = 2 * w + 1;
+    const uint64_t a = k0 < R ? project_shell(shells[k0], sp) : 0ull;
+    const uint64_t b = k1 < R ? project_shell(shells[k1], sp) : 0ull;
+    return a | (b << 32);
+  }
+  return w < R ? project_shell(shells[w], sp) : 0ull;
+}
+
 // CycleSignatureDevice::contains (signature.hpp:551-554) on 4 packed uint16.
 __device__ __forceinline__ bool cyc_ge(uint64_t d, uint64_t q) {
   const uint32_t dl = uint32_t(d), dh = uint32_t(d >> 32), ql = uint32_t(q), qh = uint32_t(q >> 32);

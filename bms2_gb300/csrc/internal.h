@@ -117,12 +117,26 @@ cudaError_t launch_label_count(const DGraphs& d, unsigned long long* counts, cud
 cudaError_t launch_query_prep(const DGraphs& q, const DSigs& qs, const unsigned long long* label_count,
                               uint8_t* filter_order, uint8_t* dup, cudaStream_t st);
 
+// Distance shells projected onto the labels that occur in the queries (a label
+// absent from every query has a zero query nibble, which any data nibble
+// satisfies): shell k keeps the K nibbles at positions pos[0..K-1]; with K <= 8
+// two projected shells share one 64-bit word, else one shell per word.
+struct ShellPack {
+  uint32_t K;
+  uint32_t PW;         // packed words per node
+  uint8_t pos[16];
+};
+cudaError_t launch_pack_query_shells(const DGraphs& q, const DSigs& qs, ShellPack sp, uint64_t* qpack,
+                                     cudaStream_t st);
+
 // Fused filter + refine + GMCR validity for every (query, data graph) pair.
 struct PairFilterArgs {
   DGraphs q, d;
   DSigs qs, ds;
   const uint8_t* filter_order;  // [Q*64]
   const uint8_t* dup;           // [Q*64] vertex with an identical record, earlier in the order, or 0xFF
+  const uint64_t* qpack;        // [Qn*8] packed query shells
+  ShellPack sp;
   const uint32_t* dperm;        // data graph ids grouped by size class
   uint32_t class_begin, class_end;
   int class_id;

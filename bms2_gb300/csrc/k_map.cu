@@ -205,22 +205,38 @@ __global__ void order_adjacency_kernel(DGraphs q, DSigs qs, DOrder o) {
 }
 
 // ------------------------------------------------------------------ tasks
+// Warp-aggregated: one atomic per warp reserves the tasks of 32 records.
 __global__ void task_emit_kernel(const PairRec* recs, uint64_t rec_cap, DGraphs q, DOrder o, const uint64_t* arena,
                                  Task* tasks, uint64_t task_cap, Counters* ctr, uint32_t* err) {
   const uint64_t n = min((unsigned long long)rec_cap, ctr->recs);
-  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
-    const PairRec r = recs[i];
-    const uint32_t root = o.perm[uint64_t(r.q) * kMaxQueryNodes];
-    B128 c = ld_b128(arena + 2 * (uint64_t(r.c_row) + root));
+  const uint32_t lane = lane_id();
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t base_i = uint64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u); base_i < n; base_i += stride) {
+    const uint64_t i = base_i + lane;
+    B128 c{0, 0};
+    if (i < n) {
+      const PairRec r = recs[i];
+      const uint32_t root = o.perm[uint64_t(r.q) * kMaxQueryNodes];
+      c = ld_b128(arena + 2 * (uint64_t(r.c_row) + root));
+    }
     const uint32_t k = b_pop(c);
-    if (!k) continue;
-    const unsigned long long base = atomicAdd(&ctr->tasks, (unsigned long long)k);
-    if (base + k > task_cap) {
-      atomicOr(err, kErrOverflow);
+    uint32_t incl = k;
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= uint32_t(d)) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    unsigned long long base = 0;
+    if (lane == 31 && total) base = atomicAdd(&ctr->tasks, (unsigned long long)total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    if (!total) continue;
+    if (base + total > task_cap) {
+      if (lane == 0) atomicOr(err, kErrOverflow);
       continue;
     }
+    unsigned long long pos = base + incl - k;
     for (uint32_t j = 0; j < k; ++j) {
-      tasks[base + j] = Task{uint32_t(i), b_low(c)};
+      tasks[pos + j] = Task{uint32_t(i), b_low(c)};
       c = b_clear_low(c);
     }
   }

@@ -22,15 +22,19 @@
 namespace bms {
 namespace {
 
-template <int ROUNDS>
+template <int ROUNDS, int PWMAX>
 struct DataNodes {
   uint32_t lab[ROUNDS], deg[ROUNDS];
-  uint64_t cyc[ROUNDS], p[ROUNDS][4], sh[ROUNDS][kMaxSteps];
+  uint64_t cyc[ROUNDS], p[ROUNDS][4], sh[ROUNDS][PWMAX];
   bool live[ROUNDS];
 };
 
-template <int ROUNDS>
-__device__ __forceinline__ B128 eval_rows(const DataNodes<ROUNDS>& dn, const uint64_t* __restrict__ qr, int R) {
+// Candidate row of one query node: label (or wildcard) and degree, then path
+// containment and cycle counts, then every distance shell; a warp-uniform
+// early exit follows each group.
+template <int ROUNDS, int PWMAX>
+__device__ __forceinline__ B128 eval_rows(const DataNodes<ROUNDS, PWMAX>& dn, const uint64_t* __restrict__ qr,
+                                          const uint64_t* __restrict__ qp, uint32_t PW) {
   const ulonglong2 a = *reinterpret_cast<const ulonglong2*>(qr);
   const uint32_t ql = uint32_t(a.x & 0xFFu), qd = uint32_t(a.x >> 32);
   bool ok[ROUNDS];
@@ -43,33 +47,30 @@ __device__ __forceinline__ B128 eval_rows(const DataNodes<ROUNDS>& dn, const uin
   if (!__any_sync(0xffffffffu, any)) return B128{0, 0};
   const ulonglong2 p01 = *reinterpret_cast<const ulonglong2*>(qr + 2);
   const ulonglong2 p23 = *reinterpret_cast<const ulonglong2*>(qr + 4);
-  uint64_t qs[kMaxSteps];
+  any = false;
 #pragma unroll
-  for (int k = 0; k < kMaxSteps; k += 2) {
-    if (k < R) {
-      const ulonglong2 s = *reinterpret_cast<const ulonglong2*>(qr + 6 + k);
-      qs[k] = s.x;
-      qs[k + 1] = s.y;
-    } else {
-      qs[k] = qs[k + 1] = 0;
-    }
+  for (int r = 0; r < ROUNDS; ++r) {
+    const uint64_t miss = (p01.x & ~dn.p[r][0]) | (p01.y & ~dn.p[r][1]) | (p23.x & ~dn.p[r][2]) | (p23.y & ~dn.p[r][3]);
+    ok[r] = ok[r] && miss == 0 && cyc_ge(dn.cyc[r], a.y);
+    any |= ok[r];
   }
+  if (!__any_sync(0xffffffffu, any)) return B128{0, 0};
+  uint64_t q[PWMAX];
+#pragma unroll
+  for (int w = 0; w < PWMAX; ++w) q[w] = uint32_t(w) < PW ? qp[w] : 0ull;
   uint32_t ballots[4] = {0, 0, 0, 0};
 #pragma unroll
   for (int r = 0; r < ROUNDS; ++r) {
-    bool o = ok[r] && (dn.p[r][0] & p01.x) == p01.x && (dn.p[r][1] & p01.y) == p01.y &&
-             (dn.p[r][2] & p23.x) == p23.x && (dn.p[r][3] & p23.y) == p23.y && cyc_ge(dn.cyc[r], a.y);
     uint64_t acc = kHiBit;
 #pragma unroll
-    for (int k = 0; k < kMaxSteps; ++k)
-      if (k < R) acc &= nib_le_bits(qs[k], dn.sh[r][k]);
-    o = o && (acc & kHiBit) == kHiBit;
-    ballots[r] = __ballot_sync(0xffffffffu, o);
+    for (int w = 0; w < PWMAX; ++w)
+      if (uint32_t(w) < PW) acc &= nib_le_bits(q[w], dn.sh[r][w]);
+    ballots[r] = __ballot_sync(0xffffffffu, ok[r] && (acc & kHiBit) == kHiBit);
   }
   return B128{uint64_t(ballots[0]) | (uint64_t(ballots[1]) << 32), uint64_t(ballots[2]) | (uint64_t(ballots[3]) << 32)};
 }
 
-template <int ROUNDS>
+template <int ROUNDS, int PWMAX>
 __global__ void __launch_bounds__(ROUNDS <= 2 ? 256 : 128) pair_filter_kernel(PairFilterArgs a) {
   constexpr int kWarpsPerBlock = (ROUNDS <= 2 ? 256 : 128) / 32;
   __shared__ B128 s_rows[kWarpsPerBlock][kMaxQueryNodes];
@@ -89,7 +90,7 @@ __global__ void __launch_bounds__(ROUNDS <= 2 ? 256 : 128) pair_filter_kernel(Pa
       if (lane == 0) a.vcounts[dg] = 0u;
       continue;
     }
-    DataNodes<ROUNDS> dn;
+    DataNodes<ROUNDS, PWMAX> dn;
 #pragma unroll
     for (int r = 0; r < ROUNDS; ++r) {
       const uint32_t v = lane + 32 * r;
@@ -105,16 +106,11 @@ __global__ void __launch_bounds__(ROUNDS <= 2 ? 256 : 128) pair_filter_kernel(Pa
       dn.p[r][1] = w23.y;
       dn.p[r][2] = w45.x;
       dn.p[r][3] = w45.y;
+      uint64_t sh[kMaxSteps];
 #pragma unroll
-      for (int k = 0; k < kMaxSteps; k += 2) {
-        if (k < R) {
-          const ulonglong2 s = *reinterpret_cast<const ulonglong2*>(rec + 6 + k);
-          dn.sh[r][k] = s.x;
-          dn.sh[r][k + 1] = s.y;
-        } else {
-          dn.sh[r][k] = dn.sh[r][k + 1] = 0;
-        }
-      }
+      for (int k = 0; k < kMaxSteps; ++k) sh[k] = k < R ? rec[6 + k] : 0ull;
+#pragma unroll
+      for (int w = 0; w < PWMAX; ++w) dn.sh[r][w] = uint32_t(w) < a.sp.PW ? packed_word(sh, R, w, a.sp) : 0ull;
     }
     const uint64_t dhist = a.ds.ghist[dg];
     const uint32_t dlab = a.ds.glabset[dg];
@@ -147,7 +143,8 @@ __global__ void __launch_bounds__(ROUNDS <= 2 ? 256 : 128) pair_filter_kernel(Pa
             __syncwarp();
             c = rows[src];  // identical record, evaluated earlier in this pair
           } else {
-            c = eval_rows<ROUNDS>(dn, a.qs.frec + uint64_t(kRecWords) * (qoff + ul), R);
+            c = eval_rows<ROUNDS, PWMAX>(dn, a.qs.frec + uint64_t(kRecWords) * (qoff + ul),
+                                         a.qpack + 8 * (uint64_t(qoff) + ul), a.sp.PW);
             if (!b_any(c)) {
               valid = false;
               break;
@@ -185,21 +182,46 @@ __global__ void __launch_bounds__(ROUNDS <= 2 ? 256 : 128) pair_filter_kernel(Pa
   }
 }
 
+__global__ void pack_query_shells_kernel(DGraphs q, DSigs qs, ShellPack sp, uint64_t* qpack) {
+  for (uint64_t u = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; u < q.N; u += uint64_t(gridDim.x) * blockDim.x) {
+    uint64_t sh[kMaxSteps];
+    for (int k = 0; k < kMaxSteps; ++k) sh[k] = k < qs.R ? qs.frec[uint64_t(kRecWords) * u + 6 + k] : 0ull;
+    for (int w = 0; w < 8; ++w) qpack[8 * u + w] = uint32_t(w) < sp.PW ? packed_word(sh, qs.R, w, sp) : 0ull;
+  }
+}
+
+template <int ROUNDS, int PWMAX>
+void launch_rounds(const PairFilterArgs& a, unsigned blocks, unsigned threads, cudaStream_t st) {
+  pair_filter_kernel<ROUNDS, PWMAX><<<blocks, threads, 0, st>>>(a); note_launch();
+}
+
+template <int ROUNDS>
+void launch_pw(const PairFilterArgs& a, unsigned blocks, unsigned threads, cudaStream_t st) {
+  if (a.sp.PW <= 2) launch_rounds<ROUNDS, 2>(a, blocks, threads, st);
+  else if (a.sp.PW <= 4) launch_rounds<ROUNDS, 4>(a, blocks, threads, st);
+  else launch_rounds<ROUNDS, 8>(a, blocks, threads, st);
+}
+
 }  // namespace
+
+cudaError_t launch_pack_query_shells(const DGraphs& q, const DSigs& qs, ShellPack sp, uint64_t* qpack,
+                                     cudaStream_t st) {
+  if (q.N == 0) return cudaSuccess;
+  const uint64_t want = (q.N + 127) / 128, cap = uint64_t(sm_count()) * 4;
+  pack_query_shells_kernel<<<unsigned(want < cap ? want : cap), 128, 0, st>>>(q, qs, sp, qpack); note_launch();
+  return cudaGetLastError();
+}
 
 cudaError_t launch_pair_filter(const PairFilterArgs& a, int rounds, cudaStream_t st) {
   if (a.class_end <= a.class_begin) return cudaSuccess;
   const uint32_t graphs = a.class_end - a.class_begin;
-  const int sms = sm_count();
+  const uint64_t sms = uint64_t(sm_count());
   if (rounds <= 1) {
-    unsigned blocks = unsigned(std::min<uint64_t>((graphs + 7) / 8, uint64_t(sms) * 8));
-    pair_filter_kernel<1><<<blocks, 256, 0, st>>>(a); note_launch();
+    launch_pw<1>(a, unsigned(std::min<uint64_t>((graphs + 7) / 8, sms * 8)), 256, st);
   } else if (rounds == 2) {
-    unsigned blocks = unsigned(std::min<uint64_t>((graphs + 7) / 8, uint64_t(sms) * 6));
-    pair_filter_kernel<2><<<blocks, 256, 0, st>>>(a); note_launch();
+    launch_pw<2>(a, unsigned(std::min<uint64_t>((graphs + 7) / 8, sms * 8)), 256, st);
   } else {
-    unsigned blocks = unsigned(std::min<uint64_t>((graphs + 3) / 4, uint64_t(sms) * 6));
-    pair_filter_kernel<4><<<blocks, 128, 0, st>>>(a); note_launch();
+    launch_pw<4>(a, unsigned(std::min<uint64_t>((graphs + 3) / 4, sms * 8)), 128, st);
   }
   return cudaGetLastError();
 }

@@ -178,7 +178,15 @@ def run_ours(args) -> None:
 
     if args.once:  # one pipeline run, for profilers
         total = step()
-        print(json.dumps({"once": True, "order": args.order, "total": int(total), **ctx.stats()}), flush=True)
+        st = ctx.stats()
+        e = np.sort(ctx.pair_expansions().astype(np.float64))[::-1]
+        c = ctx.pair_counts()
+        dist_ = {"pair_exp_max": float(e[0]) if len(e) else 0.0,
+                 "pair_exp_p99": float(np.percentile(e, 99)) if len(e) else 0.0,
+                 "pair_exp_top100_share": float(e[:100].sum() / max(e.sum(), 1.0)),
+                 "pair_count_max": int(c.max()) if len(c) else 0,
+                 "pairs_with_work": int((e > 0).sum())}
+        print(json.dumps({"once": True, "order": args.order, "total": int(total), **st, **dist_}), flush=True)
         ctx.close()
         return
     for _ in range(args.warmup):

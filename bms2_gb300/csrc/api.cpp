@@ -185,8 +185,12 @@ int join_records(bms_ctx* c, int mode, int order, int sem, bool log_vertices) {
   CK(cudaMemsetAsync(c->pair_exp.p, 0, sizeof(unsigned long long) * c->rec_cap, c->st));
   CK(cudaMemsetAsync(c->pair_flag.p, 0, sizeof(uint32_t) * c->rec_cap, c->st));
   Counters* ctr = c->ctr.as<Counters>();
-  CK(launch_task_emit(c->recs.as<PairRec>(), c->rec_cap, c->q.dg(), order_of(c), c->arena.as<uint64_t>(),
-                      c->tasks.as<Task>(), c->task_cap, ctr, c->errflag.as<uint32_t>() + 2, c->st));
+  // one task per pair, or per (pair, root) when the schedule splits pairs; the
+  // literal reference DFS restarts its visited set per root, so it always splits
+  const int per_pair = (sem == BMS_SEM_REFERENCE_DFS || c->sched.split_depth[0] >= 1) ? 0 : 1;
+  if (!per_pair)
+    CK(launch_task_emit(c->recs.as<PairRec>(), c->rec_cap, c->q.dg(), order_of(c), c->arena.as<uint64_t>(),
+                        c->tasks.as<Task>(), c->task_cap, ctr, c->errflag.as<uint32_t>() + 2, c->st));
   if (log_vertices) {
     CK(c->vertex_exp.ensure(sizeof(unsigned long long) * (c->q.N ? c->q.N : 1)));
     CK(cudaMemsetAsync(c->vertex_exp.p, 0, sizeof(unsigned long long) * (c->q.N ? c->q.N : 1), c->st));
@@ -198,8 +202,10 @@ int join_records(bms_ctx* c, int mode, int order, int sem, bool log_vertices) {
   ja.o = order_of(c);
   ja.recs = c->recs.as<PairRec>();
   ja.arena = c->arena.as<uint64_t>();
+  ja.rec_cap = c->rec_cap;
   ja.tasks = c->tasks.as<Task>();
   ja.task_cap = c->task_cap;
+  ja.per_pair = per_pair;
   ja.ctr = ctr;
   ja.pair_count = c->pair_count.as<unsigned long long>();
   ja.pair_exp = c->pair_exp.as<unsigned long long>();
@@ -210,7 +216,7 @@ int join_records(bms_ctx* c, int mode, int order, int sem, bool log_vertices) {
   ja.literal = sem == BMS_SEM_REFERENCE_DFS;
   ja.steps = c->join_steps;
   const int bucket = 0;
-  const int bps = c->sched.blocks_per_sm[bucket] ? int(c->sched.blocks_per_sm[bucket]) : 4;
+  const int bps = c->sched.blocks_per_sm[bucket] ? int(c->sched.blocks_per_sm[bucket]) : 3;
   const int wpb = c->sched.warps_per_block[bucket] ? int(c->sched.warps_per_block[bucket]) : 8;
   CK(launch_join(ja, sm_count() * bps, wpb * 32, c->st));
   CK(cudaEventRecord(c->ev[EV_JOIN], c->st));
@@ -298,8 +304,8 @@ int bms_create(int device, bms_ctx** out) {
   const uint32_t bounds[BMS_SCHED_BUCKETS] = {8, 16, 32, 64};
   for (int i = 0; i < BMS_SCHED_BUCKETS; ++i) {
     c->sched.max_query_nodes[i] = bounds[i];
-    c->sched.split_depth[i] = 1;
-    c->sched.blocks_per_sm[i] = 4;
+    c->sched.split_depth[i] = 0;
+    c->sched.blocks_per_sm[i] = 3;
     c->sched.warps_per_block[i] = 8;
   }
   *out = c;
@@ -482,6 +488,7 @@ int bms_join(bms_ctx* c, int mode, int order, int sem, uint64_t* total) {
                            c->qidx.as<uint32_t>(), c->row_off.as<uint32_t>(), c->recs.as<PairRec>(),
                            c->arena.as<uint64_t>(), c->st));
     CK(launch_set_counter(&c->ctr.as<Counters>()->recs, T, c->st));
+    CK(launch_set_counter(&c->ctr.as<Counters>()->recs_wide, T, c->st));  // GMCR order mixes sizes
     r = join_records(c, mode, order, sem, mode == BMS_COUNT_ALL && order == BMS_ORDER_GMCR && sem == BMS_SEM_EXACT);
     if (r) return r;
     CK(cudaMemcpyAsync(c->h_T, c->gmcr_off.as<uint32_t>() + c->d.G, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->st));
@@ -585,6 +592,9 @@ int run_fused(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total, 
     pa.class_end = c->class_end[k];
     pa.class_id = k;
     CK(launch_pair_filter(pa, rounds[k], c->st));
+    if (k == 2)  // records so far come from data graphs of more than 64 nodes
+      CK(cudaMemcpyAsync(&pa.ctr->recs_wide, &pa.ctr->recs, sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
+                         c->st));
   }
   CK(cudaEventRecord(c->ev[EV_FILTER], c->st));
   CK(launch_scan_u32(c->vcounts.as<uint32_t>(), c->gmcr_off.as<uint32_t>(), D, c->scan_scratch.as<uint32_t>(), c->st));
@@ -646,6 +656,7 @@ int bms::rejoin_timed(bms_ctx* c, int bps, int wpb, int steps, float* ms) {
   if (!c->have_results) return fail(c, BMS_ESTATE, "run the pipeline first");
   Counters* ctr = c->ctr.as<Counters>();
   CK(cudaMemsetAsync(&ctr->task_fetch, 0, sizeof(unsigned long long), c->st));
+  CK(cudaMemsetAsync(&ctr->task_fetch_wide, 0, sizeof(unsigned long long), c->st));
   CK(cudaMemsetAsync(c->pair_count.p, 0, sizeof(unsigned long long) * c->rec_cap, c->st));
   CK(cudaMemsetAsync(c->pair_exp.p, 0, sizeof(unsigned long long) * c->rec_cap, c->st));
   CK(cudaMemsetAsync(c->pair_flag.p, 0, sizeof(uint32_t) * c->rec_cap, c->st));
@@ -656,8 +667,10 @@ int bms::rejoin_timed(bms_ctx* c, int bps, int wpb, int steps, float* ms) {
   ja.o = order_of(c);
   ja.recs = c->recs.as<PairRec>();
   ja.arena = c->arena.as<uint64_t>();
+  ja.rec_cap = c->rec_cap;
   ja.tasks = c->tasks.as<Task>();
   ja.task_cap = c->task_cap;
+  ja.per_pair = (c->last_sem == BMS_SEM_REFERENCE_DFS || c->sched.split_depth[0] >= 1) ? 0 : 1;
   ja.ctr = ctr;
   ja.pair_count = c->pair_count.as<unsigned long long>();
   ja.pair_exp = c->pair_exp.as<unsigned long long>();
@@ -803,7 +816,7 @@ int bms_set_schedule(bms_ctx* c, const bms_schedule* s) {
   if (!s) return fail(c, BMS_EINVAL, "schedule is null");
   for (int i = 0; i < BMS_SCHED_BUCKETS; ++i)
     if (s->blocks_per_sm[i] > 32 || s->warps_per_block[i] == 0 || s->warps_per_block[i] > 32 ||
-        (s->split_depth[i] != 1 && s->split_depth[i] != 2))
+        s->split_depth[i] > 1)
       return fail(c, BMS_EINVAL, "schedule entry out of range");
   c->sched = *s;
   return BMS_OK;

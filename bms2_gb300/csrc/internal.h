@@ -81,7 +81,8 @@ struct Counters {
   unsigned long long total;       // sum of per-pair counts
   unsigned long long expansions;  // sum of per-pair expansions
   unsigned long long incomplete;  // pairs that hit the expansion budget
-  unsigned long long pad;
+  unsigned long long recs_wide;   // records [0, recs_wide) come from data graphs of > 64 nodes
+  unsigned long long task_fetch_wide;  // join work-stealing head of the two-word search
 };
 
 // ----------------------------------------------------------------- launchers
@@ -179,9 +180,11 @@ struct JoinArgs {
   DSigs ds;  // adjacency rows of the data side
   DOrder o;
   const PairRec* recs;
+  uint64_t rec_cap;
   const uint64_t* arena;
-  const Task* tasks;
+  const Task* tasks;               // (pair, root) tasks when per_pair == 0
   uint64_t task_cap;
+  int per_pair;                    // 1: one task per record (all its roots)
   Counters* ctr;
   unsigned long long* pair_count;  // per record
   unsigned long long* pair_exp;    // per record

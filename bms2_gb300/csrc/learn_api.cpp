@@ -298,7 +298,7 @@ int bms_autotune(bms_ctx* c, int R, int mode, int order, bms_schedule* out) {
   struct Shape {
     int bps, wpb, steps;
   };
-  const Shape shapes[] = {{2, 8, 32}, {4, 8, 32}, {8, 4, 32}, {4, 4, 32}, {8, 8, 16}, {4, 8, 64}, {6, 8, 32}, {2, 16, 32}};
+  const Shape shapes[] = {{2, 8, 32}, {3, 8, 32}, {4, 8, 32}, {6, 4, 32}, {3, 8, 16}, {3, 8, 64}, {2, 16, 32}};
   float best = 3.0e38f;
   Shape pick = shapes[1];
   for (const Shape& sh : shapes) {
@@ -316,7 +316,6 @@ int bms_autotune(bms_ctx* c, int R, int mode, int order, bms_schedule* out) {
   for (int b = 0; b < BMS_SCHED_BUCKETS; ++b) {
     c->sched.blocks_per_sm[b] = uint32_t(pick.bps);
     c->sched.warps_per_block[b] = uint32_t(pick.wpb);
-    c->sched.split_depth[b] = 1;
     c->sched.ms[b] = best;
   }
   c->join_steps = pick.steps;

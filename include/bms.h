@@ -243,14 +243,15 @@ int bms_model_load(bms_ctx* ctx, const char* path);
 int bms_model_predict(bms_ctx* ctx, float* cost, uint8_t* order);
 
 /* ------------------------------------------------------------ scheduling */
-/* Size-bucketed schedule of the persistent join.  Buckets are keyed by the
- * query's node count class; each entry picks lanes cooperating per task and the
- * DFS split depth.  bms_autotune times candidate schedules on the loaded
- * workload and installs the fastest per bucket. */
+/* Schedule of the persistent join: task granularity (split_depth 0 = one
+ * task per pair, 1 = one task per (pair, root)), launch shape and DFS steps
+ * between refills.  The table has one row per query-size bucket; the single
+ * persistent launch uses the shape of bucket 0.  bms_autotune times candidate
+ * schedules on the loaded workload and installs the fastest. */
 #define BMS_SCHED_BUCKETS 4
 typedef struct {
   uint32_t max_query_nodes[BMS_SCHED_BUCKETS]; /* bucket upper bounds */
-  uint32_t split_depth[BMS_SCHED_BUCKETS];     /* 1 = (pair, root) tasks, 2 = (pair, root, second) */
+  uint32_t split_depth[BMS_SCHED_BUCKETS];     /* 0 = (pair) tasks, 1 = (pair, root) tasks */
   uint32_t blocks_per_sm[BMS_SCHED_BUCKETS];
   uint32_t warps_per_block[BMS_SCHED_BUCKETS];
   float ms[BMS_SCHED_BUCKETS];                 /* measured by the autotuner */

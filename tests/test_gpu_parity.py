@@ -267,3 +267,18 @@ def test_expansion_budget_marks_pairs_incomplete(ctx):
         ctx.set_expansion_budget(0)
     full = ctx.run(0, COUNT_ALL, ORDER_GMCR, SEM_EXACT)
     assert full == oracle.run_pipeline(q, d, 0).total
+
+
+@pytest.mark.parametrize("split", [0, 1])
+def test_task_granularity_does_not_change_counts(ctx, wl, split):
+    q, d = wl
+    want = oracle.run_pipeline(q, d, 3)
+    load(ctx, q, d)
+    sched = ctx.schedule()
+    try:
+        ctx.set_schedule({**sched, "split_depth": [split] * 4})
+        assert ctx.run(3, COUNT_ALL, ORDER_GMCR, SEM_EXACT) == want.total
+        assert np.array_equal(ctx.pair_counts(), want.counts)
+        assert ctx.run(3, FIND_FIRST, ORDER_GMCR, SEM_EXACT) == int((want.counts > 0).sum())
+    finally:
+        ctx.set_schedule(sched)

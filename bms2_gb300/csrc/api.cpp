@@ -259,6 +259,102 @@ int validate_modes(bms_ctx* c, int mode, int order, int sem) {
 
 int run_fused(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total, bool log_vertices, int attempt);
 
+int run_ballot_filter(bms_ctx* c, const ShellPack& sp, int sem) {
+  PairFilterArgs pa{};
+  pa.qpack = c->qpack.as<uint64_t>();
+  pa.sp = sp;
+  pa.q = c->q.dg();
+  pa.d = c->d.dg();
+  pa.qs = c->q.ds();
+  pa.ds = c->d.ds();
+  pa.filter_order = c->filter_order.as<uint8_t>();
+  pa.dup = c->filter_dup.as<uint8_t>();
+  pa.dperm = c->dperm.as<uint32_t>();
+  pa.valid = c->valid.as<uint32_t>();
+  pa.QW = c->QW;
+  pa.vcounts = c->vcounts.as<uint32_t>();
+  pa.recs = c->recs.as<PairRec>();
+  pa.rec_cap = c->rec_cap;
+  pa.arena = c->arena.as<uint64_t>();
+  pa.row_cap = c->row_cap;
+  pa.ctr = c->ctr.as<Counters>();
+  pa.err = c->errflag.as<uint32_t>() + 2;
+  pa.skip_by_labels = sem == BMS_SEM_EXACT;
+  pa.cand_sum = nullptr;
+  const int rounds[3] = {1, 2, 4};
+  for (int k = 2; k >= 0; --k) {
+    pa.class_begin = c->class_begin[k];
+    pa.class_end = c->class_end[k];
+    pa.class_id = k;
+    CK(launch_pair_filter(pa, rounds[k], c->st));
+    if (k == 2)  // records so far come from data graphs of more than 64 nodes
+      CK(cudaMemcpyAsync(&pa.ctr->recs_wide, &pa.ctr->recs, sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
+                         c->st));
+  }
+  return BMS_OK;
+}
+
+// Clause programs of the queries, then the sliced filter: data graphs of more
+// than 64 nodes first (two-word masks), then the rest (one word).
+int run_sliced_filter(bms_ctx* c, const ShellPack& sp, int R, int sem) {
+  const uint64_t Qn = c->q.N ? c->q.N : 1;
+  const uint64_t per_node = 6 + uint64_t(R) * 16 + 256;
+  CK(c->prog_len.ensure(sizeof(uint32_t) * Qn));
+  CK(c->prog_off.ensure(sizeof(uint32_t) * (Qn + 1)));
+  CK(c->prog.ensure(sizeof(uint16_t) * Qn * per_node));
+  CK(c->prog_slow.ensure(Qn));
+  CK(c->prog_used.ensure(sizeof(uint32_t) * (kClauseIds / 32 + 1)));
+  CK(c->prog_remap.ensure(sizeof(uint16_t) * kClauseIds));
+  CK(c->prog_ids.ensure(sizeof(uint16_t) * kClauseIds));
+  CK(c->prog_nused.ensure(sizeof(uint32_t)));
+  CK(c->tmp.ensure(sizeof(uint32_t) * scan_scratch_words(Qn)));
+  CK(launch_query_programs(c->q.dg(), c->q.ds(), sp, c->prog_len.as<uint32_t>(), c->prog_off.as<uint32_t>(),
+                           c->tmp.as<uint32_t>(), c->prog_used.as<uint32_t>(), c->prog_remap.as<uint16_t>(),
+                           c->prog_ids.as<uint16_t>(), c->prog_nused.as<uint32_t>(), c->prog.as<uint16_t>(),
+                           c->prog_slow.as<uint8_t>(), Qn * per_node, nullptr, c->st));
+  SlicedArgs a{};
+  a.q = c->q.dg();
+  a.d = c->d.dg();
+  a.qs = c->q.ds();
+  a.ds = c->d.ds();
+  a.filter_order = c->filter_order.as<uint8_t>();
+  a.dup = c->filter_dup.as<uint8_t>();
+  a.prog_off = c->prog_off.as<uint32_t>();
+  a.prog = c->prog.as<uint16_t>();
+  a.slow = c->prog_slow.as<uint8_t>();
+  a.used_ids = c->prog_ids.as<uint16_t>();
+  a.n_used = c->prog_nused.as<uint32_t>();
+  uint32_t cap = 16 + 16 + 32 + 256 + uint32_t(R) * sp.K * 15;
+  a.n_used_cap = cap < kClauseIds ? cap : kClauseIds;
+  a.sp = sp;
+  a.dperm = c->dperm.as<uint32_t>();
+  a.valid = c->valid.as<uint32_t>();
+  a.QW = c->QW;
+  a.vcounts = c->vcounts.as<uint32_t>();
+  a.recs = c->recs.as<PairRec>();
+  a.rec_cap = c->rec_cap;
+  a.arena = c->arena.as<uint64_t>();
+  a.row_cap = c->row_cap;
+  a.ctr = c->ctr.as<Counters>();
+  a.err = c->errflag.as<uint32_t>() + 2;
+  a.skip_by_labels = sem == BMS_SEM_EXACT;
+  // two-word graphs (> 64 nodes)
+  a.class_begin = c->class_begin[2];
+  a.class_end = c->class_end[2];
+  a.class_id = 2;
+  size_t smem = sliced_smem_bytes(a, 2);
+  if (smem > (220u << 10)) return fail(c, BMS_EUNSUPPORTED, "too many queries for the sliced filter's shared memory");
+  CK(launch_sliced_filter(a, 2, smem, c->st));
+  CK(cudaMemcpyAsync(&a.ctr->recs_wide, &a.ctr->recs, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, c->st));
+  // one-word graphs (classes 1 and 0 are contiguous in the permutation)
+  a.class_begin = c->class_begin[1];
+  a.class_end = c->class_end[0];
+  a.class_id = 1;
+  smem = sliced_smem_bytes(a, 1);
+  CK(launch_sliced_filter(a, 1, smem, c->st));
+  return BMS_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -338,6 +434,22 @@ int bms_set_expansion_budget(bms_ctx* c, uint64_t budget) {
   GUARD(c);
   c->budget = budget;
   return BMS_OK;
+}
+
+int bms_set_option(bms_ctx* c, int option, int64_t value) {
+  GUARD(c);
+  switch (option) {
+    case BMS_OPT_FILTER_KERNEL:
+      if (value != BMS_FILTER_SLICED && value != BMS_FILTER_BALLOT) return fail(c, BMS_EINVAL, "unknown filter kernel");
+      c->filter_kernel = int(value);
+      return BMS_OK;
+    case BMS_OPT_JOIN_STEPS:
+      if (value < 1 || value > 4096) return fail(c, BMS_EINVAL, "join steps must be in [1, 4096]");
+      c->join_steps = int(value);
+      return BMS_OK;
+    default:
+      return fail(c, BMS_EINVAL, "unknown option");
+  }
 }
 
 int bms_set_logging(bms_ctx* c, int vertex_expansions) {
@@ -565,36 +677,12 @@ int run_fused(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total, 
   CK(c->qpack.ensure(sizeof(uint64_t) * 8 * (c->q.N ? c->q.N : 1)));
   CK(launch_pack_query_shells(c->q.dg(), c->q.ds(), sp, c->qpack.as<uint64_t>(), c->st));
   CK(cudaEventRecord(c->ev[EV_SIG], c->st));
-  PairFilterArgs pa{};
-  pa.qpack = c->qpack.as<uint64_t>();
-  pa.sp = sp;
-  pa.q = c->q.dg();
-  pa.d = c->d.dg();
-  pa.qs = c->q.ds();
-  pa.ds = c->d.ds();
-  pa.filter_order = c->filter_order.as<uint8_t>();
-  pa.dup = c->filter_dup.as<uint8_t>();
-  pa.dperm = c->dperm.as<uint32_t>();
-  pa.valid = c->valid.as<uint32_t>();
-  pa.QW = c->QW;
-  pa.vcounts = c->vcounts.as<uint32_t>();
-  pa.recs = c->recs.as<PairRec>();
-  pa.rec_cap = c->rec_cap;
-  pa.arena = c->arena.as<uint64_t>();
-  pa.row_cap = c->row_cap;
-  pa.ctr = c->ctr.as<Counters>();
-  pa.err = c->errflag.as<uint32_t>() + 2;
-  pa.skip_by_labels = sem == BMS_SEM_EXACT;
-  pa.cand_sum = learned ? c->cand_sum.as<unsigned int>() : nullptr;
-  const int rounds[3] = {1, 2, 4};
-  for (int k = 2; k >= 0; --k) {
-    pa.class_begin = c->class_begin[k];
-    pa.class_end = c->class_end[k];
-    pa.class_id = k;
-    CK(launch_pair_filter(pa, rounds[k], c->st));
-    if (k == 2)  // records so far come from data graphs of more than 64 nodes
-      CK(cudaMemcpyAsync(&pa.ctr->recs_wide, &pa.ctr->recs, sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
-                         c->st));
+  if (c->filter_kernel == BMS_FILTER_BALLOT) {
+    int r2 = run_ballot_filter(c, sp, sem);
+    if (r2) return r2;
+  } else {
+    int r2 = run_sliced_filter(c, sp, R, sem);
+    if (r2) return r2;
   }
   CK(cudaEventRecord(c->ev[EV_FILTER], c->st));
   CK(launch_scan_u32(c->vcounts.as<uint32_t>(), c->gmcr_off.as<uint32_t>(), D, c->scan_scratch.as<uint32_t>(), c->st));

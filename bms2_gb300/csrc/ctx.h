@@ -89,7 +89,7 @@ struct bms_ctx {
   uint64_t rec_cap = 0, row_cap = 0, task_cap = 0;
   DevBuf dperm;
   uint32_t class_begin[3] = {0, 0, 0}, class_end[3] = {0, 0, 0};
-  DevBuf filter_order, filter_dup, qpack, label_count, perm, dadj, vertex_exp, cand_sum, recs_per_query, features, cost;
+  DevBuf filter_order, filter_dup, qpack, prog_len, prog_off, prog, prog_slow, prog_used, prog_remap, prog_ids, prog_nused, label_count, perm, dadj, vertex_exp, cand_sum, recs_per_query, features, cost;
   bool have_results = false, have_vexp = false;
   int last_mode = 0, last_order = 0, last_sem = 0;
   DevBuf tmp;
@@ -97,6 +97,7 @@ struct bms_ctx {
   DevBuf model_master, model_bf16, adam_m, adam_v, grad, grad_partial, loss_buf, train_x, train_y, pred;
   bool model_set = false;
   bool log_vertices = false;
+  int filter_kernel = 0;  // BMS_FILTER_SLICED or BMS_FILTER_BALLOT
   int join_steps = 32;
   uint64_t budget = 0;
   bms_schedule sched{};

@@ -155,6 +155,42 @@ struct PairFilterArgs {
 };
 cudaError_t launch_pair_filter(const PairFilterArgs& a, int rounds, cudaStream_t st);
 
+// Bit-sliced fused filter (k_sliced.cu): per query node a clause program (mask
+// ids), per data graph a shared-memory table of the used clause masks.
+struct SlicedArgs {
+  DGraphs q, d;
+  DSigs qs, ds;
+  const uint8_t* filter_order;  // [Q*64]
+  const uint8_t* dup;           // [Q*64]
+  const uint32_t* prog_off;     // [Qn+1]
+  const uint16_t* prog;         // compact mask indices
+  const uint8_t* slow;          // [Qn] clauses outside the table
+  const uint16_t* used_ids;     // compact index -> clause id
+  const uint32_t* n_used;       // number of used clauses (device)
+  uint32_t n_used_cap;          // bound used to size shared memory
+  ShellPack sp;
+  const uint32_t* dperm;
+  uint32_t class_begin, class_end;
+  int class_id;
+  uint32_t* valid;
+  uint32_t QW;
+  uint32_t* vcounts;
+  PairRec* recs;
+  uint64_t rec_cap;
+  uint64_t* arena;
+  uint64_t row_cap;
+  Counters* ctr;
+  uint32_t* err;
+  int skip_by_labels;
+};
+constexpr uint32_t kClauseIds = 320 + kMaxSteps * 16 * 15;
+cudaError_t launch_query_programs(const DGraphs& q, const DSigs& qs, ShellPack sp, uint32_t* len, uint32_t* prog_off,
+                                  uint32_t* scan_scratch, uint32_t* used, uint16_t* remap, uint16_t* used_ids,
+                                  uint32_t* n_used, uint16_t* prog, uint8_t* slow, uint64_t prog_cap,
+                                  uint32_t* prog_total_host, cudaStream_t st);
+size_t sliced_smem_bytes(const SlicedArgs& a, int words);
+cudaError_t launch_sliced_filter(const SlicedArgs& a, int words, size_t smem, cudaStream_t st);
+
 // exclusive scan of n uint32 values into out[0..n] (out[n] = total); scratch
 // must hold scan_scratch_words(n) words.
 size_t scan_scratch_words(uint64_t n);

@@ -1,0 +1,419 @@
+// Fused filter + refine + GMCR validity with bit-sliced threshold masks.
+//
+// The reference tests every (query node, data node) pair of the batch with the
+// full predicate (filterCandidates, isomorphism.hpp:30-104, then R passes of
+// refineCandidates, :106-203) and then every (query, data graph) pair for
+// validity (GMCR kernel 1, gmcr.hpp:54-88).  Every clause of that predicate is
+// a threshold on one data-node attribute:
+//   label == l (or any label for the wildcard)      -> LAB[l]
+//   degree >= k                                     -> DEG[k]
+//   cycle count of type t >= c (4 types)            -> CYC[t][c]
+//   path-filter bit b set (the query's bit b is set) -> PATH[b]
+//   shell k nibble of label l >= c                  -> SHELL[k][l][c]
+// So for one data graph, the candidate row of a query node is the AND of the
+// node masks of the clauses its own signature selects.  A block owns one data
+// graph at a time: it builds, in shared memory, the masks any query uses (one
+// thread per mask, a loop over the graph's nodes), then evaluates the queries
+// level by level in their selectivity order with one thread per still-alive
+// query: each evaluation is a walk over the query node's precomputed clause
+// list ("program"), ANDing 64- or 128-bit masks.  A query dies at its first
+// empty row; its output rows are allocated once its first row is non-empty.
+// Queries whose label multiset cannot embed (EXACT semantics) keep being tested
+// for GMCR validity but write no rows and reach no join.
+#include "device_common.cuh"
+
+namespace bms {
+namespace {
+
+constexpr uint32_t kMLab = 0, kMDeg = 16, kMCyc = 32, kMPath = 64, kMShell = 320;
+constexpr uint32_t kMaxMaskIds = kClauseIds;  // 2240
+constexpr uint8_t kSlowLabel = 1, kSlowDeg = 2, kSlowCyc = 4;
+constexpr uint32_t kNoRow = 0xFFFFFFFFu;
+
+template <int W>
+struct Mask {
+  uint64_t w[W];
+};
+template <int W>
+__device__ __forceinline__ Mask<W> mand(Mask<W> a, Mask<W> b) {
+#pragma unroll
+  for (int i = 0; i < W; ++i) a.w[i] &= b.w[i];
+  return a;
+}
+template <int W>
+__device__ __forceinline__ bool many(Mask<W> a) {
+  uint64_t x = 0;
+#pragma unroll
+  for (int i = 0; i < W; ++i) x |= a.w[i];
+  return x != 0;
+}
+template <int W>
+__device__ __forceinline__ Mask<W> mlow(uint32_t m) {
+  Mask<W> r;
+#pragma unroll
+  for (int i = 0; i < W; ++i) {
+    const uint32_t lo = 64u * i;
+    r.w[i] = m <= lo ? 0ull : (m >= lo + 64 ? ~0ull : ((uint64_t(1) << (m - lo)) - 1));
+  }
+  return r;
+}
+template <int W>
+__device__ __forceinline__ B128 to128(Mask<W> a) {
+  return W == 1 ? B128{a.w[0], 0ull} : B128{a.w[0], a.w[W - 1]};
+}
+
+// ------------------------------------------------------------- query side
+// Clause list of one query node, most selective clauses first: label, degree,
+// cycles, shells, path bits.  Clauses that do not fit the mask table (labels
+// 16..254, degree > 16, cycle counts > 8) set a slow-path flag instead.
+template <bool kWrite>
+__device__ uint32_t query_clauses(const uint64_t* rec, int R, const ShellPack& sp, uint16_t* out, uint8_t* slow,
+                                  uint32_t* used) {
+  uint32_t n = 0;
+  auto emit = [&](uint32_t id) {
+    if (kWrite) out[n] = uint16_t(id);
+    else atomicOr(&used[id >> 5], 1u << (id & 31));
+    ++n;
+  };
+  uint8_t s = 0;
+  const uint32_t l = uint32_t(rec[0] & 0xFFu), deg = uint32_t(rec[0] >> 32);
+  if (l < 16) emit(kMLab + l);
+  else if (l != kWildcard) s |= kSlowLabel;
+  if (deg >= 1) {
+    if (deg <= 16) emit(kMDeg + deg - 1);
+    else s |= kSlowDeg;
+  }
+  for (int t = 0; t < 4; ++t) {
+    const uint32_t c = uint32_t(rec[1] >> (16 * t)) & 0xFFFFu;
+    if (c) {
+      if (c <= 8) emit(kMCyc + 8 * t + c - 1);
+      else s |= kSlowCyc;
+    }
+  }
+  for (int k = 0; k < R; ++k) {
+    const uint64_t sh = rec[6 + k];
+    for (uint32_t j = 0; j < sp.K; ++j) {
+      const uint32_t c = uint32_t(sh >> (4 * sp.pos[j])) & 15u;
+      if (c) emit(kMShell + (uint32_t(k) * sp.K + j) * 15 + c - 1);
+    }
+  }
+  for (int w = 0; w < 4; ++w)
+    for (uint64_t b = rec[2 + w]; b; b &= b - 1) emit(kMPath + 64 * w + uint32_t(__ffsll((long long)b) - 1));
+  if (kWrite && slow) *slow = s;
+  return n;
+}
+
+__global__ void program_count_kernel(DGraphs q, DSigs qs, ShellPack sp, uint32_t* len, uint32_t* used) {
+  for (uint64_t u = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; u < q.N; u += uint64_t(gridDim.x) * blockDim.x)
+    len[u] = query_clauses<false>(qs.frec + uint64_t(kRecWords) * u, qs.R, sp, nullptr, nullptr, used);
+}
+
+// compact index of every used mask id (single block)
+__global__ void program_compact_kernel(const uint32_t* used, uint16_t* remap, uint16_t* used_ids, uint32_t* n_used) {
+  __shared__ uint32_t base[kMaxMaskIds / 32 + 1];
+  if (threadIdx.x == 0) {
+    uint32_t b = 0;
+    for (uint32_t w = 0; w < kMaxMaskIds / 32; ++w) {
+      base[w] = b;
+      b += __popc(used[w]);
+    }
+    *n_used = b;
+  }
+  __syncthreads();
+  for (uint32_t id = threadIdx.x; id < kMaxMaskIds; id += blockDim.x) {
+    const uint32_t w = id >> 5, bit = id & 31u;
+    if ((used[w] >> bit) & 1u) {
+      const uint32_t k = base[w] + __popc(used[w] & ((1u << bit) - 1u));
+      remap[id] = uint16_t(k);
+      used_ids[k] = uint16_t(id);
+    }
+  }
+}
+
+__global__ void program_fill_kernel(DGraphs q, DSigs qs, ShellPack sp, const uint32_t* off, const uint16_t* remap,
+                                    uint16_t* prog, uint8_t* slow) {
+  for (uint64_t u = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; u < q.N; u += uint64_t(gridDim.x) * blockDim.x) {
+    uint16_t* p = prog + off[u];
+    const uint32_t n = query_clauses<true>(qs.frec + uint64_t(kRecWords) * u, qs.R, sp, p, slow + u, nullptr);
+    for (uint32_t i = 0; i < n; ++i) p[i] = remap[p[i]];
+  }
+}
+
+// ------------------------------------------------------------- data side
+
+template <int W>
+__device__ __forceinline__ bool clause_holds(uint32_t id, uint32_t v, const uint8_t* lab, const uint8_t* deg,
+                                             const uint64_t* cyc, const uint64_t* path, const uint64_t* sh, int R,
+                                             const ShellPack& sp) {
+  if (id < kMDeg) return lab[v] == id;
+  if (id < kMCyc) return uint32_t(deg[v]) >= id - kMDeg + 1;
+  if (id < kMPath) {
+    const uint32_t t = (id - kMCyc) >> 3, c = ((id - kMCyc) & 7u) + 1;
+    return ((cyc[v] >> (16 * t)) & 0xFFFFull) >= c;
+  }
+  if (id < kMShell) {
+    const uint32_t b = id - kMPath;
+    return (path[4 * v + (b >> 6)] >> (b & 63u)) & 1ull;
+  }
+  const uint32_t x = id - kMShell;
+  const uint32_t c = x % 15 + 1, kj = x / 15;
+  const uint32_t k = kj / sp.K, j = kj % sp.K;
+  return ((sh[uint32_t(R) * v + k] >> (4 * sp.pos[j])) & 15ull) >= c;
+}
+
+template <int W>
+__global__ void __launch_bounds__(256) sliced_filter_kernel(SlicedArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr uint32_t MAXN = 64 * W;
+  const int R = a.ds.R;
+  // shared layout
+  uint64_t* s_path = reinterpret_cast<uint64_t*>(smem);            // [MAXN*4]
+  uint64_t* s_cyc = s_path + 4 * MAXN;                              // [MAXN]
+  uint64_t* s_sh = s_cyc + MAXN;                                    // [MAXN*R]
+  Mask<W>* s_tab = reinterpret_cast<Mask<W>*>(s_sh + MAXN * (R > 0 ? R : 1));  // [n_used]
+  uint32_t* s_aq = reinterpret_cast<uint32_t*>(s_tab + (a.n_used_cap ? a.n_used_cap : 1));  // [2][Q] query | join << 31
+  uint32_t* s_as = s_aq + 2 * a.q.G;                                // [2][Q] first output row or kNoRow
+  uint32_t* s_valid = s_as + 2 * a.q.G;                             // [QW]
+  uint8_t* s_lab = reinterpret_cast<uint8_t*>(s_valid + a.QW);      // [MAXN]
+  uint8_t* s_deg = s_lab + MAXN;                                    // [MAXN]
+  __shared__ uint32_t s_count[2], s_graph, s_nvalid;
+  const uint32_t tid = threadIdx.x, lane = lane_id();
+  const uint32_t Q = a.q.G;
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) s_graph = atomicAdd(&a.ctr->work[a.class_id], 1u);
+    __syncthreads();
+    if (a.class_begin + s_graph >= a.class_end) break;
+    const uint32_t dg = a.dperm[a.class_begin + s_graph];
+    const uint32_t start = a.d.goff[dg], m = a.d.goff[dg + 1] - start;
+    // stage node attributes
+    for (uint32_t v = tid; v < m; v += blockDim.x) {
+      const uint64_t* rec = a.ds.frec + uint64_t(kRecWords) * (uint64_t(start) + v);
+      const uint64_t w0 = rec[0];
+      s_lab[v] = uint8_t(w0 & 0xFFu);
+      const uint32_t dgv = uint32_t(w0 >> 32);
+      s_deg[v] = uint8_t(dgv > 255u ? 255u : dgv);
+      s_cyc[v] = rec[1];
+      for (int w = 0; w < 4; ++w) s_path[4 * v + w] = rec[2 + w];
+      for (int k = 0; k < R; ++k) s_sh[uint32_t(R) * v + k] = rec[6 + k];
+    }
+    for (uint32_t w = tid; w < a.QW; w += blockDim.x) s_valid[w] = 0;
+    if (tid < 2) s_count[tid] = 0;
+    if (tid == 0) s_nvalid = 0;
+    __syncthreads();
+    // one mask per used clause
+    const uint32_t n_used = min(*a.n_used, a.n_used_cap);
+    for (uint32_t i = tid; i < n_used; i += blockDim.x) {
+      const uint32_t id = a.used_ids[i];
+      Mask<W> mk;
+#pragma unroll
+      for (int x = 0; x < W; ++x) mk.w[x] = 0;
+      for (uint32_t v = 0; v < m; ++v)
+        if (clause_holds<W>(id, v, s_lab, s_deg, s_cyc, s_path, s_sh, R, a.sp)) mk.w[v >> 6] |= uint64_t(1) << (v & 63u);
+      s_tab[i] = mk;
+    }
+    // screening: label set, more than one node, label multiset (join)
+    const uint64_t dhist = a.ds.ghist[dg];
+    const uint32_t dlab = a.ds.glabset[dg];
+    for (uint32_t qb = 0; qb < Q; qb += blockDim.x) {
+      const uint32_t qg = qb + tid;
+      bool p1 = false, p2 = false;
+      if (qg < Q && m > 0) {
+        const uint32_t n = a.q.goff[qg + 1] - a.q.goff[qg];
+        p1 = n > 1 && (a.qs.glabset[qg] & ~dlab) == 0;  // gmcr.hpp:64 and label presence
+        p2 = p1 && (!a.skip_by_labels || nib_le(a.qs.ghist[qg], dhist));
+      }
+      const uint32_t bal = __ballot_sync(0xffffffffu, p1);
+      uint32_t base = 0;
+      if (lane == 0 && bal) base = atomicAdd(&s_count[0], __popc(bal));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (p1) {
+        const uint32_t k = base + __popc(bal & ((1u << lane) - 1u));
+        s_aq[k] = qg | (p2 ? 0x80000000u : 0u);
+        s_as[k] = kNoRow;
+      }
+    }
+    __syncthreads();
+    const Mask<W> all = mlow<W>(m);
+    // levels
+    for (uint32_t level = 0, cur = 0;; ++level, cur ^= 1u) {
+      const uint32_t count = s_count[cur];
+      if (count == 0) break;
+      uint32_t* aq = s_aq + cur * Q;
+      uint32_t* as = s_as + cur * Q;
+      uint32_t* nq = s_aq + (cur ^ 1u) * Q;
+      uint32_t* ns = s_as + (cur ^ 1u) * Q;
+      const uint32_t rounds = (count + blockDim.x - 1) / blockDim.x;
+      for (uint32_t r = 0; r < rounds; ++r) {
+        const uint32_t i = r * blockDim.x + tid;
+        const bool live = i < count;
+        uint32_t qg = 0, row0 = kNoRow, n = 0, qoff = 0;
+        bool join = false, alive = false, done = false;
+        Mask<W> row;
+#pragma unroll
+        for (int x = 0; x < W; ++x) row.w[x] = 0;
+        uint32_t ul = 0;
+        if (live) {
+          const uint32_t e = aq[i];
+          qg = e & 0x7FFFFFFFu;
+          join = (e >> 31) != 0;
+          row0 = as[i];
+          qoff = a.q.goff[qg];
+          n = a.q.goff[qg + 1] - qoff;
+          ul = a.filter_order[uint64_t(qg) * kMaxQueryNodes + level];
+          const uint32_t src = a.dup[uint64_t(qg) * kMaxQueryNodes + ul];
+          if (src != 0xFFu) {
+            alive = true;  // same record as an earlier, non-empty row
+            if (join && row0 != kNoRow) {
+              const B128 c = ld_b128(a.arena + 2 * (uint64_t(row0) + src));
+              row.w[0] = c.lo;
+              if (W > 1) row.w[W - 1] = c.hi;
+            }
+          } else {
+            row = all;
+            const uint64_t u = uint64_t(qoff) + ul;
+            const uint32_t pb = a.prog_off[u], pe = a.prog_off[u + 1];
+            for (uint32_t p = pb; p < pe; ++p) {
+              row = mand(row, s_tab[a.prog[p]]);
+              if (((p - pb) & 7u) == 7u && !many(row)) break;
+            }
+            const uint8_t slow = a.slow[u];
+            if (slow && many(row)) {
+              const uint64_t rec0 = a.qs.frec[uint64_t(kRecWords) * u], rec1 = a.qs.frec[uint64_t(kRecWords) * u + 1];
+              const uint32_t ql = uint32_t(rec0 & 0xFFu), qd = uint32_t(rec0 >> 32);
+              for (uint32_t v = 0; v < m; ++v) {
+                bool ok = true;
+                if (slow & kSlowLabel) ok = ok && s_lab[v] == ql;
+                if (slow & kSlowDeg) {
+                  const uint64_t* dr = a.ds.frec + uint64_t(kRecWords) * (uint64_t(start) + v);
+                  ok = ok && uint32_t(dr[0] >> 32) >= qd;
+                }
+                if (slow & kSlowCyc) ok = ok && cyc_ge(s_cyc[v], rec1);
+                if (!ok) row.w[v >> 6] &= ~(uint64_t(1) << (v & 63u));
+              }
+            }
+            alive = many(row);
+          }
+          done = alive && level + 1 == n;
+        }
+        // output rows: allocated when the first row of a join-eligible query is non-empty
+        const bool need = live && alive && join && row0 == kNoRow;
+        const uint32_t nb = __ballot_sync(0xffffffffu, need);
+        if (nb) {
+          uint32_t incl = need ? n : 0u;
+          for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= uint32_t(d)) incl += y;
+          }
+          unsigned long long base = 0;
+          const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
+          if (lane == 31) base = atomicAdd(&a.ctr->rows, (unsigned long long)tot);
+          base = __shfl_sync(0xffffffffu, base, 31);
+          if (need) {
+            const unsigned long long b = base + incl - n;
+            if (b + n > a.row_cap) {
+              atomicOr(a.err, kErrOverflow);
+              join = false;
+            } else {
+              row0 = uint32_t(b);
+            }
+          }
+        }
+        if (live && alive && join && row0 != kNoRow) st_b128(a.arena + 2 * (uint64_t(row0) + ul), to128(row));
+        // finished queries: validity bit and record; others go on
+        if (done) {
+          atomicOr(&s_valid[qg >> 5], 1u << (qg & 31u));
+        }
+        const bool rec_need = done && join && row0 != kNoRow;
+        const uint32_t rb = __ballot_sync(0xffffffffu, rec_need);
+        if (rb) {
+          unsigned long long base = 0;
+          if (lane == __ffs(rb) - 1) base = atomicAdd(&a.ctr->recs, (unsigned long long)__popc(rb));
+          base = __shfl_sync(0xffffffffu, base, __ffs(rb) - 1);
+          if (rec_need) {
+            const unsigned long long k = base + __popc(rb & ((1u << lane) - 1u));
+            if (k < a.rec_cap) a.recs[k] = PairRec{qg, dg, 0u, row0};
+            else atomicOr(a.err, kErrOverflow);
+          }
+        }
+        const bool cont = live && alive && !done;
+        const uint32_t cb = __ballot_sync(0xffffffffu, cont);
+        if (cb) {
+          uint32_t base = 0;
+          if (lane == __ffs(cb) - 1) base = atomicAdd(&s_count[cur ^ 1u], __popc(cb));
+          base = __shfl_sync(0xffffffffu, base, __ffs(cb) - 1);
+          if (cont) {
+            const uint32_t k = base + __popc(cb & ((1u << lane) - 1u));
+            nq[k] = qg | (join ? 0x80000000u : 0u);
+            ns[k] = row0;
+          }
+        }
+      }
+      __syncthreads();
+      if (tid == 0) s_count[cur] = 0;
+      __syncthreads();
+    }
+    // validity bits and per-graph count
+    uint32_t nv = 0;
+    for (uint32_t w = tid; w < a.QW; w += blockDim.x) {
+      const uint32_t bits = s_valid[w];
+      a.valid[uint64_t(dg) * a.QW + w] = bits;
+      nv += __popc(bits);
+    }
+    for (int d = 16; d > 0; d >>= 1) nv += __shfl_down_sync(0xffffffffu, nv, d);
+    if (lane == 0 && nv) atomicAdd(&s_nvalid, nv);
+    __syncthreads();
+    if (tid == 0) a.vcounts[dg] = s_nvalid;
+  }
+}
+
+template <int W>
+size_t sliced_smem(const SlicedArgs& a) {
+  constexpr size_t MAXN = 64 * W;
+  const size_t R = size_t(a.ds.R > 0 ? a.ds.R : 1);
+  size_t b = 8 * (4 * MAXN + MAXN + MAXN * R);
+  b += sizeof(uint64_t) * W * (a.n_used_cap ? a.n_used_cap : 1);
+  b += 4 * (4 * size_t(a.q.G) + a.QW);
+  b += 2 * MAXN;
+  return (b + 15) & ~size_t(15);
+}
+
+}  // namespace
+
+size_t sliced_smem_bytes(const SlicedArgs& a, int words) { return words == 1 ? sliced_smem<1>(a) : sliced_smem<2>(a); }
+
+cudaError_t launch_query_programs(const DGraphs& q, const DSigs& qs, ShellPack sp, uint32_t* len, uint32_t* prog_off,
+                                  uint32_t* scan_scratch, uint32_t* used, uint16_t* remap, uint16_t* used_ids,
+                                  uint32_t* n_used, uint16_t* prog, uint8_t* slow, uint64_t prog_cap,
+                                  uint32_t* prog_total_host, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(used, 0, sizeof(uint32_t) * (kMaxMaskIds / 32 + 1), st);
+  if (e != cudaSuccess || q.N == 0) return e;
+  const uint64_t want = (q.N + 127) / 128, cap = uint64_t(sm_count()) * 4;
+  const unsigned blocks = unsigned(want < cap ? want : cap);
+  program_count_kernel<<<blocks, 128, 0, st>>>(q, qs, sp, len, used); note_launch();
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = launch_scan_u32(len, prog_off, q.N, scan_scratch, st)) != cudaSuccess) return e;
+  program_compact_kernel<<<1, 256, 0, st>>>(used, remap, used_ids, n_used); note_launch();
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  (void)prog_cap;
+  (void)prog_total_host;
+  program_fill_kernel<<<blocks, 128, 0, st>>>(q, qs, sp, prog_off, remap, prog, slow); note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sliced_filter(const SlicedArgs& a, int words, size_t smem, cudaStream_t st) {
+  if (a.class_end <= a.class_begin) return cudaSuccess;
+  const uint32_t graphs = a.class_end - a.class_begin;
+  const uint64_t per_sm = smem ? std::max<uint64_t>(1, std::min<uint64_t>(8, (200u << 10) / smem)) : 8;
+  const unsigned blocks = unsigned(std::min<uint64_t>(graphs, uint64_t(sm_count()) * per_sm));
+  if (words == 1) {
+    cudaFuncSetAttribute(sliced_filter_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    sliced_filter_kernel<1><<<blocks, 256, smem, st>>>(a); note_launch();
+  } else {
+    cudaFuncSetAttribute(sliced_filter_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    sliced_filter_kernel<2><<<blocks, 256, smem, st>>>(a); note_launch();
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace bms

@@ -26,6 +26,8 @@ SIZE_UNIFORM, SIZE_NORMAL, SIZE_LOGNORMAL = 0, 1, 2
 NUM_FEATURES = 12
 MLP_PARAMS = 64 * 12 + 64 + 64 * 64 + 64 + 64 + 1
 SCHED_BUCKETS = 4
+OPT_FILTER_KERNEL, OPT_JOIN_STEPS = 1, 2
+FILTER_SLICED, FILTER_BALLOT = 0, 1
 
 
 class BmsError(RuntimeError):
@@ -100,6 +102,7 @@ SIGNATURES = [
     ("bms_set_stream", C.c_int, [_vp, _vp]),
     ("bms_set_expansion_budget", C.c_int, [_vp, C.c_uint64]),
     ("bms_set_logging", C.c_int, [_vp, C.c_int]),
+    ("bms_set_option", C.c_int, [_vp, C.c_int, C.c_int64]),
     ("bms_load_graphs", C.c_int, [_vp, C.c_int, _vp]),
     ("bms_load_csr", C.c_int, [_vp, C.c_int, C.c_uint32, _u32p, _u32p, _u32p, _u8p, _u8p]),
     ("bms_signatures", C.c_int, [_vp, C.c_int]),
@@ -298,6 +301,9 @@ class Context:
 
     def set_expansion_budget(self, budget: int) -> None:
         self._c(lib().bms_set_expansion_budget(self._h, budget))
+
+    def set_option(self, option: int, value: int) -> None:
+        self._c(lib().bms_set_option(self._h, option, value))
 
     def set_logging(self, vertex_expansions: bool) -> None:
         self._c(lib().bms_set_logging(self._h, int(vertex_expansions)))

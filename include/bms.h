@@ -145,6 +145,15 @@ int bms_set_expansion_budget(bms_ctx* ctx, uint64_t budget);
  * semantics only) for bms_vertex_expansions; off by default. */
 int bms_set_logging(bms_ctx* ctx, int vertex_expansions);
 
+/* Engine options (no reference counterpart). */
+typedef enum {
+  BMS_OPT_FILTER_KERNEL = 1, /* fused filter: BMS_FILTER_SLICED (default) or BMS_FILTER_BALLOT */
+  BMS_OPT_JOIN_STEPS = 2     /* DFS steps a warp runs between refills (default 32) */
+} bms_option;
+#define BMS_FILTER_SLICED 0 /* clause masks per data graph in shared memory, one thread per query */
+#define BMS_FILTER_BALLOT 1 /* one lane per data node, candidate rows formed by warp ballots */
+int bms_set_option(bms_ctx* ctx, int option, int64_t value);
+
 /* createDeviceCSRGraph (graph.hpp:251-310): upload a batch as the query or the
  * data side.  The CSR must be symmetric with column ids inside each graph; the
  * check runs on the device and is reported by the next stage call. */

@@ -282,3 +282,37 @@ def test_task_granularity_does_not_change_counts(ctx, wl, split):
         assert ctx.run(3, FIND_FIRST, ORDER_GMCR, SEM_EXACT) == int((want.counts > 0).sum())
     finally:
         ctx.set_schedule(sched)
+
+
+@pytest.mark.parametrize("kernel", [0, 1])
+@pytest.mark.parametrize("R", [0, 6])
+def test_both_fused_filter_kernels_bit_exact(ctx, wl, kernel, R):
+    from bms2_gb300.native import OPT_FILTER_KERNEL
+
+    q, d = wl
+    want = oracle.run_pipeline(q, d, R)
+    load(ctx, q, d)
+    try:
+        ctx.set_option(OPT_FILTER_KERNEL, kernel)
+        total = ctx.run(R, COUNT_ALL, ORDER_GMCR, SEM_EXACT)
+        off, qidx = ctx.gmcr()
+        assert np.array_equal(off, want.offsets) and np.array_equal(qidx, want.qidx)
+        assert np.array_equal(ctx.pair_counts(), want.counts) and total == want.total
+    finally:
+        ctx.set_option(OPT_FILTER_KERNEL, 0)
+
+
+def test_sliced_filter_slow_clauses(ctx):
+    # labels >= 16, degree > 16 and cycle counts > 8 fall outside the mask table
+    big = ([C] + [30] * 20, [(0, i + 1) for i in range(20)])  # degree-20 centre, label-30 leaves
+    kq = ([C] + list(range(16, 33)), [(0, i + 1) for i in range(17)])  # degree 17, leaves labelled 16..32
+    kd = ([C] + list(range(16, 34)), [(0, i + 1) for i in range(18)])  # one embedding of kq
+    k8 = ([C] * 8, [(i, j) for i in range(8) for j in range(i + 1, 8)])  # 420 5-cycles through each node
+    q = graphs(([C, 30], [(0, 1)]), kq, k8, ([30, C, 30], [(0, 1), (1, 2)]))
+    d = graphs(big, k8, kd, ring(6))
+    for R in (0, 2):
+        want = oracle.run_pipeline(q, d, R)
+        load(ctx, q, d)
+        assert ctx.run(R, COUNT_ALL, ORDER_GMCR, SEM_EXACT) == want.total
+        assert np.array_equal(ctx.pair_counts(), want.counts)
+    assert want.total == 20 + 20 * 19 + 40320 + 1 + 1  # the [C,30] edge also sits once in kd

@@ -113,6 +113,7 @@ SIGNATURES = [
     ("bms_run", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _u64p]),
     ("bms_get_stats", C.c_int, [_vp, C.POINTER(Stats)]),
     ("bms_get_gmcr", C.c_int, [_vp, _u32p, _u32p, C.c_uint64]),
+    ("bms_gmcr_offsets_static", C.c_int, [_vp, _vp, C.c_uint64, _vp]),
     ("bms_get_pair_counts", C.c_int, [_vp, _u64p, C.c_uint64]),
     ("bms_get_pair_expansions", C.c_int, [_vp, _u64p, C.c_uint64]),
     ("bms_get_pair_status", C.c_int, [_vp, _u8p, C.c_uint64]),

@@ -208,6 +208,21 @@ int bms_get_stats(bms_ctx* ctx, bms_stats* out);
 /* GMCR as the reference stores it (gmcr.hpp:220-224): data_graph_offsets
  * [n_data_graphs+1] and query_graph_indices [n_valid_pairs]. */
 int bms_get_gmcr(bms_ctx* ctx, uint32_t* data_graph_offsets, uint32_t* query_graph_indices, uint64_t cap);
+/* GMCR data_graph_offsets from per-data-graph pair counts, on the device, with
+ * no device allocation: counts[n] and offsets[n + 1] are device pointers owned
+ * by the caller; offsets[i] = counts[0] + ... + counts[i-1] and offsets[n] is
+ * the total.  No counterpart in the reference.  It serves callers that must not
+ * allocate device memory while they run — applications whose device memory is
+ * held by their own pool allocator, and latency-sensitive pipelines that cannot
+ * take the device-wide synchronisation of cudaMalloc/cudaFree — by keeping the
+ * scan's scratch in a fixed 256 KiB array that every GPU loading libbms holds
+ * until the process exits.  Limit: n <= 100,000,000 (BMS_EUNSUPPORTED above).
+ * The first call on a device looks up that array's device address (a one-time
+ * set-up); make that first call before any stream capture.  All calls share the
+ * one array, so calls that overlap on the GPU (other streams, other threads)
+ * race: order them.  The work is queued on `stream` (a cudaStream_t, NULL for
+ * the default stream); the call does not wait for it. */
+int bms_gmcr_offsets_static(const uint32_t* counts, uint32_t* offsets, uint64_t n, void* stream);
 /* Per-pair counts in GMCR order (find-first: 0/1). */
 int bms_get_pair_counts(bms_ctx* ctx, uint64_t* counts, uint64_t cap);
 /* Per-pair expansion counts in GMCR order. */

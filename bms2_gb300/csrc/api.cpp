@@ -92,6 +92,7 @@ int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const 
   CK(s.adjin.ensure(sizeof(uint64_t) * 2 * (N ? N : 1)));
   CK(s.ghist.ensure(sizeof(uint64_t) * (G ? G : 1)));
   CK(s.glabset.ensure(sizeof(uint32_t) * (G ? G : 1)));
+  CK(s.maxin.ensure(sizeof(uint32_t)));
   s.loaded = true;
   return BMS_OK;
 }
@@ -133,6 +134,7 @@ int run_signatures(bms_ctx* c, int R) {
   for (int i = 0; i < 2; ++i) {
     Side& s = *sides[i];
     s.sig_steps = R;
+    CK(cudaMemsetAsync(s.maxin.p, 0, sizeof(uint32_t), c->st));
     CK(launch_signatures(s.dg(), s.ds(), i == 0 ? kMaxDataNodes : kMaxQueryNodes, c->errflag.as<uint32_t>() + i, c->st));
   }
   return BMS_OK;
@@ -287,15 +289,17 @@ int run_ballot_filter(bms_ctx* c, const ShellPack& sp, int sem) {
     pa.class_end = c->class_end[k];
     pa.class_id = k;
     CK(launch_pair_filter(pa, rounds[k], c->st));
-    if (k == 2)  // records so far come from data graphs of more than 64 nodes
-      CK(cudaMemcpyAsync(&pa.ctr->recs_wide, &pa.ctr->recs, sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
-                         c->st));
+    // record class boundaries: > 64 nodes, then 33..64 nodes, then the rest
+    if (k > 0)
+      CK(cudaMemcpyAsync(k == 2 ? &pa.ctr->recs_wide : &pa.ctr->recs_mid, &pa.ctr->recs, sizeof(unsigned long long),
+                         cudaMemcpyDeviceToDevice, c->st));
   }
   return BMS_OK;
 }
 
 // Clause programs of the queries, then the sliced filter: data graphs of more
-// than 64 nodes first (two-word masks), then the rest (one word).
+// than 64 nodes first (two-word masks), then 33..64 nodes, then the rest (one
+// word); the record counter after each launch marks the class boundary.
 int run_sliced_filter(bms_ctx* c, const ShellPack& sp, int R, int sem) {
   const uint64_t Qn = c->q.N ? c->q.N : 1;
   const uint64_t per_node = 6 + uint64_t(R) * 16 + 256;
@@ -346,12 +350,16 @@ int run_sliced_filter(bms_ctx* c, const ShellPack& sp, int R, int sem) {
   if (smem > (220u << 10)) return fail(c, BMS_EUNSUPPORTED, "too many queries for the sliced filter's shared memory");
   CK(launch_sliced_filter(a, 2, smem, c->st));
   CK(cudaMemcpyAsync(&a.ctr->recs_wide, &a.ctr->recs, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, c->st));
-  // one-word graphs (classes 1 and 0 are contiguous in the permutation)
-  a.class_begin = c->class_begin[1];
-  a.class_end = c->class_end[0];
-  a.class_id = 1;
+  // one-word graphs
   smem = sliced_smem_bytes(a, 1);
-  CK(launch_sliced_filter(a, 1, smem, c->st));
+  for (int k = 1; k >= 0; --k) {
+    a.class_begin = c->class_begin[k];
+    a.class_end = c->class_end[k];
+    a.class_id = k;
+    CK(launch_sliced_filter(a, 1, smem, c->st));
+    if (k == 1)
+      CK(cudaMemcpyAsync(&a.ctr->recs_mid, &a.ctr->recs, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, c->st));
+  }
   return BMS_OK;
 }
 
@@ -601,6 +609,7 @@ int bms_join(bms_ctx* c, int mode, int order, int sem, uint64_t* total) {
                            c->arena.as<uint64_t>(), c->st));
     CK(launch_set_counter(&c->ctr.as<Counters>()->recs, T, c->st));
     CK(launch_set_counter(&c->ctr.as<Counters>()->recs_wide, T, c->st));  // GMCR order mixes sizes
+    CK(launch_set_counter(&c->ctr.as<Counters>()->recs_mid, T, c->st));
     r = join_records(c, mode, order, sem, mode == BMS_COUNT_ALL && order == BMS_ORDER_GMCR && sem == BMS_SEM_EXACT);
     if (r) return r;
     CK(cudaMemcpyAsync(c->h_T, c->gmcr_off.as<uint32_t>() + c->d.G, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->st));
@@ -745,6 +754,7 @@ int bms::rejoin_timed(bms_ctx* c, int bps, int wpb, int steps, float* ms) {
   Counters* ctr = c->ctr.as<Counters>();
   CK(cudaMemsetAsync(&ctr->task_fetch, 0, sizeof(unsigned long long), c->st));
   CK(cudaMemsetAsync(&ctr->task_fetch_wide, 0, sizeof(unsigned long long), c->st));
+  CK(cudaMemsetAsync(&ctr->task_fetch_small, 0, sizeof(unsigned long long), c->st));
   CK(cudaMemsetAsync(c->pair_count.p, 0, sizeof(unsigned long long) * c->rec_cap, c->st));
   CK(cudaMemsetAsync(c->pair_exp.p, 0, sizeof(unsigned long long) * c->rec_cap, c->st));
   CK(cudaMemsetAsync(c->pair_flag.p, 0, sizeof(uint32_t) * c->rec_cap, c->st));

@@ -45,14 +45,14 @@ struct Side {
   uint32_t max_nodes = 0;
   std::vector<uint32_t> h_goff;
   DevBuf goff, rowp, col, lab, elab;
-  DevBuf frec, adj, adjin, ghist, glabset;
+  DevBuf frec, adj, adjin, ghist, glabset, maxin;
   int sig_steps = -1;
   bool asymmetric = false;
   uint32_t labels_lt16 = 0;  // bit l: some node carries label l < 16
   DGraphs dg() const { return DGraphs{goff.as<uint32_t>(), rowp.as<uint32_t>(), col.as<uint32_t>(), lab.as<uint8_t>(), G, N, E}; }
   DSigs ds() const {
     return DSigs{frec.as<uint64_t>(), adj.as<uint64_t>(), adjin.as<uint64_t>(), ghist.as<uint64_t>(),
-                 glabset.as<uint32_t>(), sig_steps < 0 ? 0 : sig_steps};
+                 glabset.as<uint32_t>(), maxin.as<uint32_t>(), sig_steps < 0 ? 0 : sig_steps};
   }
 };
 

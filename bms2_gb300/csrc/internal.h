@@ -45,6 +45,7 @@ struct DSigs {
   uint64_t* adjin;      // [N*2]
   uint64_t* ghist;      // [G]   per-graph nibble histogram of labels < 16
   uint32_t* glabset;    // [G]   bit l: some node has label l (< 16)
+  uint32_t* maxin;      // [1]   largest in-degree (distinct in-neighbours) of the side
   int R;
 };
 
@@ -83,6 +84,8 @@ struct Counters {
   unsigned long long incomplete;  // pairs that hit the expansion budget
   unsigned long long recs_wide;   // records [0, recs_wide) come from data graphs of > 64 nodes
   unsigned long long task_fetch_wide;  // join work-stealing head of the two-word search
+  unsigned long long recs_mid;    // records [recs_wide, recs_mid) come from graphs of 33..64 nodes
+  unsigned long long task_fetch_small;  // join work-stealing head of the 32-bit search
 };
 
 // ----------------------------------------------------------------- launchers

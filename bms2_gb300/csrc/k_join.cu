@@ -10,21 +10,31 @@
 // (chunks shrink as the queue drains).  Idle lanes are refilled as soon as a
 // few of them are waiting, so lanes never wait long for a slow neighbour.
 //
-// The search state is bitsets over the data graph's local ids (one 64-bit word
-// for graphs of <= 64 nodes, two up to 128): `cur` holds the candidates left at
-// the current depth t: the vertices v of C[order[t]], not yet mapped, that pass
-// the induced test of isValidMapping_fast_bitwise (isomorphism.hpp:268-288)
-// against every earlier depth i (v in row(f_i) iff query vertex order[i] is in
-// the row of order[t]).  The test is evaluated in two parts: C is intersected
-// with the rows of the nodes mapped at the query-adjacent earlier depths
-// (usually one or two), and each surviving candidate v is kept iff every mapped
-// node whose row contains v (v's in-row, intersected with the mapped set) sits
-// at one of those depths.  On molecular graphs (degree <= 4) that is a few
-// independent loads per level.  The last depth is never expanded: its
-// candidates are counted with one popcount.  `cur` lives in registers; the
-// per-thread stack (interleaved local memory) is touched only on descend and
-// backtrack, and a step first pops every exhausted frame, so each step is one
-// assignment.
+// The search state is bitsets over the data graph's local ids: one 32-bit word
+// for graphs of <= 32 nodes, one 64-bit word up to 64, two up to 128 (records
+// arrive grouped by these classes and each class has its own kernel).  `cur`
+// holds the candidates left at the current depth t: the vertices v of
+// C[order[t]], not yet mapped, that pass the induced test of
+// isValidMapping_fast_bitwise (isomorphism.hpp:268-288) against every earlier
+// depth i (v in row(f_i) iff query vertex order[i] is in the row of order[t]).
+// C is intersected with the rows of the nodes mapped at the query-adjacent
+// earlier depths (usually one or two); a surviving v must then lie in the row
+// of no other mapped node.  Two ways to test that:
+//  - counted (EXACT semantics, every in-degree <= 7): each lane keeps, for
+//    every data node, the number of mapped nodes whose row contains it, as
+//    three bit planes updated with ripple-carry adds and borrows when a node
+//    is mapped or unmapped.  v passes iff its count equals the number of
+//    query-adjacent earlier depths: one plane comparison for the whole level,
+//    no per-candidate load.
+//  - in-row (REFERENCE_DFS, or larger in-degrees): each surviving v is kept iff
+//    its in-row, intersected with the mapped set, holds only nodes mapped at
+//    the adjacent depths: one load per candidate.
+// Each kernel reads the side's largest in-degree on the device and returns at
+// once when the other variant applies, so no host round trip decides it.  The
+// last depth is never expanded: its candidates are counted with one popcount.
+// `cur` lives in registers; the per-thread stack (interleaved local memory) is
+// touched only on descend and backtrack, and a step first pops every exhausted
+// frame, so each step is one assignment.
 //
 // EXACT semantics count every injective induced embedding.  REFERENCE_DFS
 // (literal) restates the reference DFS: a frame never clears the visited bit of
@@ -33,79 +43,107 @@
 // first write) — isomorphism.hpp:414-448, with mapping[] reset per root.  In
 // that mode tasks are always (pair, root): the reference searches every root
 // with a fresh visited set.
+#include <type_traits>
+
 #include "device_common.cuh"
 
 namespace bms {
 namespace {
 
-template <int W>
+constexpr int kPlanes = 3;  // counted test: counts 0..7
+
+__device__ __forceinline__ uint32_t wpop(uint32_t x) { return uint32_t(__popc(x)); }
+__device__ __forceinline__ uint32_t wpop(uint64_t x) { return uint32_t(__popcll(x)); }
+__device__ __forceinline__ uint32_t wlow(uint32_t x) { return uint32_t(__ffs(int(x)) - 1); }
+__device__ __forceinline__ uint32_t wlow(uint64_t x) { return uint32_t(__ffsll((long long)x) - 1); }
+__device__ __forceinline__ uint32_t whigh(uint32_t x) { return uint32_t(31 - __clz(int(x))); }
+__device__ __forceinline__ uint32_t whigh(uint64_t x) { return uint32_t(63 - __clzll((long long)x)); }
+
+// A set of local ids: W words of type T.
+template <typename T, int W>
 struct Bits {
-  uint64_t w[W];
+  static constexpr uint32_t kBits = 8 * sizeof(T);
+  T w[W];
 };
-template <int W>
-__device__ __forceinline__ Bits<W> z() {
-  Bits<W> r;
+template <typename T, int W>
+__device__ __forceinline__ Bits<T, W> z() {
+  Bits<T, W> r;
 #pragma unroll
   for (int i = 0; i < W; ++i) r.w[i] = 0;
   return r;
 }
-template <int W>
-__device__ __forceinline__ Bits<W> band(Bits<W> a, Bits<W> b) {
+template <typename T, int W>
+__device__ __forceinline__ Bits<T, W> ones() {
+  Bits<T, W> r;
+#pragma unroll
+  for (int i = 0; i < W; ++i) r.w[i] = T(~T(0));
+  return r;
+}
+template <typename T, int W>
+__device__ __forceinline__ Bits<T, W> band(Bits<T, W> a, Bits<T, W> b) {
 #pragma unroll
   for (int i = 0; i < W; ++i) a.w[i] &= b.w[i];
   return a;
 }
-template <int W>
-__device__ __forceinline__ Bits<W> bandn(Bits<W> a, Bits<W> b) {
+template <typename T, int W>
+__device__ __forceinline__ Bits<T, W> bandn(Bits<T, W> a, Bits<T, W> b) {
 #pragma unroll
-  for (int i = 0; i < W; ++i) a.w[i] &= ~b.w[i];
+  for (int i = 0; i < W; ++i) a.w[i] &= T(~b.w[i]);
   return a;
 }
-template <int W>
-__device__ __forceinline__ Bits<W> bor(Bits<W> a, Bits<W> b) {
+template <typename T, int W>
+__device__ __forceinline__ Bits<T, W> bor(Bits<T, W> a, Bits<T, W> b) {
 #pragma unroll
   for (int i = 0; i < W; ++i) a.w[i] |= b.w[i];
   return a;
 }
-template <int W>
-__device__ __forceinline__ bool bany(Bits<W> a) {
-  uint64_t x = 0;
+template <typename T, int W>
+__device__ __forceinline__ Bits<T, W> bxor(Bits<T, W> a, Bits<T, W> b) {
+#pragma unroll
+  for (int i = 0; i < W; ++i) a.w[i] ^= b.w[i];
+  return a;
+}
+template <typename T, int W>
+__device__ __forceinline__ bool bany(Bits<T, W> a) {
+  T x = 0;
 #pragma unroll
   for (int i = 0; i < W; ++i) x |= a.w[i];
   return x != 0;
 }
-template <int W>
-__device__ __forceinline__ uint32_t bpop(Bits<W> a) {
+template <typename T, int W>
+__device__ __forceinline__ uint32_t bpop(Bits<T, W> a) {
   uint32_t c = 0;
 #pragma unroll
-  for (int i = 0; i < W; ++i) c += __popcll(a.w[i]);
+  for (int i = 0; i < W; ++i) c += wpop(a.w[i]);
   return c;
 }
-template <int W>
-__device__ __forceinline__ Bits<W> bbit(uint32_t v) {
-  Bits<W> r = z<W>();
+template <typename T, int W>
+__device__ __forceinline__ Bits<T, W> bbit(uint32_t v) {
+  constexpr uint32_t kB = Bits<T, W>::kBits;
+  Bits<T, W> r;
 #pragma unroll
-  for (int i = 0; i < W; ++i) r.w[i] = (v >> 6) == uint32_t(i) ? (uint64_t(1) << (v & 63u)) : 0ull;
+  for (int i = 0; i < W; ++i) r.w[i] = v / kB == uint32_t(i) ? T(T(1) << (v % kB)) : T(0);
   return r;
 }
-template <int W>
-__device__ __forceinline__ bool bhas(Bits<W> a, uint32_t v) {
-  uint64_t x = a.w[0];
-  if (W > 1 && v >= 64) x = a.w[W - 1];
-  return (x >> (v & 63u)) & 1u;
+template <typename T, int W>
+__device__ __forceinline__ bool bhas(Bits<T, W> a, uint32_t v) {
+  constexpr uint32_t kB = Bits<T, W>::kBits;
+  T x = a.w[0];
+  if (W > 1 && v >= kB) x = a.w[W - 1];
+  return (x >> (v % kB)) & 1u;
 }
-template <int W>
-__device__ __forceinline__ uint32_t blow(Bits<W> a) {
-  if (W == 1 || a.w[0]) return uint32_t(__ffsll((long long)a.w[0]) - 1);
-  return uint32_t(64 + __ffsll((long long)a.w[W - 1]) - 1);
+template <typename T, int W>
+__device__ __forceinline__ uint32_t blow(Bits<T, W> a) {
+  if (W == 1 || a.w[0]) return wlow(a.w[0]);
+  return Bits<T, W>::kBits + wlow(a.w[W - 1]);
 }
-template <int W>
-__device__ __forceinline__ uint32_t bhigh(Bits<W> a) {
-  if (W > 1 && a.w[W - 1]) return uint32_t(127 - __clzll((long long)a.w[W - 1]));
-  return uint32_t(63 - __clzll((long long)a.w[0]));
+template <typename T, int W>
+__device__ __forceinline__ uint32_t bhigh(Bits<T, W> a) {
+  if (W > 1 && a.w[W - 1]) return Bits<T, W>::kBits + whigh(a.w[W - 1]);
+  return whigh(a.w[0]);
 }
-template <int W>
-__device__ __forceinline__ Bits<W> bclear_low(Bits<W> a) {
+template <typename T, int W>
+__device__ __forceinline__ Bits<T, W> bclear_low(Bits<T, W> a) {
   if (W == 1 || a.w[0]) {
     a.w[0] &= a.w[0] - 1;
   } else {
@@ -113,21 +151,56 @@ __device__ __forceinline__ Bits<W> bclear_low(Bits<W> a) {
   }
   return a;
 }
-// rows are stored as two 64-bit words; a 1-word search reads the low word
-template <int W>
-__device__ __forceinline__ Bits<W> bload(const uint64_t* p) {
-  Bits<W> r;
-  if (W == 1) {
-    r.w[0] = *p;
+// Rows are stored as two 64-bit words (little-endian); narrower searches read
+// the low word, or its low half.  Rows are read-only during the join.
+template <typename T, int W>
+__device__ __forceinline__ Bits<T, W> bload(const uint64_t* p) {
+  Bits<T, W> r;
+  if constexpr (sizeof(T) == 4) {
+    r.w[0] = __ldg(reinterpret_cast<const unsigned int*>(p));
+  } else if constexpr (W == 1) {
+    r.w[0] = __ldg(reinterpret_cast<const unsigned long long*>(p));
   } else {
-    const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(p);
+    const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(p));
     r.w[0] = v.x;
     r.w[W - 1] = v.y;
   }
   return r;
 }
 
-template <int W>
+// Per-node counts of mapped in-neighbours as kPlanes bit planes.
+template <typename T, int W>
+struct Planes {
+  Bits<T, W> p[kPlanes];
+};
+template <typename T, int W>
+__device__ __forceinline__ void padd(Planes<T, W>& P, Bits<T, W> carry) {
+#pragma unroll
+  for (int b = 0; b < kPlanes; ++b) {
+    const Bits<T, W> nc = band(P.p[b], carry);
+    P.p[b] = bxor(P.p[b], carry);
+    carry = nc;
+  }
+}
+template <typename T, int W>
+__device__ __forceinline__ void psub(Planes<T, W>& P, Bits<T, W> borrow) {
+#pragma unroll
+  for (int b = 0; b < kPlanes; ++b) {
+    const Bits<T, W> nb = bandn(borrow, P.p[b]);
+    P.p[b] = bxor(P.p[b], borrow);
+    borrow = nb;
+  }
+}
+// nodes whose count equals k (k < 2^kPlanes)
+template <typename T, int W>
+__device__ __forceinline__ Bits<T, W> peq(const Planes<T, W>& P, uint32_t k) {
+  Bits<T, W> m = ones<T, W>();
+#pragma unroll
+  for (int b = 0; b < kPlanes; ++b) m = ((k >> b) & 1u) ? band(m, P.p[b]) : bandn(m, P.p[b]);
+  return m;
+}
+
+template <typename T, int W>
 struct Lane {
   bool active;
   bool done_fetching;
@@ -138,35 +211,27 @@ struct Lane {
   const uint8_t* perm;
   const uint64_t* dadj;
   int t;
-  Bits<W> cur;     // candidates left at depth t
-  Bits<W> mapped;  // nodes mapped at depths < t
-  Bits<W> vis;     // REFERENCE_DFS: the reference's visited bitset
-  uint64_t mpset;  // REFERENCE_DFS: depths whose mapping[] has been written
+  Bits<T, W> cur;     // candidates left at depth t
+  Bits<T, W> mapped;  // nodes mapped at depths < t
+  Bits<T, W> vis;     // REFERENCE_DFS: the reference's visited bitset
+  Planes<T, W> P;     // counted test: mapped in-neighbour counts
+  uint64_t mpset;     // REFERENCE_DFS: depths whose mapping[] has been written
   unsigned long long cnt, exps;
   uint32_t since_check;
 };
 
-template <int W>
-__device__ __forceinline__ Bits<W> compute_level(const Lane<W>& L, uint32_t j, const uint8_t* f, bool literal) {
-  Bits<W> c = bload<W>(L.crow + 2 * uint64_t(L.perm[j]));
-  if (!literal) c = bandn(c, L.mapped);
-  Bits<W> pset = z<W>();
-  for (uint64_t pm = L.dadj[j]; pm; pm &= pm - 1) {
-    const uint32_t x = f[__ffsll((long long)pm) - 1];
-    c = band(c, bload<W>(L.arow + 2 * uint64_t(x)));
-    pset = bor(pset, bbit<W>(x));
-  }
-  Bits<W> res = z<W>();
-  for (Bits<W> r = c; bany(r); r = bclear_low(r)) {
-    const uint32_t v = blow(r);
-    const Bits<W> bad = bandn(band(bload<W>(L.irow + 2 * uint64_t(v)), L.mapped), pset);
-    if (!bany(bad)) res = bor(res, bbit<W>(v));
-  }
-  return res;
-}
+// Per-thread stacks, indexed by depth.
+template <typename T, int W>
+struct Stack {
+  uint8_t f[kMaxQueryNodes];         // node mapped at each depth
+  uint8_t mp[kMaxQueryNodes];        // REFERENCE_DFS: mapping[] as the reference writes it
+  Bits<T, W> F[kMaxQueryNodes];      // candidates left in each frame
+  Bits<T, W> row[kMaxQueryNodes];    // counted test: row of f[depth]
+  uint32_t expd[kMaxQueryNodes];     // per-depth expansions (logging)
+};
 
-template <int W>
-__device__ __forceinline__ void finish(Lane<W>& L, const JoinArgs& a, const uint32_t* expd) {
+template <typename T, int W>
+__device__ __forceinline__ void finish(Lane<T, W>& L, const JoinArgs& a, const uint32_t* expd) {
   if (L.cnt) atomicAdd(&a.pair_count[L.rec], L.cnt);
   if (L.exps) atomicAdd(&a.pair_exp[L.rec], L.exps);
   if (a.find_first && L.cnt) atomicOr(&a.pair_flag[L.rec], 1u);
@@ -176,95 +241,185 @@ __device__ __forceinline__ void finish(Lane<W>& L, const JoinArgs& a, const uint
   L.active = false;
 }
 
-// One assignment of an active lane: pop exhausted frames, take the next
-// candidate, compute the next level (or count the leaf level).
-template <int W>
-__device__ __forceinline__ void step(Lane<W>& L, const JoinArgs& a, uint8_t* f, uint8_t* mp, Bits<W>* F,
-                                     uint32_t* expd) {
+template <typename T, int W>
+__device__ __forceinline__ bool after_step(Lane<T, W>& L, const JoinArgs& a, const uint32_t* expd) {
+  if (a.budget && L.exps > a.budget) {
+    atomicOr(&a.pair_flag[L.rec], 2u);
+    finish(L, a, expd);
+    return false;
+  }
+  if (a.find_first && ++L.since_check >= 64) {
+    L.since_check = 0;
+    if (*(volatile const uint32_t*)&a.pair_flag[L.rec] & 1u) {
+      finish(L, a, expd);
+      return false;
+    }
+  }
+  return true;
+}
+
+// ----------------------------------------------------------- counted test
+// One assignment: pop exhausted frames, take the next candidate v of depth t,
+// compute depth t+1 with v mapped; count it when it is the leaf level, else
+// push.  Leaf and dead-end steps write no stack state.
+template <typename T, int W>
+__device__ __forceinline__ void step_counted(Lane<T, W>& L, const JoinArgs& a, Stack<T, W>& S) {
   int t = L.t;
   while (!bany(L.cur)) {  // frame t exhausted
-    if (a.literal && ((L.mpset >> t) & 1ull)) L.vis = bandn(L.vis, bbit<W>(mp[t]));
     if (t == 0) {
-      finish(L, a, expd);
+      finish(L, a, S.expd);
       return;
     }
     --t;
-    L.cur = F[t];
-    L.mapped = bandn(L.mapped, bbit<W>(f[t]));  // back in frame t: its node leaves the path
+    L.cur = S.F[t];
+    L.mapped = bandn(L.mapped, bbit<T, W>(S.f[t]));  // back in frame t: its node leaves the path
+    psub(L.P, S.row[t]);
+  }
+  L.t = t;
+  const uint32_t v = blow(L.cur);
+  L.cur = bclear_low(L.cur);
+  const uint32_t j = uint32_t(t) + 1;
+  const Bits<T, W> row = bload<T, W>(L.arow + 2 * uint64_t(v));
+  const uint64_t dm = __ldg(reinterpret_cast<const unsigned long long*>(L.dadj) + j);
+  Bits<T, W> c = bload<T, W>(L.crow + 2 * uint64_t(__ldg(L.perm + j)));
+  const Bits<T, W> mapped = bor(L.mapped, bbit<T, W>(v));
+  c = bandn(c, mapped);
+  if ((dm >> t) & 1ull) c = band(c, row);
+  for (uint64_t pm = dm & ~(uint64_t(1) << t); pm; pm &= pm - 1) c = band(c, S.row[__ffsll((long long)pm) - 1]);
+  Planes<T, W> P = L.P;
+  padd(P, row);
+  const uint32_t k = uint32_t(__popcll(dm));
+  c = k < (1u << kPlanes) ? band(c, peq(P, k)) : z<T, W>();
+  L.exps += 1;
+  if (a.vertex_exp) S.expd[t] += 1;
+  if (j + 1 == L.n) {  // depth j is the leaf level: count it without expanding
+    const uint32_t pc = bpop(c);
+    L.cnt += pc;
+    L.exps += pc;
+    if (a.vertex_exp) S.expd[j] += pc;
+    if (a.find_first && pc) {
+      finish(L, a, S.expd);
+      return;
+    }
+  } else if (bany(c)) {
+    S.F[t] = L.cur;
+    S.f[t] = uint8_t(v);
+    S.row[t] = row;
+    L.P = P;
+    L.mapped = mapped;
+    L.t = int(j);
+    L.cur = c;
+  }
+  after_step(L, a, S.expd);
+}
+
+// ----------------------------------------------------------- in-row test
+template <typename T, int W>
+__device__ __forceinline__ Bits<T, W> compute_level(const Lane<T, W>& L, uint32_t j, const uint8_t* f, bool literal) {
+  Bits<T, W> c = bload<T, W>(L.crow + 2 * uint64_t(__ldg(L.perm + j)));
+  if (!literal) c = bandn(c, L.mapped);
+  Bits<T, W> pset = z<T, W>();
+  for (uint64_t pm = __ldg(reinterpret_cast<const unsigned long long*>(L.dadj) + j); pm; pm &= pm - 1) {
+    const uint32_t x = f[__ffsll((long long)pm) - 1];
+    c = band(c, bload<T, W>(L.arow + 2 * uint64_t(x)));
+    pset = bor(pset, bbit<T, W>(x));
+  }
+  Bits<T, W> res = z<T, W>();
+  for (Bits<T, W> r = c; bany(r); r = bclear_low(r)) {
+    const uint32_t v = blow(r);
+    const Bits<T, W> bad = bandn(band(bload<T, W>(L.irow + 2 * uint64_t(v)), L.mapped), pset);
+    if (!bany(bad)) res = bor(res, bbit<T, W>(v));
+  }
+  return res;
+}
+
+template <typename T, int W>
+__device__ __forceinline__ void step_inrow(Lane<T, W>& L, const JoinArgs& a, Stack<T, W>& S) {
+  int t = L.t;
+  while (!bany(L.cur)) {  // frame t exhausted
+    if (a.literal && ((L.mpset >> t) & 1ull)) L.vis = bandn(L.vis, bbit<T, W>(S.mp[t]));
+    if (t == 0) {
+      finish(L, a, S.expd);
+      return;
+    }
+    --t;
+    L.cur = S.F[t];
+    L.mapped = bandn(L.mapped, bbit<T, W>(S.f[t]));  // back in frame t: its node leaves the path
   }
   L.t = t;
   const uint32_t v = blow(L.cur);
   L.cur = bclear_low(L.cur);
   if (a.literal) {
     if (bhas(L.vis, v)) return;
-    mp[t] = uint8_t(v);
+    S.mp[t] = uint8_t(v);
     L.mpset |= uint64_t(1) << t;
-    L.vis = bor(L.vis, bbit<W>(v));
+    L.vis = bor(L.vis, bbit<T, W>(v));
   }
-  f[t] = uint8_t(v);
-  L.mapped = bor(L.mapped, bbit<W>(v));
+  S.f[t] = uint8_t(v);
+  L.mapped = bor(L.mapped, bbit<T, W>(v));
   L.exps += 1;
-  if (a.vertex_exp) expd[t] += 1;
-  const Bits<W> nf = compute_level(L, uint32_t(t) + 1, f, a.literal);
+  if (a.vertex_exp) S.expd[t] += 1;
+  const Bits<T, W> nf = compute_level(L, uint32_t(t) + 1, S.f, a.literal);
   if (uint32_t(t) + 2 == L.n) {
     // depth n-1 is the leaf level: count it without expanding
     const uint32_t last = L.n - 1;
-    Bits<W> acc = nf;
+    Bits<T, W> acc = nf;
     if (a.literal) acc = bandn(nf, L.vis);
     const uint32_t pc = bpop(acc);
     L.cnt += pc;
     L.exps += pc;
-    if (a.vertex_exp) expd[last] += pc;
+    if (a.vertex_exp) S.expd[last] += pc;
     if (a.literal && pc) {
       L.vis = bor(L.vis, acc);
-      mp[last] = uint8_t(bhigh(acc));
+      S.mp[last] = uint8_t(bhigh(acc));
       L.mpset |= uint64_t(1) << last;
     }
     if (a.find_first && pc) {
-      finish(L, a, expd);
+      finish(L, a, S.expd);
       return;
     }
-    if (a.literal && ((L.mpset >> last) & 1ull)) L.vis = bandn(L.vis, bbit<W>(mp[last]));  // frame n-1 exhausted
-    L.mapped = bandn(L.mapped, bbit<W>(v));  // frame t moves on
+    if (a.literal && ((L.mpset >> last) & 1ull)) L.vis = bandn(L.vis, bbit<T, W>(S.mp[last]));  // frame n-1 exhausted
+    L.mapped = bandn(L.mapped, bbit<T, W>(v));  // frame t moves on
   } else {
-    F[t] = L.cur;
+    S.F[t] = L.cur;
     L.t = t + 1;
     L.cur = nf;
   }
-  if (a.budget && L.exps > a.budget) {
-    atomicOr(&a.pair_flag[L.rec], 2u);
-    finish(L, a, expd);
-    return;
-  }
-  if (a.find_first && ++L.since_check >= 64) {
-    L.since_check = 0;
-    if (*(volatile const uint32_t*)&a.pair_flag[L.rec] & 1u) finish(L, a, expd);
-  }
+  after_step(L, a, S.expd);
 }
 
-template <int W>
+// Record class K: 2 = data graphs of 65..128 nodes (two 64-bit words), 1 =
+// 33..64 nodes (one 64-bit word), 0 = up to 32 nodes (one 32-bit word).
+// kCounted selects the counted test (EXACT, in-degrees <= 7) or the in-row test.
+template <int K, bool kCounted>
 __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
+  using T = typename std::conditional<K == 0, uint32_t, uint64_t>::type;
+  constexpr int W = K == 2 ? 2 : 1;
+  const bool counted_applies = !a.literal && *a.ds.maxin < (1u << kPlanes);
+  if (counted_applies != kCounted) return;  // the other variant runs this class
   const uint32_t lane = lane_id();
   const uint32_t lt_mask = (1u << lane) - 1u;
-  // task range: records [0, recs_wide) need two words, the rest one word
+  // record ranges: [0, wide) two words, [wide, mid) one word, [mid, recs) 32 bits
   const unsigned long long recs = min((unsigned long long)a.rec_cap, a.ctr->recs);
   const unsigned long long wide = min(recs, a.ctr->recs_wide);
+  const unsigned long long mid = max(wide, min(recs, a.ctr->recs_mid));
+  const unsigned long long lo = K == 2 ? 0 : (K == 1 ? wide : mid);
+  const unsigned long long hi = K == 2 ? wide : (K == 1 ? mid : recs);
   unsigned long long first, ntasks;
   if (a.per_pair) {
-    first = W == 2 ? 0 : wide;
-    ntasks = W == 2 ? wide : recs - wide;
+    first = lo;
+    ntasks = hi - lo;
   } else {
     first = 0;
     ntasks = min((unsigned long long)a.task_cap, a.ctr->tasks);
   }
-  unsigned long long* head = W == 2 ? &a.ctr->task_fetch_wide : &a.ctr->task_fetch;
+  unsigned long long* head =
+      K == 2 ? &a.ctr->task_fetch_wide : (K == 1 ? &a.ctr->task_fetch : &a.ctr->task_fetch_small);
   const unsigned long long nwarps = (unsigned long long)(gridDim.x * blockDim.x) >> 5;
-  Lane<W> L;
+  Lane<T, W> L;
   L.active = false;
   L.done_fetching = false;
-  uint8_t f[kMaxQueryNodes], mp[kMaxQueryNodes];
-  Bits<W> F[kMaxQueryNodes];
-  uint32_t expd[kMaxQueryNodes];
+  Stack<T, W> S;
   unsigned long long qbase = 0, qend = 0;  // this warp's chunk of the queue (warp-uniform)
   bool queue_empty = false;
   for (;;) {
@@ -295,15 +450,15 @@ __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
       const uint32_t took = uint64_t(__popc(need)) < avail ? uint32_t(__popc(need)) : uint32_t(avail);
       if (mine) {
         uint32_t rec;
-        Bits<W> roots;
+        Bits<T, W> roots;
         bool take = true;
         if (a.per_pair) {
           rec = uint32_t(first + qbase + rank);
         } else {
           const Task tk = a.tasks[qbase + rank];
           rec = tk.pair;
-          take = (rec < wide) == (W == 2);
-          roots = bbit<W>(tk.root);
+          take = (K == 2 || rec >= lo) && rec < hi;  // class 2 starts at record 0
+          roots = bbit<T, W>(tk.root);
         }
         L.active = take;
         if (take) {
@@ -316,18 +471,20 @@ __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
           L.irow = a.ds.adjin + 2 * uint64_t(a.d.goff[r.d]);
           L.perm = a.o.perm + uint64_t(r.q) * kMaxQueryNodes;
           L.dadj = a.o.dadj + uint64_t(r.q) * kMaxQueryNodes;
-          if (a.per_pair) roots = bload<W>(L.crow + 2 * uint64_t(L.perm[0]));
+          if (a.per_pair) roots = bload<T, W>(L.crow + 2 * uint64_t(L.perm[0]));
           L.cnt = 0;
           L.exps = 0;
           L.since_check = 0;
           L.t = 0;
           L.cur = roots;
-          L.mapped = z<W>();
-          L.vis = z<W>();
+          L.mapped = z<T, W>();
+          L.vis = z<T, W>();
+#pragma unroll
+          for (int b = 0; b < kPlanes; ++b) L.P.p[b] = z<T, W>();
           L.mpset = 0;
           if (a.vertex_exp)
-            for (uint32_t t = 0; t < L.n; ++t) expd[t] = 0;
-          if (a.find_first && (*(volatile const uint32_t*)&a.pair_flag[L.rec] & 1u)) finish(L, a, expd);
+            for (uint32_t t = 0; t < L.n; ++t) S.expd[t] = 0;
+          if (a.find_first && (*(volatile const uint32_t*)&a.pair_flag[L.rec] & 1u)) finish(L, a, S.expd);
         }
       }
       qbase += took;
@@ -336,21 +493,34 @@ __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
     if (queue_empty && !L.active) L.done_fetching = true;
     if (__all_sync(0xffffffffu, !L.active && L.done_fetching)) break;
     for (int s = 0; s < a.steps; ++s) {
-      if (L.active) step(L, a, f, mp, F, expd);
+      if (L.active) {
+        if constexpr (kCounted) step_counted(L, a, S);
+        else step_inrow(L, a, S);
+      }
       const uint32_t idle = __ballot_sync(0xffffffffu, !L.active && !L.done_fetching);
       if (__popc(idle) >= 4 || (idle && !__any_sync(0xffffffffu, L.active))) break;
     }
   }
 }
 
+template <int K>
+cudaError_t launch_class(const JoinArgs& a, int blocks, int threads, cudaStream_t st) {
+  if (!a.literal) {
+    join_kernel<K, true><<<blocks, threads, 0, st>>>(a); note_launch();
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  join_kernel<K, false><<<blocks, threads, 0, st>>>(a); note_launch();
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 cudaError_t launch_join(const JoinArgs& a, int blocks, int threads, cudaStream_t st) {
-  join_kernel<2><<<blocks, threads, 0, st>>>(a); note_launch();
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  join_kernel<1><<<blocks, threads, 0, st>>>(a); note_launch();
-  return cudaGetLastError();
+  cudaError_t e = launch_class<2>(a, blocks, threads, st);
+  if (e == cudaSuccess) e = launch_class<1>(a, blocks, threads, st);
+  if (e == cudaSuccess) e = launch_class<0>(a, blocks, threads, st);
+  return e;
 }
 
 }  // namespace bms

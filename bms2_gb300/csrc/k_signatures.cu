@@ -186,6 +186,7 @@ __global__ void __launch_bounds__(kWarps * 32) signatures_kernel(DGraphs g, DSig
       }
     }
     __syncwarp();
+    uint32_t max_in = 0;
     for (uint32_t v = lane; v < m; v += 32) {
       B128 eq{0, 0};
       const uint8_t l = s.lab[v];
@@ -195,7 +196,10 @@ __global__ void __launch_bounds__(kWarps * 32) signatures_kernel(DGraphs g, DSig
       // symmetry as sets: out-set equals in-set
       const B128 o = s.adj[v], i = s.in[v];
       if (o.lo != i.lo || o.hi != i.hi) bad |= kErrAsym;
+      max_in = max(max_in, b_pop(i));
     }
+    max_in = __reduce_max_sync(0xffffffffu, max_in);
+    if (lane == 0 && max_in) atomicMax(out.maxin, max_in);
     bad = __reduce_or_sync(0xffffffffu, bad);
     if (bad && lane == 0) atomicOr(err, bad);
     __syncwarp();

@@ -180,6 +180,29 @@ def test_large_graphs_two_word_bitsets(ctx):
             assert np.array_equal(got["shells"], want.d_sigs.shells)
 
 
+def test_join_counted_and_in_row_tests_agree(ctx):
+    # Data graphs of 8-120 nodes cover all three record classes (32-bit, one
+    # and two 64-bit words).  Molecules have in-degrees <= 4, so the join uses
+    # its counted induced test; appending a star with 9 leaves (in-degree 9)
+    # switches the whole batch to the in-row test.  Counts and expansions of
+    # the shared pairs must not change, and both equal the oracle.
+    d = Graphs.synth_molecules(150, 11, 0, 0, 0, 8, 120, 1, 4)
+    q = Graphs.synth_queries(d, 16, 12, 3, 12)
+    d_hub = Graphs.parse_text(_text(d.arrays()) + line(*star(9)) + "\n")
+    results = []
+    for dd in (d, d_hub):
+        want = oracle.run_pipeline(q, dd, 2)
+        load(ctx, q, dd)
+        ctx.run(2, COUNT_ALL, ORDER_GMCR, SEM_EXACT)
+        counts, exps = ctx.pair_counts(), ctx.pair_expansions()
+        assert np.array_equal(counts, want.counts)
+        results.append((counts, exps))
+    n = len(results[0][0])
+    assert n > 0 and results[0][0].sum() > 0
+    assert np.array_equal(results[1][0][:n], results[0][0])
+    assert np.array_equal(results[1][1][:n], results[0][1])
+
+
 def test_many_entries_graph_reads_rows_from_global_memory(ctx):
     # a 127-leaf star with every edge listed 5 times: 1270 CSR entries (more
     # than the 1024 staged in shared memory), repeated entries, 128 nodes

@@ -8,8 +8,14 @@ workload is mol100k: 100,000 seeded synthetic molecular data graphs (N(28, 9)
 atoms clipped to 10-60) x 600 queries of 5-30 nodes, 30% pure-carbon chains
 and rings — the shapes of the reference's plain-method GPU configuration.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--order learned|plain]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--order learned|plain] [--workload mol100k|mol1m]
   python bench.py --impl reference ...   # the CPU restatement of the reference
+
+With the learned order (the default) the cost model is first trained on a
+seed-A workload of the same shape (plain-order expansion logging, GPU
+training); the timed steps run on seed-B inputs, and the plain GMCR order is
+timed on the same inputs for the learned-over-plain ratio, with per-pair counts
+compared.
 
 With N > 1 (torchrun, one rank per GPU) every rank processes its own shard of
 data graphs (seeded by rank): weak scaling, no collective on the data path.
@@ -33,7 +39,7 @@ sys.path.insert(0, str(ROOT))
 
 WORKLOAD = "mol100k"
 REFINE_STEPS = 6
-METRIC = "query x data-graph pairs/s (count-all, bit-exact counts)"
+METRIC = "query x data-graph pairs/s, learned vs plain GMCR order (count-all, bit-exact counts)"
 HBM_FALLBACK_GBS = 6800.0
 
 
@@ -131,18 +137,19 @@ def _head(a: dict, k: int) -> dict:
             "node_labels": a["node_labels"][:n].copy(), "edge_labels": a["edge_labels"][:e].copy()}
 
 
-def train_cost_model(ctx, seed: int, n_data: int) -> dict:
+def train_cost_model(ctx, workload: str, seed: int, n_data: int) -> dict:
     """Seed-A plain-order run with vertex logging -> features + targets -> GPU training."""
     from bms2_gb300 import COUNT_ALL, DATA, ORDER_GMCR, QUERY, SEM_EXACT, workloads
     from bms2_gb300.train import collect, train
 
-    qa, da = workloads.make(WORKLOAD, seed, n_data=n_data)
+    qa, da = workloads.make(workload, seed, n_data=n_data)
     ctx.load(QUERY, qa)
     ctx.load(DATA, da)
     x, y = collect(ctx, REFINE_STEPS)
     loss = train(ctx, x, y, seed=seed)
     del COUNT_ALL, ORDER_GMCR, SEM_EXACT
-    return {"train_samples": int(len(y)), "train_loss": float(loss), "train_seed": seed, "train_data_graphs": n_data}
+    return {"train_samples": int(len(y)), "train_loss": float(loss), "train_seed": seed, "train_data_graphs": n_data,
+            "train_workload": workload}
 
 
 def run_ours(args) -> None:
@@ -164,17 +171,31 @@ def run_ours(args) -> None:
     order = ORDER_LEARNED if args.order == "learned" else ORDER_GMCR
     extra = {}
     if order == ORDER_LEARNED:
-        extra.update(train_cost_model(ctx, seed=101, n_data=args.train_graphs))
+        extra.update(train_cost_model(ctx, args.workload, seed=101, n_data=args.train_graphs))
     # evaluation workload (seed B; each rank its own shard)
-    q, d = workloads.make(WORKLOAD, 202 + rank, n_data=args.data_graphs)
+    q, d = workloads.make(args.workload, 202 + rank, n_data=args.data_graphs)
     Q, D = q.n_graphs, d.n_graphs
     qa, da = q.arrays(), d.arrays()
     ctx.load(QUERY, q)
     ctx.load(DATA, d)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
 
-    def step():
-        return ctx.run(REFINE_STEPS, COUNT_ALL, order, SEM_EXACT)
+    def step(o=order):
+        return ctx.run(REFINE_STEPS, COUNT_ALL, o, SEM_EXACT)
+
+    def timed(o, k):
+        """k steps of order o, each bracketed by CUDA events on the library's stream."""
+        ms, stages = [], []
+        for _ in range(k):
+            flush.fill_(1)  # L2 flush between steps (outside the timed events)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            tot = step(o)
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            stages.append(ctx.stats())
+        return ms, stages, tot
 
     if args.once:  # one pipeline run, for profilers
         total = step()
@@ -191,30 +212,30 @@ def run_ours(args) -> None:
         return
     for _ in range(args.warmup):
         step()
-    plain_total = None
+    plain = None
     if order == ORDER_LEARNED:
-        plain_total = ctx.run(REFINE_STEPS, COUNT_ALL, ORDER_GMCR, SEM_EXACT)
-        plain_exp = ctx.stats()["expansions"]
-        plain_ms = ctx.stats()["ms_join"]
+        # the plain GMCR order on the same inputs: per-pair counts must be equal,
+        # and its timed steps give the learned-over-plain ratio
+        plain_total = step(ORDER_GMCR)
+        plain_counts, plain_exp = ctx.pair_counts(), ctx.stats()["expansions"]
+        step()
+        same_pairs = bool(np.array_equal(ctx.pair_counts(), plain_counts))
+        for _ in range(args.warmup):
+            step(ORDER_GMCR)
+        p_ms, p_stage, _ = timed(ORDER_GMCR, args.steps)
+        plain = {"plain_total_matches": int(plain_total), "plain_expansions": int(plain_exp),
+                 "counts_equal_every_pair": same_pairs,
+                 "plain_ms_per_step": float(np.mean(p_ms)),
+                 "plain_join_ms": float(np.mean([s["ms_join"] for s in p_stage]))}
+        for _ in range(args.warmup):
+            step()
     clocks = Clocks(local)
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize(dev)
     clocks.start()
-    ms_steps, stage = [], []
-    total = None
-    launches = 0
-    for _ in range(args.steps):
-        flush.fill_(1)  # L2 flush between steps (outside the timed events)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        total = step()
-        e1.record(stream)
-        e1.synchronize()
-        ms_steps.append(e0.elapsed_time(e1))
-        st = ctx.stats()
-        stage.append(st)
-        launches += st["kernel_launches"]
+    ms_steps, stage, total = timed(order, args.steps)
+    launches = sum(s["kernel_launches"] for s in stage)
     torch.cuda.synchronize(dev)
     if world > 1:
         dist.barrier()
@@ -271,7 +292,7 @@ def run_ours(args) -> None:
         "vs_baseline": None,
         "dtype": "u64",
         "data": "synthetic",
-        "config": {"workload": f"{WORKLOAD}: {D} data graphs x {Q} queries per GPU, refine steps {REFINE_STEPS}, "
+        "config": {"workload": f"{args.workload}: {D} data graphs x {Q} queries per GPU, refine steps {REFINE_STEPS}, "
                                f"count-all, EXACT semantics, order {args.order}",
                    "data_graphs_per_gpu": D, "queries": Q, "refine_steps": REFINE_STEPS, "order": args.order,
                    "l2": "flushed between steps (512 MiB write outside the timed events)",
@@ -288,12 +309,11 @@ def run_ours(args) -> None:
         "gpu_launches": int(launches),
         "results": {"total_matches": int(total), "valid_pairs": int(T), "expansions": int(st["expansions"])},
     }
-    if plain_total is not None:
-        line["results"]["plain_total_matches"] = int(plain_total)
-        line["results"]["counts_equal_plain"] = bool(plain_total == total)
-        line["results"]["plain_expansions"] = int(plain_exp)
-        line["results"]["expansion_ratio_plain_over_learned"] = float(plain_exp) / max(1, st["expansions"])
-        line["results"]["plain_join_ms"] = float(plain_ms)
+    if plain is not None:
+        line["results"].update(plain)
+        line["results"]["plain_value"] = world * pairs / (plain["plain_ms_per_step"] / 1e3)
+        line["results"]["learned_over_plain"] = line["results"]["plain_value"] and value / line["results"]["plain_value"]
+        line["results"]["expansion_ratio_plain_over_learned"] = float(plain["plain_expansions"]) / max(1, st["expansions"])
     line["results"].update(extra)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(q, d, os.cpu_count() or 1, args.cpu_budget)
@@ -313,7 +333,7 @@ def run_reference(args) -> None:
         return
     from bms2_gb300 import workloads
 
-    q, d = workloads.make(WORKLOAD, 202)
+    q, d = workloads.make(args.workload, 202)
     threads = os.cpu_count() or 1
     cb = None
     vals = []
@@ -326,7 +346,7 @@ def run_reference(args) -> None:
     line = {"metric": METRIC, "value": v, "unit": "pairs/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": f"{WORKLOAD}: {d.n_graphs} data graphs x {q.n_graphs} queries (bounded sample per "
+            "config": {"workload": f"{args.workload}: {d.n_graphs} data graphs x {q.n_graphs} queries (bounded sample per "
                                    f"step), refine steps {REFINE_STEPS}, count-all", "order": "plain"},
             "cpu_baseline": cb, "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -338,7 +358,8 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--order", choices=["learned", "plain"], default="plain")
+    ap.add_argument("--order", choices=["learned", "plain"], default="learned")
+    ap.add_argument("--workload", choices=["mol100k", "mol1m", "mol10m"], default=WORKLOAD)
     ap.add_argument("--train-graphs", type=int, default=20000)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")

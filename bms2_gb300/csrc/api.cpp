@@ -165,6 +165,10 @@ int ensure_join_buffers(bms_ctx* c) {
   CK(c->pair_count.ensure(sizeof(unsigned long long) * (c->rec_cap ? c->rec_cap : 1)));
   CK(c->pair_exp.ensure(sizeof(unsigned long long) * (c->rec_cap ? c->rec_cap : 1)));
   CK(c->pair_flag.ensure(sizeof(uint32_t) * (c->rec_cap ? c->rec_cap : 1)));
+  // subtree buffers: one entry per record up to 4M entries (352 MiB each); a
+  // search that finds no room keeps its work instead of splitting
+  c->sub_cap = c->sub_cap_opt ? c->sub_cap_opt : std::min<uint64_t>(std::max<uint64_t>(c->rec_cap, 1 << 16), 1 << 22);
+  for (auto& b : c->sub) CK(b.ensure(sizeof(SubTask) * c->sub_cap));
   return BMS_OK;
 }
 
@@ -217,6 +221,10 @@ int join_records(bms_ctx* c, int mode, int order, int sem, bool log_vertices) {
   ja.find_first = mode == BMS_FIND_FIRST;
   ja.literal = sem == BMS_SEM_REFERENCE_DFS;
   ja.steps = c->join_steps;
+  ja.sub[0] = c->sub[0].as<SubTask>();
+  ja.sub[1] = c->sub[1].as<SubTask>();
+  ja.sub_cap = c->sub_cap;
+  ja.split_budget = c->split_budget;
   const int bucket = 0;
   const int bps = c->sched.blocks_per_sm[bucket] ? int(c->sched.blocks_per_sm[bucket]) : 3;
   const int wpb = c->sched.warps_per_block[bucket] ? int(c->sched.warps_per_block[bucket]) : 8;
@@ -454,6 +462,14 @@ int bms_set_option(bms_ctx* c, int option, int64_t value) {
     case BMS_OPT_JOIN_STEPS:
       if (value < 1 || value > 4096) return fail(c, BMS_EINVAL, "join steps must be in [1, 4096]");
       c->join_steps = int(value);
+      return BMS_OK;
+    case BMS_OPT_SPLIT_BUDGET:
+      if (value < 0 || value > (int64_t(1) << 31)) return fail(c, BMS_EINVAL, "split budget must be in [0, 2^31]");
+      c->split_budget = uint32_t(value);
+      return BMS_OK;
+    case BMS_OPT_SUBTREE_CAP:
+      if (value < 0 || value > (int64_t(1) << 28)) return fail(c, BMS_EINVAL, "subtree capacity must be in [0, 2^28]");
+      c->sub_cap_opt = uint64_t(value);
       return BMS_OK;
     default:
       return fail(c, BMS_EINVAL, "unknown option");
@@ -752,9 +768,7 @@ int run_fused(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total, 
 int bms::rejoin_timed(bms_ctx* c, int bps, int wpb, int steps, float* ms) {
   if (!c->have_results) return fail(c, BMS_ESTATE, "run the pipeline first");
   Counters* ctr = c->ctr.as<Counters>();
-  CK(cudaMemsetAsync(&ctr->task_fetch, 0, sizeof(unsigned long long), c->st));
-  CK(cudaMemsetAsync(&ctr->task_fetch_wide, 0, sizeof(unsigned long long), c->st));
-  CK(cudaMemsetAsync(&ctr->task_fetch_small, 0, sizeof(unsigned long long), c->st));
+  CK(cudaMemsetAsync(&ctr->join_head, 0, sizeof(ctr->join_head) + sizeof(ctr->sub_n), c->st));
   CK(cudaMemsetAsync(c->pair_count.p, 0, sizeof(unsigned long long) * c->rec_cap, c->st));
   CK(cudaMemsetAsync(c->pair_exp.p, 0, sizeof(unsigned long long) * c->rec_cap, c->st));
   CK(cudaMemsetAsync(c->pair_flag.p, 0, sizeof(uint32_t) * c->rec_cap, c->st));
@@ -777,6 +791,10 @@ int bms::rejoin_timed(bms_ctx* c, int bps, int wpb, int steps, float* ms) {
   ja.find_first = c->last_mode == BMS_FIND_FIRST;
   ja.literal = c->last_sem == BMS_SEM_REFERENCE_DFS;
   ja.steps = steps;
+  ja.sub[0] = c->sub[0].as<SubTask>();
+  ja.sub[1] = c->sub[1].as<SubTask>();
+  ja.sub_cap = c->sub_cap;
+  ja.split_budget = c->split_budget;
   CK(cudaEventRecord(c->ev[EV_ORDER], c->st));
   CK(launch_join(ja, sm_count() * bps, wpb * 32, c->st));
   CK(cudaEventRecord(c->ev[EV_JOIN], c->st));

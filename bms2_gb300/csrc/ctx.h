@@ -86,6 +86,9 @@ struct bms_ctx {
   uint64_t T = 0;
   // records and join
   DevBuf recs, arena, tasks, pair_count, pair_exp, pair_flag;
+  DevBuf sub[2];  // join subtrees, ping-pong between rounds
+  uint64_t sub_cap = 0;
+  uint64_t sub_cap_opt = 0;  // BMS_OPT_SUBTREE_CAP (0: automatic)
   uint64_t rec_cap = 0, row_cap = 0, task_cap = 0;
   DevBuf dperm;
   uint32_t class_begin[3] = {0, 0, 0}, class_end[3] = {0, 0, 0};
@@ -99,6 +102,7 @@ struct bms_ctx {
   bool log_vertices = false;
   int filter_kernel = 0;  // BMS_FILTER_SLICED or BMS_FILTER_BALLOT
   int join_steps = 32;
+  uint32_t split_budget = 1024;
   uint64_t budget = 0;
   bms_schedule sched{};
   cudaEvent_t ev[EV_COUNT] = {};

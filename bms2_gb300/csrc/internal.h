@@ -63,6 +63,19 @@ struct Task {
   uint32_t root;
 };
 
+// The join runs in rounds.  A search that passes the round's expansion budget
+// writes every unexplored subtree it holds — the mapped prefix of its path and
+// the candidates left at that depth — as one SubTask and stops; the next round
+// runs those subtrees in parallel.  The last round has no budget.
+constexpr int kJoinRounds = 6;
+constexpr uint32_t kNoRecord = 0xFFFFFFFFu;  // a SubTask slot that holds nothing
+struct SubTask {
+  uint32_t rec;                   // record (pair) index, or kNoRecord
+  uint32_t depth;                 // depth of the candidates; f[0..depth) is the prefix
+  uint64_t cand[2];               // candidates left at that depth
+  uint8_t f[kMaxQueryNodes];      // data node mapped at each depth of the prefix
+};
+
 // Per-query search order: perm[q*64 + t] is the vertex at depth t; dadj[q*64 + t]
 // has bit i (i < t) set iff the vertex at depth i is in the CSR row of the
 // vertex at depth t (the reference's query_adj_masks, isomorphism.hpp:383-390).
@@ -77,15 +90,15 @@ struct Counters {
   unsigned long long recs;        // PairRecs written
   unsigned long long rows;        // candidate rows allocated in the arena
   unsigned long long tasks;       // join tasks emitted
-  unsigned long long task_fetch;  // join work-stealing head
   unsigned int work[4];           // pair-filter work heads, one per size class
   unsigned long long total;       // sum of per-pair counts
   unsigned long long expansions;  // sum of per-pair expansions
   unsigned long long incomplete;  // pairs that hit the expansion budget
   unsigned long long recs_wide;   // records [0, recs_wide) come from data graphs of > 64 nodes
-  unsigned long long task_fetch_wide;  // join work-stealing head of the two-word search
   unsigned long long recs_mid;    // records [recs_wide, recs_mid) come from graphs of 33..64 nodes
-  unsigned long long task_fetch_small;  // join work-stealing head of the 32-bit search
+  // join: work-stealing head per round and record class, subtrees per round
+  unsigned long long join_head[kJoinRounds][3];
+  unsigned long long sub_n[kJoinRounds + 1];
 };
 
 // ----------------------------------------------------------------- launchers
@@ -233,6 +246,10 @@ struct JoinArgs {
   int find_first;
   int literal;                     // REFERENCE_DFS semantics
   int steps;                       // DFS steps between refills
+  SubTask* sub[2];                 // subtrees: round r reads sub[r & 1], writes sub[(r + 1) & 1]
+  uint64_t sub_cap;                // entries of each subtree buffer
+  uint32_t split_budget;           // expansions before a search splits (0: never)
+  int round;                       // set by launch_join
 };
 cudaError_t launch_join(const JoinArgs& a, int blocks, int threads, cudaStream_t st);
 

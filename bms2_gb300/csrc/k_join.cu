@@ -211,6 +211,8 @@ struct Lane {
   const uint8_t* perm;
   const uint64_t* dadj;
   int t;
+  int base;           // depth the task starts at (a subtree's prefix length)
+  bool no_split;      // the subtree buffer was full: keep the work
   Bits<T, W> cur;     // candidates left at depth t
   Bits<T, W> mapped;  // nodes mapped at depths < t
   Bits<T, W> vis;     // REFERENCE_DFS: the reference's visited bitset
@@ -241,12 +243,51 @@ __device__ __forceinline__ void finish(Lane<T, W>& L, const JoinArgs& a, const u
   L.active = false;
 }
 
+// Hand every unexplored subtree of the search to the next round: frame i in
+// [base, t) still holds F[i], frame t holds cur; each candidate left in them
+// becomes its own SubTask with the prefix f[0..i), so the next round spreads
+// the search over as many lanes as it has branches.  Returns false (and keeps
+// the work) when the buffer has no room.
 template <typename T, int W>
-__device__ __forceinline__ bool after_step(Lane<T, W>& L, const JoinArgs& a, const uint32_t* expd) {
+__device__ bool split(Lane<T, W>& L, const JoinArgs& a, const Stack<T, W>& S) {
+  uint32_t m = bpop(L.cur);
+  for (int i = L.base; i < L.t; ++i) m += bpop(S.F[i]);
+  if (m == 0) return false;  // nothing left: the next step finishes
+  SubTask* out = a.sub[(a.round + 1) & 1];
+  const unsigned long long b = atomicAdd(&a.ctr->sub_n[a.round + 1], (unsigned long long)m);
+  if (b + m > a.sub_cap) {
+    for (unsigned long long k = b; k < a.sub_cap && k < b + m; ++k) out[k].rec = kNoRecord;
+    return false;
+  }
+  unsigned long long k = b;
+  for (int i = L.base; i <= L.t; ++i) {
+    for (Bits<T, W> c = i < L.t ? S.F[i] : L.cur; bany(c); c = bclear_low(c)) {
+      const uint32_t v = blow(c);
+      SubTask& o = out[k++];
+      o.rec = L.rec;
+      o.depth = uint32_t(i);
+      o.cand[0] = v < 64 ? uint64_t(1) << v : 0ull;
+      o.cand[1] = v >= 64 ? uint64_t(1) << (v - 64) : 0ull;
+      for (int j = 0; j < i; ++j) o.f[j] = S.f[j];
+    }
+  }
+  return true;
+}
+
+template <typename T, int W>
+__device__ __forceinline__ bool after_step(Lane<T, W>& L, const JoinArgs& a, const Stack<T, W>& S) {
+  const uint32_t* expd = S.expd;
   if (a.budget && L.exps > a.budget) {
     atomicOr(&a.pair_flag[L.rec], 2u);
     finish(L, a, expd);
     return false;
+  }
+  if (a.split_budget && L.exps >= a.split_budget && !L.no_split) {
+    if (split(L, a, S)) {
+      finish(L, a, expd);
+      return false;
+    }
+    L.no_split = true;
   }
   if (a.find_first && ++L.since_check >= 64) {
     L.since_check = 0;
@@ -266,7 +307,7 @@ template <typename T, int W>
 __device__ __forceinline__ void step_counted(Lane<T, W>& L, const JoinArgs& a, Stack<T, W>& S) {
   int t = L.t;
   while (!bany(L.cur)) {  // frame t exhausted
-    if (t == 0) {
+    if (t == L.base) {
       finish(L, a, S.expd);
       return;
     }
@@ -310,7 +351,7 @@ __device__ __forceinline__ void step_counted(Lane<T, W>& L, const JoinArgs& a, S
     L.t = int(j);
     L.cur = c;
   }
-  after_step(L, a, S.expd);
+  after_step(L, a, S);
 }
 
 // ----------------------------------------------------------- in-row test
@@ -338,7 +379,7 @@ __device__ __forceinline__ void step_inrow(Lane<T, W>& L, const JoinArgs& a, Sta
   int t = L.t;
   while (!bany(L.cur)) {  // frame t exhausted
     if (a.literal && ((L.mpset >> t) & 1ull)) L.vis = bandn(L.vis, bbit<T, W>(S.mp[t]));
-    if (t == 0) {
+    if (t == L.base) {
       finish(L, a, S.expd);
       return;
     }
@@ -385,7 +426,7 @@ __device__ __forceinline__ void step_inrow(Lane<T, W>& L, const JoinArgs& a, Sta
     L.t = t + 1;
     L.cur = nf;
   }
-  after_step(L, a, S.expd);
+  after_step(L, a, S);
 }
 
 // Record class K: 2 = data graphs of 65..128 nodes (two 64-bit words), 1 =
@@ -405,16 +446,23 @@ __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
   const unsigned long long mid = max(wide, min(recs, a.ctr->recs_mid));
   const unsigned long long lo = K == 2 ? 0 : (K == 1 ? wide : mid);
   const unsigned long long hi = K == 2 ? wide : (K == 1 ? mid : recs);
+  // round 0: records (per-pair tasks) or (pair, root) tasks; later rounds:
+  // the subtrees the previous round handed over
+  const bool subtrees = a.round > 0;
+  const SubTask* sub_in = a.sub[a.round & 1];
   unsigned long long first, ntasks;
-  if (a.per_pair) {
+  if (subtrees) {
+    first = 0;
+    ntasks = min((unsigned long long)a.sub_cap, a.ctr->sub_n[a.round]);
+  } else if (a.per_pair) {
     first = lo;
     ntasks = hi - lo;
   } else {
     first = 0;
     ntasks = min((unsigned long long)a.task_cap, a.ctr->tasks);
   }
-  unsigned long long* head =
-      K == 2 ? &a.ctr->task_fetch_wide : (K == 1 ? &a.ctr->task_fetch : &a.ctr->task_fetch_small);
+  if (ntasks == 0) return;
+  unsigned long long* head = &a.ctr->join_head[a.round][K];
   const unsigned long long nwarps = (unsigned long long)(gridDim.x * blockDim.x) >> 5;
   Lane<T, W> L;
   L.active = false;
@@ -452,7 +500,12 @@ __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
         uint32_t rec;
         Bits<T, W> roots;
         bool take = true;
-        if (a.per_pair) {
+        const SubTask* sub = nullptr;
+        if (subtrees) {
+          sub = sub_in + (qbase + rank);
+          rec = sub->rec;
+          take = (K == 2 || rec >= lo) && rec < hi;  // kNoRecord is never in range
+        } else if (a.per_pair) {
           rec = uint32_t(first + qbase + rank);
         } else {
           const Task tk = a.tasks[qbase + rank];
@@ -471,17 +524,36 @@ __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
           L.irow = a.ds.adjin + 2 * uint64_t(a.d.goff[r.d]);
           L.perm = a.o.perm + uint64_t(r.q) * kMaxQueryNodes;
           L.dadj = a.o.dadj + uint64_t(r.q) * kMaxQueryNodes;
-          if (a.per_pair) roots = bload<T, W>(L.crow + 2 * uint64_t(L.perm[0]));
+          if (a.per_pair && !subtrees) roots = bload<T, W>(L.crow + 2 * uint64_t(L.perm[0]));
           L.cnt = 0;
           L.exps = 0;
           L.since_check = 0;
           L.t = 0;
-          L.cur = roots;
+          L.base = 0;
+          L.no_split = false;
           L.mapped = z<T, W>();
           L.vis = z<T, W>();
 #pragma unroll
           for (int b = 0; b < kPlanes; ++b) L.P.p[b] = z<T, W>();
           L.mpset = 0;
+          if (subtrees) {  // rebuild the prefix state of the subtree
+            const int dep = int(sub->depth);
+            L.t = dep;
+            L.base = dep;
+            roots.w[0] = T(sub->cand[0]);
+            if (W > 1) roots.w[W - 1] = T(sub->cand[1]);
+            for (int j = 0; j < dep; ++j) {
+              const uint32_t x = sub->f[j];
+              S.f[j] = uint8_t(x);
+              L.mapped = bor(L.mapped, bbit<T, W>(x));
+              if constexpr (kCounted) {
+                const Bits<T, W> row = bload<T, W>(L.arow + 2 * uint64_t(x));
+                S.row[j] = row;
+                padd(L.P, row);
+              }
+            }
+          }
+          L.cur = roots;
           if (a.vertex_exp)
             for (uint32_t t = 0; t < L.n; ++t) S.expd[t] = 0;
           if (a.find_first && (*(volatile const uint32_t*)&a.pair_flag[L.rec] & 1u)) finish(L, a, S.expd);
@@ -516,10 +588,18 @@ cudaError_t launch_class(const JoinArgs& a, int blocks, int threads, cudaStream_
 
 }  // namespace
 
-cudaError_t launch_join(const JoinArgs& a, int blocks, int threads, cudaStream_t st) {
-  cudaError_t e = launch_class<2>(a, blocks, threads, st);
-  if (e == cudaSuccess) e = launch_class<1>(a, blocks, threads, st);
-  if (e == cudaSuccess) e = launch_class<0>(a, blocks, threads, st);
+cudaError_t launch_join(const JoinArgs& args, int blocks, int threads, cudaStream_t st) {
+  JoinArgs a = args;
+  // the reference DFS's visited state does not survive a split
+  const bool splits = a.split_budget != 0 && !a.literal;
+  cudaError_t e = cudaSuccess;
+  for (int r = 0; r < (splits ? kJoinRounds : 1) && e == cudaSuccess; ++r) {
+    a.round = r;
+    a.split_budget = splits && r + 1 < kJoinRounds ? args.split_budget : 0u;
+    e = launch_class<2>(a, blocks, threads, st);
+    if (e == cudaSuccess) e = launch_class<1>(a, blocks, threads, st);
+    if (e == cudaSuccess) e = launch_class<0>(a, blocks, threads, st);
+  }
   return e;
 }
 

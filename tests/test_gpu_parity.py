@@ -203,6 +203,38 @@ def test_join_counted_and_in_row_tests_agree(ctx):
     assert np.array_equal(results[1][1][:n], results[0][1])
 
 
+@pytest.mark.parametrize("budget,cap", [(1, 0), (3, 0), (64, 0), (2, 16), (1, 1)])
+def test_join_subtree_splitting_is_exact(ctx, budget, cap):
+    # A search passing `budget` expansions hands its unexplored subtrees to the
+    # next round (cap: subtree buffer entries; tiny caps force the buffer-full
+    # path, where a search keeps its work).  Counts and per-pair expansions must
+    # equal the unsplit join and the oracle, in both induced-test variants and
+    # in find-first mode.
+    from bms2_gb300.native import OPT_SPLIT_BUDGET, OPT_SUBTREE_CAP
+    d = Graphs.synth_molecules(120, 21, 0, 0, 0, 8, 120, 1, 4)
+    q = Graphs.synth_queries(d, 12, 22, 3, 12)
+    d_hub = Graphs.parse_text(_text(d.arrays()) + line(*star(9)) + "\n")
+    try:
+        for dd in (d, d_hub):
+            load(ctx, q, dd)
+            for mode in (COUNT_ALL, FIND_FIRST):
+                want = oracle.run_pipeline(q, dd, 2, find_first=mode == FIND_FIRST)
+                ctx.set_option(OPT_SPLIT_BUDGET, 0)
+                ctx.run(2, mode, ORDER_GMCR, SEM_EXACT)
+                base_counts, base_exps = ctx.pair_counts(), ctx.pair_expansions()
+                ctx.set_option(OPT_SPLIT_BUDGET, budget)
+                ctx.set_option(OPT_SUBTREE_CAP, cap)
+                total = ctx.run(2, mode, ORDER_GMCR, SEM_EXACT)
+                assert np.array_equal(ctx.pair_counts(), want.counts)
+                assert total == want.total
+                if mode == COUNT_ALL:
+                    assert np.array_equal(base_counts, want.counts)
+                    assert np.array_equal(ctx.pair_expansions(), base_exps)
+    finally:
+        ctx.set_option(OPT_SPLIT_BUDGET, 1024)
+        ctx.set_option(OPT_SUBTREE_CAP, 0)
+
+
 def test_many_entries_graph_reads_rows_from_global_memory(ctx):
     # a 127-leaf star with every edge listed 5 times: 1270 CSR entries (more
     # than the 1024 staged in shared memory), repeated entries, 128 nodes

@@ -61,15 +61,26 @@ class Clocks:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
+        self.skip = 0
         self.out = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
 
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.out,
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.out,
                                          stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        # the sampler takes a moment to start: wait for its first line so that
+        # the samples cover the timed region
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 5.0 and self.proc.poll() is None:
+            self.out.flush()
+            if Path(self.out.name).stat().st_size > 0:
+                break
+            time.sleep(0.02)
+        self.skip = Path(self.out.name).read_text().count("\n")
 
     def stop(self) -> dict:
         if self.proc is None:
@@ -80,7 +91,7 @@ class Clocks:
         except Exception:
             self.proc.kill()
         self.out.flush()
-        rows = [r.split(",") for r in Path(self.out.name).read_text().strip().splitlines() if r.strip()]
+        rows = [r.split(",") for r in Path(self.out.name).read_text().strip().splitlines()[self.skip:] if r.strip()]
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for r in rows:
@@ -355,7 +366,7 @@ def run_reference(args) -> None:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--order", choices=["learned", "plain"], default="learned")

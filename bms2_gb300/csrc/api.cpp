@@ -76,6 +76,16 @@ int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const 
   CK(s.lab.ensure(N ? N : 1));
   CK(s.elab.ensure(E ? E : 1));
   CK(cudaMemcpyAsync(s.goff.p, s.h_goff.data(), sizeof(uint32_t) * (G + 1), cudaMemcpyHostToDevice, c->st));
+  if (&s == &c->q) {  // the fused filter screens queries longest first
+    s.h_size_order.resize(G);
+    for (uint32_t i = 0; i < G; ++i) s.h_size_order[i] = i;
+    std::stable_sort(s.h_size_order.begin(), s.h_size_order.end(), [&](uint32_t x, uint32_t y) {
+      return s.h_goff[x + 1] - s.h_goff[x] > s.h_goff[y + 1] - s.h_goff[y];
+    });
+    CK(s.size_order.ensure(sizeof(uint32_t) * (G ? G : 1)));
+    if (G)
+      CK(cudaMemcpyAsync(s.size_order.p, s.h_size_order.data(), sizeof(uint32_t) * G, cudaMemcpyHostToDevice, c->st));
+  }
   if (N) {
     CK(cudaMemcpyAsync(s.rowp.p, v.row_offsets, sizeof(uint32_t) * (N + 1), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(s.lab.p, v.node_labels, N, cudaMemcpyHostToDevice, c->st));
@@ -310,7 +320,7 @@ int run_ballot_filter(bms_ctx* c, const ShellPack& sp, int sem) {
 // word); the record counter after each launch marks the class boundary.
 int run_sliced_filter(bms_ctx* c, const ShellPack& sp, int R, int sem) {
   const uint64_t Qn = c->q.N ? c->q.N : 1;
-  const uint64_t per_node = 6 + uint64_t(R) * 16 + 256;
+  const uint64_t per_node = 6 + uint64_t(R) * 16 + 256 + 8;  // clauses, padded to groups of 8
   CK(c->prog_len.ensure(sizeof(uint32_t) * Qn));
   CK(c->prog_off.ensure(sizeof(uint32_t) * (Qn + 1)));
   CK(c->prog.ensure(sizeof(uint16_t) * Qn * per_node));
@@ -331,13 +341,16 @@ int run_sliced_filter(bms_ctx* c, const ShellPack& sp, int R, int sem) {
   a.ds = c->d.ds();
   a.filter_order = c->filter_order.as<uint8_t>();
   a.dup = c->filter_dup.as<uint8_t>();
+  a.qorder = c->q.size_order.as<uint32_t>();
   a.prog_off = c->prog_off.as<uint32_t>();
   a.prog = c->prog.as<uint16_t>();
   a.slow = c->prog_slow.as<uint8_t>();
   a.used_ids = c->prog_ids.as<uint16_t>();
+  a.used_bits = c->prog_used.as<uint32_t>();
+  a.remap = c->prog_remap.as<uint16_t>();
   a.n_used = c->prog_nused.as<uint32_t>();
   uint32_t cap = 16 + 16 + 32 + 256 + uint32_t(R) * sp.K * 15;
-  a.n_used_cap = cap < kClauseIds ? cap : kClauseIds;
+  a.n_used_cap = (cap < kClauseIds ? cap : kClauseIds) + 1;  // + the all-ones padding mask
   a.sp = sp;
   a.dperm = c->dperm.as<uint32_t>();
   a.valid = c->valid.as<uint32_t>();

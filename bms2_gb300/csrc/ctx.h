@@ -44,7 +44,8 @@ struct Side {
   uint64_t N = 0, E = 0;
   uint32_t max_nodes = 0;
   std::vector<uint32_t> h_goff;
-  DevBuf goff, rowp, col, lab, elab;
+  std::vector<uint32_t> h_size_order;  // query side: graph ids by decreasing node count
+  DevBuf goff, rowp, col, lab, elab, size_order;
   DevBuf frec, adj, adjin, ghist, glabset, maxin;
   int sig_steps = -1;
   bool asymmetric = false;

@@ -178,10 +178,13 @@ struct SlicedArgs {
   DSigs qs, ds;
   const uint8_t* filter_order;  // [Q*64]
   const uint8_t* dup;           // [Q*64]
+  const uint32_t* qorder;       // [Q] query ids by decreasing node count
   const uint32_t* prog_off;     // [Qn+1]
   const uint16_t* prog;         // compact mask indices
   const uint8_t* slow;          // [Qn] clauses outside the table
   const uint16_t* used_ids;     // compact index -> clause id
+  const uint32_t* used_bits;    // [kClauseIds/32 + 1] bit id: some query uses clause id
+  const uint16_t* remap;        // clause id -> compact index (used ids only)
   const uint32_t* n_used;       // number of used clauses (device)
   uint32_t n_used_cap;          // bound used to size shared memory
   ShellPack sp;

@@ -103,9 +103,15 @@ __device__ uint32_t query_clauses(const uint64_t* rec, int R, const ShellPack& s
   return n;
 }
 
+// Programs are padded to whole groups of 8 clause indices (16 bytes) with the
+// index of an all-ones mask, so the filter reads a group with one load.
+constexpr uint32_t kGroup = 8;
+
 __global__ void program_count_kernel(DGraphs q, DSigs qs, ShellPack sp, uint32_t* len, uint32_t* used) {
-  for (uint64_t u = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; u < q.N; u += uint64_t(gridDim.x) * blockDim.x)
-    len[u] = query_clauses<false>(qs.frec + uint64_t(kRecWords) * u, qs.R, sp, nullptr, nullptr, used);
+  for (uint64_t u = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; u < q.N; u += uint64_t(gridDim.x) * blockDim.x) {
+    const uint32_t n = query_clauses<false>(qs.frec + uint64_t(kRecWords) * u, qs.R, sp, nullptr, nullptr, used);
+    len[u] = (n + kGroup - 1) / kGroup * kGroup;
+  }
 }
 
 // compact index of every used mask id (single block)
@@ -130,35 +136,86 @@ __global__ void program_compact_kernel(const uint32_t* used, uint16_t* remap, ui
   }
 }
 
+// the all-ones mask sits right after the used ones, at index n_used
 __global__ void program_fill_kernel(DGraphs q, DSigs qs, ShellPack sp, const uint32_t* off, const uint16_t* remap,
-                                    uint16_t* prog, uint8_t* slow) {
+                                    const uint32_t* n_used, uint16_t* prog, uint8_t* slow) {
+  const uint16_t pad = uint16_t(*n_used);
   for (uint64_t u = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; u < q.N; u += uint64_t(gridDim.x) * blockDim.x) {
     uint16_t* p = prog + off[u];
     const uint32_t n = query_clauses<true>(qs.frec + uint64_t(kRecWords) * u, qs.R, sp, p, slow + u, nullptr);
     for (uint32_t i = 0; i < n; ++i) p[i] = remap[p[i]];
+    for (uint32_t i = n; i < off[u + 1] - off[u]; ++i) p[i] = pad;
   }
 }
 
 // ------------------------------------------------------------- data side
 
+
+// The data graph a block works on: its mask table and staged attributes.
 template <int W>
-__device__ __forceinline__ bool clause_holds(uint32_t id, uint32_t v, const uint8_t* lab, const uint8_t* deg,
-                                             const uint64_t* cyc, const uint64_t* path, const uint64_t* sh, int R,
-                                             const ShellPack& sp) {
-  if (id < kMDeg) return lab[v] == id;
-  if (id < kMCyc) return uint32_t(deg[v]) >= id - kMDeg + 1;
-  if (id < kMPath) {
-    const uint32_t t = (id - kMCyc) >> 3, c = ((id - kMCyc) & 7u) + 1;
-    return ((cyc[v] >> (16 * t)) & 0xFFFFull) >= c;
+struct GraphCtx {
+  const Mask<W>* tab;
+  const uint8_t* lab;
+  const uint64_t* cyc;
+  uint32_t start, m;
+  Mask<W> all;
+};
+
+// Candidate row of the query vertex at position `level` of query qg's filter
+// order.  A vertex whose record equals an earlier one in that order (dup)
+// repeats that row (read back from the arena when the query has rows, row0).
+// Returns whether the row is non-empty.
+template <int W>
+__device__ __forceinline__ bool eval_node(const SlicedArgs& a, const GraphCtx<W>& g, uint32_t qg, uint32_t level,
+                                          uint32_t row0, Mask<W>& row) {
+  const uint32_t ul = a.filter_order[uint64_t(qg) * kMaxQueryNodes + level];
+  const uint32_t src = a.dup[uint64_t(qg) * kMaxQueryNodes + ul];
+  if (src != 0xFFu) {  // same record as an earlier, non-empty row
+    if (row0 != kNoRow) {
+      const B128 c = ld_b128(a.arena + 2 * (uint64_t(row0) + src));
+      row.w[0] = c.lo;
+      if (W > 1) row.w[W - 1] = c.hi;
+    }
+    return true;
   }
-  if (id < kMShell) {
-    const uint32_t b = id - kMPath;
-    return (path[4 * v + (b >> 6)] >> (b & 63u)) & 1ull;
+  row = g.all;
+  const uint64_t u = uint64_t(a.q.goff[qg]) + ul;
+  const uint32_t pb = a.prog_off[u], pe = a.prog_off[u + 1];
+  const uint4* grp = reinterpret_cast<const uint4*>(a.prog + pb);  // pb is a multiple of 8
+  for (uint32_t k = 0; k < (pe - pb) / kGroup; ++k) {
+    const uint4 w = __ldg(grp + k);
+    row = mand(row, mand(mand(g.tab[w.x & 0xFFFFu], g.tab[w.x >> 16]), mand(g.tab[w.y & 0xFFFFu], g.tab[w.y >> 16])));
+    row = mand(row, mand(mand(g.tab[w.z & 0xFFFFu], g.tab[w.z >> 16]), mand(g.tab[w.w & 0xFFFFu], g.tab[w.w >> 16])));
+    if (!many(row)) return false;
   }
-  const uint32_t x = id - kMShell;
-  const uint32_t c = x % 15 + 1, kj = x / 15;
-  const uint32_t k = kj / sp.K, j = kj % sp.K;
-  return ((sh[uint32_t(R) * v + k] >> (4 * sp.pos[j])) & 15ull) >= c;
+  const uint8_t slow = a.slow[u];
+  if (slow && many(row)) {
+    const uint64_t rec0 = a.qs.frec[uint64_t(kRecWords) * u], rec1 = a.qs.frec[uint64_t(kRecWords) * u + 1];
+    const uint32_t ql = uint32_t(rec0 & 0xFFu), qd = uint32_t(rec0 >> 32);
+    for (uint32_t v = 0; v < g.m; ++v) {
+      bool ok = true;
+      if (slow & kSlowLabel) ok = ok && g.lab[v] == ql;
+      if (slow & kSlowDeg) {
+        const uint64_t* dr = a.ds.frec + uint64_t(kRecWords) * (uint64_t(g.start) + v);
+        ok = ok && uint32_t(dr[0] >> 32) >= qd;
+      }
+      if (slow & kSlowCyc) ok = ok && cyc_ge(g.cyc[v], rec1);
+      if (!ok) row.w[v >> 6] &= ~(uint64_t(1) << (v & 63u));
+    }
+  }
+  return many(row);
+}
+
+// Chunk ch (32 nodes) of the mask of clause id, if some query uses it; the
+// halves from zero_from on (past the graph's last node) are cleared.
+template <int W>
+__device__ __forceinline__ void put_chunk(uint32_t* tab32, const uint32_t* used, const uint16_t* remap, uint32_t id,
+                                          uint32_t ch, uint32_t bits, uint32_t zero_from) {
+  if ((used[id >> 5] >> (id & 31u)) & 1u) {
+    uint32_t* p = tab32 + uint32_t(remap[id]) * (2 * W);
+    p[ch] = bits;
+    for (uint32_t z = zero_from; z < 2 * W; ++z) p[z] = 0;
+  }
 }
 
 template <int W>
@@ -176,9 +233,22 @@ __global__ void __launch_bounds__(256) sliced_filter_kernel(SlicedArgs a) {
   uint32_t* s_valid = s_as + 2 * a.q.G;                             // [QW]
   uint8_t* s_lab = reinterpret_cast<uint8_t*>(s_valid + a.QW);      // [MAXN]
   uint8_t* s_deg = s_lab + MAXN;                                    // [MAXN]
-  __shared__ uint32_t s_count[2], s_graph, s_nvalid;
+  __shared__ uint32_t s_count[2], s_graph, s_nvalid, s_next, s_nrec;
+  __shared__ unsigned long long s_recbase;
+  __shared__ uint32_t s_used[kMaxMaskIds / 32 + 1];
+  __shared__ uint16_t s_remap[kMaxMaskIds];
   const uint32_t tid = threadIdx.x, lane = lane_id();
   const uint32_t Q = a.q.G;
+  for (uint32_t w = tid; w < kMaxMaskIds / 32 + 1; w += blockDim.x) s_used[w] = a.used_bits[w];
+  __syncthreads();
+  for (uint32_t id = tid; id < kMaxMaskIds; id += blockDim.x)
+    if ((s_used[id >> 5] >> (id & 31u)) & 1u) s_remap[id] = a.remap[id];
+  if (tid == 0) {  // the all-ones mask that pads programs; used masks never overwrite it
+    Mask<W> ones;
+#pragma unroll
+    for (int x = 0; x < W; ++x) ones.w[x] = ~0ull;
+    s_tab[min(*a.n_used, a.n_used_cap - 1)] = ones;
+  }
   for (;;) {
     __syncthreads();
     if (tid == 0) s_graph = atomicAdd(&a.ctr->work[a.class_id], 1u);
@@ -199,24 +269,79 @@ __global__ void __launch_bounds__(256) sliced_filter_kernel(SlicedArgs a) {
     }
     for (uint32_t w = tid; w < a.QW; w += blockDim.x) s_valid[w] = 0;
     if (tid < 2) s_count[tid] = 0;
-    if (tid == 0) s_nvalid = 0;
+    if (tid == 0) {
+      s_nvalid = 0;
+      s_next = 0;
+      s_nrec = 0;
+    }
     __syncthreads();
-    // one mask per used clause
-    const uint32_t n_used = min(*a.n_used, a.n_used_cap);
-    for (uint32_t i = tid; i < n_used; i += blockDim.x) {
-      const uint32_t id = a.used_ids[i];
-      Mask<W> mk;
+    // The mask table, bit-sliced: a warp takes one clause family and one
+    // 32-node chunk of the graph, lane = node; every clause of the family is
+    // one ballot, and lane i keeps the i-th ballot so the used masks are
+    // stored in parallel.  Families: labels + degrees, cycles, 8 x 32 path
+    // bits, then one per shell step (per packed label: four nibble-plane
+    // ballots, lane c-1 forms the mask of nibbles >= c).
+    {
+      const uint32_t chunks = (m + 31) >> 5;
+      const uint32_t n_items = 10 + uint32_t(R);
+      uint32_t* tab32 = reinterpret_cast<uint32_t*>(s_tab);
+      for (uint32_t it = tid >> 5; it < n_items * chunks; it += blockDim.x >> 5) {
+        const uint32_t item = it / chunks, ch = it - item * chunks;
+        const uint32_t v = ch * 32 + lane;
+        const bool in = v < m;
+        const uint32_t zero_from = ch + 1 == chunks ? chunks : 2 * W;  // halves past the graph
+        if (item < 10) {
+          uint32_t mine = 0;
+          for (uint32_t i = 0; i < 32; ++i) {
+            bool p = false;
+            if (in) {
+              if (item == 0) {
+                p = i < 16 ? uint32_t(s_lab[v]) == i : uint32_t(s_deg[v]) >= i - 15;
+              } else if (item == 1) {
+                p = ((s_cyc[v] >> (16 * (i >> 3))) & 0xFFFFull) >= (i & 7u) + 1;
+              } else {
+                const uint32_t b = (item - 2) * 32 + i;
+                p = (s_path[4 * v + (b >> 6)] >> (b & 63u)) & 1ull;
+              }
+            }
+            const uint32_t bal = __ballot_sync(0xffffffffu, p);
+            if (lane == i) mine = bal;
+          }
+          const uint32_t id = item == 0 ? kMLab + lane : (item == 1 ? kMCyc + lane : kMPath + (item - 2) * 32 + lane);
+          put_chunk<W>(tab32, s_used, s_remap, id, ch, mine, zero_from);
+        } else {
+          const uint32_t k = item - 10;
+          for (uint32_t j = 0; j < a.sp.K; ++j) {
+            const uint32_t id = kMShell + (k * a.sp.K + j) * 15 + lane;
+            const bool used = lane < 15 && ((s_used[id >> 5] >> (id & 31u)) & 1u);
+            if (!__any_sync(0xffffffffu, used)) continue;
+            const uint32_t nib = in ? uint32_t(s_sh[uint32_t(R) * v + k] >> (4 * a.sp.pos[j])) & 15u : 0u;
+            uint32_t x[4];
 #pragma unroll
-      for (int x = 0; x < W; ++x) mk.w[x] = 0;
-      for (uint32_t v = 0; v < m; ++v)
-        if (clause_holds<W>(id, v, s_lab, s_deg, s_cyc, s_path, s_sh, R, a.sp)) mk.w[v >> 6] |= uint64_t(1) << (v & 63u);
-      s_tab[i] = mk;
+            for (int b = 0; b < 4; ++b) x[b] = __ballot_sync(0xffffffffu, (nib >> b) & 1u);
+            if (used) {
+              const uint32_t c = lane + 1;  // nodes whose nibble >= c
+              uint32_t gt = 0, eq = 0xFFFFFFFFu;
+#pragma unroll
+              for (int b = 3; b >= 0; --b) {
+                if ((c >> b) & 1u) {
+                  eq &= x[b];
+                } else {
+                  gt |= eq & x[b];
+                  eq &= ~x[b];
+                }
+              }
+              put_chunk<W>(tab32, s_used, s_remap, id, ch, gt | eq, zero_from);
+            }
+          }
+        }
+      }
     }
     // screening: label set, more than one node, label multiset (join)
     const uint64_t dhist = a.ds.ghist[dg];
     const uint32_t dlab = a.ds.glabset[dg];
     for (uint32_t qb = 0; qb < Q; qb += blockDim.x) {
-      const uint32_t qg = qb + tid;
+      const uint32_t qg = qb + tid < Q ? a.qorder[qb + tid] : Q;  // longest queries first
       bool p1 = false, p2 = false;
       if (qg < Q && m > 0) {
         const uint32_t n = a.q.goff[qg + 1] - a.q.goff[qg];
@@ -235,69 +360,27 @@ __global__ void __launch_bounds__(256) sliced_filter_kernel(SlicedArgs a) {
     }
     __syncthreads();
     const Mask<W> all = mlow<W>(m);
-    // levels
-    for (uint32_t level = 0, cur = 0;; ++level, cur ^= 1u) {
-      const uint32_t count = s_count[cur];
-      if (count == 0) break;
-      uint32_t* aq = s_aq + cur * Q;
-      uint32_t* as = s_as + cur * Q;
-      uint32_t* nq = s_aq + (cur ^ 1u) * Q;
-      uint32_t* ns = s_as + (cur ^ 1u) * Q;
-      const uint32_t rounds = (count + blockDim.x - 1) / blockDim.x;
-      for (uint32_t r = 0; r < rounds; ++r) {
-        const uint32_t i = r * blockDim.x + tid;
+    const GraphCtx<W> g{s_tab, s_lab, s_cyc, start, m, all};
+    // Level 0 over the screened queries, block-parallel: it ends most pairs.
+    // Survivors get their output rows (warp-aggregated allocation) and go to
+    // list 1.
+    {
+      const uint32_t count = s_count[0];
+      for (uint32_t i0 = 0; i0 < count; i0 += blockDim.x) {
+        const uint32_t i = i0 + tid;
         const bool live = i < count;
-        uint32_t qg = 0, row0 = kNoRow, n = 0, qoff = 0;
-        bool join = false, alive = false, done = false;
-        Mask<W> row;
-#pragma unroll
-        for (int x = 0; x < W; ++x) row.w[x] = 0;
-        uint32_t ul = 0;
+        uint32_t qg = 0, n = 0;
+        bool join = false, alive = false;
+        Mask<W> row = all;
         if (live) {
-          const uint32_t e = aq[i];
+          const uint32_t e = s_aq[i];
           qg = e & 0x7FFFFFFFu;
           join = (e >> 31) != 0;
-          row0 = as[i];
-          qoff = a.q.goff[qg];
-          n = a.q.goff[qg + 1] - qoff;
-          ul = a.filter_order[uint64_t(qg) * kMaxQueryNodes + level];
-          const uint32_t src = a.dup[uint64_t(qg) * kMaxQueryNodes + ul];
-          if (src != 0xFFu) {
-            alive = true;  // same record as an earlier, non-empty row
-            if (join && row0 != kNoRow) {
-              const B128 c = ld_b128(a.arena + 2 * (uint64_t(row0) + src));
-              row.w[0] = c.lo;
-              if (W > 1) row.w[W - 1] = c.hi;
-            }
-          } else {
-            row = all;
-            const uint64_t u = uint64_t(qoff) + ul;
-            const uint32_t pb = a.prog_off[u], pe = a.prog_off[u + 1];
-            for (uint32_t p = pb; p < pe; ++p) {
-              row = mand(row, s_tab[a.prog[p]]);
-              if (((p - pb) & 7u) == 7u && !many(row)) break;
-            }
-            const uint8_t slow = a.slow[u];
-            if (slow && many(row)) {
-              const uint64_t rec0 = a.qs.frec[uint64_t(kRecWords) * u], rec1 = a.qs.frec[uint64_t(kRecWords) * u + 1];
-              const uint32_t ql = uint32_t(rec0 & 0xFFu), qd = uint32_t(rec0 >> 32);
-              for (uint32_t v = 0; v < m; ++v) {
-                bool ok = true;
-                if (slow & kSlowLabel) ok = ok && s_lab[v] == ql;
-                if (slow & kSlowDeg) {
-                  const uint64_t* dr = a.ds.frec + uint64_t(kRecWords) * (uint64_t(start) + v);
-                  ok = ok && uint32_t(dr[0] >> 32) >= qd;
-                }
-                if (slow & kSlowCyc) ok = ok && cyc_ge(s_cyc[v], rec1);
-                if (!ok) row.w[v >> 6] &= ~(uint64_t(1) << (v & 63u));
-              }
-            }
-            alive = many(row);
-          }
-          done = alive && level + 1 == n;
+          n = a.q.goff[qg + 1] - a.q.goff[qg];
+          alive = eval_node<W>(a, g, qg, 0, kNoRow, row);
         }
-        // output rows: allocated when the first row of a join-eligible query is non-empty
-        const bool need = live && alive && join && row0 == kNoRow;
+        const bool need = live && alive && join;
+        uint32_t row0 = kNoRow;
         const uint32_t nb = __ballot_sync(0xffffffffu, need);
         if (nb) {
           uint32_t incl = need ? n : 0u;
@@ -316,42 +399,67 @@ __global__ void __launch_bounds__(256) sliced_filter_kernel(SlicedArgs a) {
               join = false;
             } else {
               row0 = uint32_t(b);
+              st_b128(a.arena + 2 * (uint64_t(row0) + a.filter_order[uint64_t(qg) * kMaxQueryNodes]), to128(row));
             }
           }
         }
-        if (live && alive && join && row0 != kNoRow) st_b128(a.arena + 2 * (uint64_t(row0) + ul), to128(row));
-        // finished queries: validity bit and record; others go on
-        if (done) {
-          atomicOr(&s_valid[qg >> 5], 1u << (qg & 31u));
-        }
-        const bool rec_need = done && join && row0 != kNoRow;
-        const uint32_t rb = __ballot_sync(0xffffffffu, rec_need);
-        if (rb) {
-          unsigned long long base = 0;
-          if (lane == __ffs(rb) - 1) base = atomicAdd(&a.ctr->recs, (unsigned long long)__popc(rb));
-          base = __shfl_sync(0xffffffffu, base, __ffs(rb) - 1);
-          if (rec_need) {
-            const unsigned long long k = base + __popc(rb & ((1u << lane) - 1u));
-            if (k < a.rec_cap) a.recs[k] = PairRec{qg, dg, 0u, row0};
-            else atomicOr(a.err, kErrOverflow);
-          }
-        }
-        const bool cont = live && alive && !done;
+        const bool cont = live && alive;
         const uint32_t cb = __ballot_sync(0xffffffffu, cont);
         if (cb) {
           uint32_t base = 0;
-          if (lane == __ffs(cb) - 1) base = atomicAdd(&s_count[cur ^ 1u], __popc(cb));
+          if (lane == __ffs(cb) - 1) base = atomicAdd(&s_count[1], __popc(cb));
           base = __shfl_sync(0xffffffffu, base, __ffs(cb) - 1);
           if (cont) {
             const uint32_t k = base + __popc(cb & ((1u << lane) - 1u));
-            nq[k] = qg | (join ? 0x80000000u : 0u);
-            ns[k] = row0;
+            s_aq[Q + k] = qg | (join ? 0x80000000u : 0u);
+            s_as[Q + k] = row0;
           }
         }
       }
+    }
+    __syncthreads();
+    // Levels 1.. : each survivor runs to completion on one thread, taken from
+    // a shared counter (queries were screened longest first).  Finished
+    // join-eligible queries are collected in list 0 and written out with one
+    // global atomic per graph.
+    {
+      const uint32_t count = s_count[1];
+      for (;;) {
+        const uint32_t i = atomicAdd(&s_next, 1u);
+        if (i >= count) break;
+        const uint32_t e = s_aq[Q + i];
+        const uint32_t qg = e & 0x7FFFFFFFu;
+        const bool join = (e >> 31) != 0;
+        const uint32_t row0 = s_as[Q + i];
+        const uint32_t n = a.q.goff[qg + 1] - a.q.goff[qg];
+        bool alive = true;
+        for (uint32_t level = 1; level < n && alive; ++level) {
+          Mask<W> row = all;
+          alive = eval_node<W>(a, g, qg, level, join ? row0 : kNoRow, row);
+          if (alive && join && row0 != kNoRow)
+            st_b128(a.arena + 2 * (uint64_t(row0) + a.filter_order[uint64_t(qg) * kMaxQueryNodes + level]),
+                    to128(row));
+        }
+        if (alive) {
+          atomicOr(&s_valid[qg >> 5], 1u << (qg & 31u));
+          if (join && row0 != kNoRow) {
+            const uint32_t k = atomicAdd(&s_nrec, 1u);
+            s_aq[k] = qg;
+            s_as[k] = row0;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    {
+      const uint32_t nrec = s_nrec;
+      if (tid == 0 && nrec) s_recbase = atomicAdd(&a.ctr->recs, (unsigned long long)nrec);
       __syncthreads();
-      if (tid == 0) s_count[cur] = 0;
-      __syncthreads();
+      for (uint32_t k = tid; k < nrec; k += blockDim.x) {
+        const unsigned long long r = s_recbase + k;
+        if (r < a.rec_cap) a.recs[r] = PairRec{s_aq[k], dg, 0u, s_as[k]};
+        else atomicOr(a.err, kErrOverflow);
+      }
     }
     // validity bits and per-graph count
     uint32_t nv = 0;
@@ -397,7 +505,7 @@ cudaError_t launch_query_programs(const DGraphs& q, const DSigs& qs, ShellPack s
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   (void)prog_cap;
   (void)prog_total_host;
-  program_fill_kernel<<<blocks, 128, 0, st>>>(q, qs, sp, prog_off, remap, prog, slow); note_launch();
+  program_fill_kernel<<<blocks, 128, 0, st>>>(q, qs, sp, prog_off, remap, n_used, prog, slow); note_launch();
   return cudaGetLastError();
 }
 

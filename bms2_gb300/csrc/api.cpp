@@ -20,6 +20,8 @@ using namespace bms;
 
 namespace bms {
 
+std::atomic<unsigned long long> g_alloc_epoch{0};
+
 int fail(bms_ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg;
   bms::set_thread_error(msg);
@@ -34,6 +36,19 @@ int fail_cuda(bms_ctx* c, cudaError_t e, const char* what) {
 }  // namespace bms
 
 namespace {
+
+// Timing events are recorded as external event nodes while the stream is being
+// captured into the pipeline graph, plainly otherwise (the external flag is
+// only valid during a capture).
+cudaError_t record_event(bms_ctx* c, Ev e) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  const cudaError_t r = cudaStreamIsCapturing(c->st, &cs);
+  if (r != cudaSuccess) return r;
+  return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(c->ev[e], c->st, cudaEventRecordExternal)
+                                             : cudaEventRecord(c->ev[e], c->st);
+}
+
+void drop_plan(bms_ctx* c);
 
 int check_side_errors(bms_ctx* c, const char* side, uint32_t e) {
   if (e & kErrRows) return fail(c, BMS_EINVAL, std::string(side) + ": row offsets decrease or exceed the entry count");
@@ -61,6 +76,7 @@ int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const 
   if (E && !v.column_indices) return fail(c, BMS_EINVAL, "column_indices is null");
   s.loaded = false;
   s.sig_steps = -1;
+  ++c->load_gen;
   s.G = G;
   s.N = N;
   s.E = E;
@@ -196,7 +212,7 @@ int join_records(bms_ctx* c, int mode, int order, int sem, bool log_vertices) {
     CK(launch_plain_order(c->q.dg(), order_of(c), c->st));
   }
   CK(launch_order_adjacency(c->q.dg(), c->q.ds(), order_of(c), c->st));
-  CK(cudaEventRecord(c->ev[EV_ORDER], c->st));
+  CK(record_event(c, EV_ORDER));
   CK(cudaMemsetAsync(c->pair_count.p, 0, sizeof(unsigned long long) * c->rec_cap, c->st));
   CK(cudaMemsetAsync(c->pair_exp.p, 0, sizeof(unsigned long long) * c->rec_cap, c->st));
   CK(cudaMemsetAsync(c->pair_flag.p, 0, sizeof(uint32_t) * c->rec_cap, c->st));
@@ -239,7 +255,7 @@ int join_records(bms_ctx* c, int mode, int order, int sem, bool log_vertices) {
   const int bps = c->sched.blocks_per_sm[bucket] ? int(c->sched.blocks_per_sm[bucket]) : 3;
   const int wpb = c->sched.warps_per_block[bucket] ? int(c->sched.warps_per_block[bucket]) : 8;
   CK(launch_join(ja, sm_count() * bps, wpb * 32, c->st));
-  CK(cudaEventRecord(c->ev[EV_JOIN], c->st));
+  CK(record_event(c, EV_JOIN));
   CK(launch_totals(ctr, c->rec_cap, ja.pair_count, ja.pair_exp, ja.pair_flag, ja.find_first, ctr, c->st));
   c->last_mode = mode;
   c->last_order = order;
@@ -248,7 +264,7 @@ int join_records(bms_ctx* c, int mode, int order, int sem, bool log_vertices) {
 }
 
 int finish_run(bms_ctx* c, uint64_t* total) {
-  CK(cudaEventRecord(c->ev[EV_END], c->st));
+  CK(record_event(c, EV_END));
   CK(cudaMemcpyAsync(c->h_ctr, c->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, c->st));
   CK(cudaMemcpyAsync(c->h_err, c->errflag.p, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->st));
   CK(cudaMemcpyAsync(c->h_T, c->gmcr_off.as<uint32_t>() + c->d.G, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->st));
@@ -441,6 +457,7 @@ void bms_destroy(bms_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->st) cudaStreamSynchronize(c->st);
+  drop_plan(c);
   for (int i = 0; i < EV_COUNT; ++i)
     if (c->ev[i]) cudaEventDestroy(c->ev[i]);
   if (c->h_err) cudaFreeHost(c->h_err);
@@ -479,6 +496,10 @@ int bms_set_option(bms_ctx* c, int option, int64_t value) {
     case BMS_OPT_SPLIT_BUDGET:
       if (value < 0 || value > (int64_t(1) << 31)) return fail(c, BMS_EINVAL, "split budget must be in [0, 2^31]");
       c->split_budget = uint32_t(value);
+      return BMS_OK;
+    case BMS_OPT_CUDA_GRAPH:
+      c->use_graph = value != 0;
+      if (!c->use_graph) drop_plan(c);
       return BMS_OK;
     case BMS_OPT_SUBTREE_CAP:
       if (value < 0 || value > (int64_t(1) << 28)) return fail(c, BMS_EINVAL, "subtree capacity must be in [0, 2^28]");
@@ -536,10 +557,10 @@ int bms_signatures(bms_ctx* c, int R) {
   // signatures are a pure function of the loaded graphs: steps 1..k do not
   // change when more steps are requested, so an existing candidate matrix
   // stays valid (uploads invalidate it)
-  CK(cudaEventRecord(c->ev[EV_START], c->st));
+  CK(record_event(c, EV_START));
   int r = run_signatures(c, R);
   if (r) return r;
-  CK(cudaEventRecord(c->ev[EV_SIG], c->st));
+  CK(record_event(c, EV_SIG));
   r = read_side_errors(c);
   if (r) return r;
   c->stats.ms_signatures = elapsed(c, EV_START, EV_SIG);
@@ -554,9 +575,9 @@ int bms_filter(bms_ctx* c) {
   const uint64_t words = c->q.N * c->W;
   CK(c->cand.ensure(sizeof(uint32_t) * (words ? words : 1)));
   if (words) CK(cudaMemsetAsync(c->cand.p, 0, sizeof(uint32_t) * words, c->st));
-  CK(cudaEventRecord(c->ev[EV_SIG], c->st));
+  CK(record_event(c, EV_SIG));
   CK(launch_filter_dense(c->q.dg(), c->q.ds(), c->d.dg(), c->d.ds(), c->cand.as<uint32_t>(), c->W, c->st));
-  CK(cudaEventRecord(c->ev[EV_FILTER], c->st));
+  CK(record_event(c, EV_FILTER));
   CK(cudaStreamSynchronize(c->st));
   c->stats.ms_filter = elapsed(c, EV_SIG, EV_FILTER);
   c->have_cand = true;
@@ -569,9 +590,9 @@ int bms_refine(bms_ctx* c, int step) {
   if (!c->have_cand) return fail(c, BMS_ESTATE, "run bms_filter first");
   if (step < 1 || step > c->q.sig_steps || step > c->d.sig_steps)
     return fail(c, BMS_EINVAL, "step must be in [1, refine_steps of bms_signatures]");
-  CK(cudaEventRecord(c->ev[EV_SIG], c->st));
+  CK(record_event(c, EV_SIG));
   CK(launch_refine_dense(c->q.ds(), c->q.N, c->d.ds(), c->d.N, step, c->cand.as<uint32_t>(), c->W, c->st));
-  CK(cudaEventRecord(c->ev[EV_FILTER], c->st));
+  CK(record_event(c, EV_FILTER));
   CK(cudaStreamSynchronize(c->st));
   c->stats.ms_refine = elapsed(c, EV_SIG, EV_FILTER);
   c->mapped = c->have_qidx = c->have_results = false;
@@ -587,7 +608,7 @@ int bms_map(bms_ctx* c, uint64_t* n_pairs) {
   CK(c->vcounts.ensure(sizeof(uint32_t) * (D + 1)));
   CK(c->gmcr_off.ensure(sizeof(uint32_t) * (D + 1)));
   CK(c->scan_scratch.ensure(sizeof(uint32_t) * scan_scratch_words(D)));
-  CK(cudaEventRecord(c->ev[EV_FILTER], c->st));
+  CK(record_event(c, EV_FILTER));
   CK(launch_gmcr_dense(c->q.dg(), c->d.dg(), c->cand.as<uint32_t>(), c->W, c->valid.as<uint32_t>(), c->QW,
                        c->vcounts.as<uint32_t>(), c->st));
   CK(launch_scan_u32(c->vcounts.as<uint32_t>(), c->gmcr_off.as<uint32_t>(), D, c->scan_scratch.as<uint32_t>(), c->st));
@@ -596,7 +617,7 @@ int bms_map(bms_ctx* c, uint64_t* n_pairs) {
   c->T = *c->h_T;
   CK(c->qidx.ensure(sizeof(uint32_t) * (c->T ? c->T : 1)));
   CK(launch_gmcr_indices(c->valid.as<uint32_t>(), c->QW, c->q.G, D, c->gmcr_off.as<uint32_t>(), c->qidx.as<uint32_t>(), c->st));
-  CK(cudaEventRecord(c->ev[EV_MAP], c->st));
+  CK(record_event(c, EV_MAP));
   CK(cudaStreamSynchronize(c->st));
   c->stats.ms_map = elapsed(c, EV_FILTER, EV_MAP);
   c->mapped = true;
@@ -632,7 +653,7 @@ int bms_join(bms_ctx* c, int mode, int order, int sem, uint64_t* total) {
     if (r) return r;
     CK(cudaMemsetAsync(c->ctr.p, 0, sizeof(Counters), c->st));
     CK(cudaMemsetAsync(c->errflag.as<uint32_t>() + 2, 0, sizeof(uint32_t), c->st));
-    CK(cudaEventRecord(c->ev[EV_MAP], c->st));
+    CK(record_event(c, EV_MAP));
     CK(launch_gather_pairs(c->q.dg(), c->d.dg(), c->cand.as<uint32_t>(), c->W, c->gmcr_off.as<uint32_t>(),
                            c->qidx.as<uint32_t>(), c->row_off.as<uint32_t>(), c->recs.as<PairRec>(),
                            c->arena.as<uint64_t>(), c->st));
@@ -673,6 +694,108 @@ int bms_run(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total) {
 
 namespace {
 
+// Device work of one fused run: signatures -> filter -> GMCR -> order -> join
+// -> totals.  No host synchronisation, so it can be captured as a CUDA graph.
+int enqueue_fused(bms_ctx* c, int R, int mode, int order, int sem, bool log_vertices) {
+  const uint32_t D = c->d.G;
+  if (order == BMS_ORDER_LEARNED)
+    CK(cudaMemsetAsync(c->cand_sum.p, 0, sizeof(unsigned int) * (c->q.N ? c->q.N : 1), c->st));
+  CK(cudaMemsetAsync(c->ctr.p, 0, sizeof(Counters), c->st));
+  CK(record_event(c, EV_START));
+  int r = run_signatures(c, R);
+  if (r) return r;
+  CK(launch_label_count(c->d.dg(), c->label_count.as<unsigned long long>(), c->st));
+  CK(launch_query_prep(c->q.dg(), c->q.ds(), c->label_count.as<unsigned long long>(), c->filter_order.as<uint8_t>(),
+                       c->filter_dup.as<uint8_t>(), c->st));
+  ShellPack sp{};
+  for (uint32_t l = 0; l < 16; ++l)
+    if ((c->q.labels_lt16 >> l) & 1u) sp.pos[sp.K++] = uint8_t(l);
+  sp.PW = sp.K == 0 ? 0u : (sp.K <= 8 ? uint32_t(R + 1) / 2 : uint32_t(R));
+  CK(c->qpack.ensure(sizeof(uint64_t) * 8 * (c->q.N ? c->q.N : 1)));
+  CK(launch_pack_query_shells(c->q.dg(), c->q.ds(), sp, c->qpack.as<uint64_t>(), c->st));
+  CK(record_event(c, EV_SIG));
+  r = c->filter_kernel == BMS_FILTER_BALLOT ? run_ballot_filter(c, sp, sem) : run_sliced_filter(c, sp, R, sem);
+  if (r) return r;
+  CK(record_event(c, EV_FILTER));
+  CK(launch_scan_u32(c->vcounts.as<uint32_t>(), c->gmcr_off.as<uint32_t>(), D, c->scan_scratch.as<uint32_t>(), c->st));
+  CK(launch_pair_positions(c->recs.as<PairRec>(), c->ctr.as<Counters>(), c->rec_cap, c->valid.as<uint32_t>(), c->QW,
+                           c->gmcr_off.as<uint32_t>(), c->st));
+  CK(record_event(c, EV_MAP));
+  return join_records(c, mode, order, sem, log_vertices);
+}
+
+PlanKey plan_key(const bms_ctx* c, int R, int mode, int order, int sem) {
+  PlanKey k;
+  std::memset(&k, 0, sizeof k);
+  k.load_gen = c->load_gen;
+  k.epoch = g_alloc_epoch.load();
+  k.R = R;
+  k.mode = mode;
+  k.order = order;
+  k.sem = sem;
+  k.filter_kernel = c->filter_kernel;
+  k.join_steps = c->join_steps;
+  k.model_set = c->model_set ? 1 : 0;
+  k.split_budget = c->split_budget;
+  k.sub_cap_opt = c->sub_cap_opt;
+  k.budget = c->budget;
+  k.rec_cap = c->rec_cap;
+  k.row_cap = c->row_cap;
+  k.task_cap = c->task_cap;
+  k.sub_cap = c->sub_cap;
+  k.sched = c->sched;
+  return k;
+}
+
+bool same_key(const PlanKey& a, const PlanKey& b) { return std::memcmp(&a, &b, sizeof(PlanKey)) == 0; }
+
+void drop_plan(bms_ctx* c) {
+  if (c->plan_exec) cudaGraphExecDestroy(c->plan_exec);
+  if (c->plan_graph) cudaGraphDestroy(c->plan_graph);
+  c->plan_exec = nullptr;
+  c->plan_graph = nullptr;
+  c->plan_warm = false;
+}
+
+// Capture enqueue_fused into a graph and instantiate it; false (and no plan)
+// if anything in the capture failed.
+bool capture_plan(bms_ctx* c, int R, int mode, int order, int sem, const PlanKey& key) {
+  drop_plan(c);
+  if (cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  const unsigned long long l0 = g_launches;
+  const int r = enqueue_fused(c, R, mode, order, sem, false);
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(c->st, &g);
+  const unsigned long long launches = g_launches - l0;
+  if (r != BMS_OK || e != cudaSuccess || !g || !same_key(key, plan_key(c, R, mode, order, sem))) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    c->plan_key = key;
+    c->capture_failed = true;  // run eagerly until the key changes
+    return false;
+  }
+  cudaGraphExec_t x = nullptr;
+  if (cudaGraphInstantiate(&x, g, 0) != cudaSuccess) {
+    cudaGraphDestroy(g);
+    cudaGetLastError();
+    c->plan_key = key;
+    c->capture_failed = true;
+    return false;
+  }
+  c->plan_graph = g;
+  c->plan_exec = x;
+  c->plan_launches = launches;
+  c->plan_key = key;
+  c->plan_warm = true;
+  return true;
+}
+
+int complete_fused(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total, bool log_vertices, int attempt,
+                   unsigned long long launches);
+
 int run_fused(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total, bool log_vertices, int attempt) {
   if (!c->q.loaded || !c->d.loaded) return fail(c, BMS_ESTATE, "load query and data graphs first");
   const unsigned long long launches0 = g_launches;
@@ -696,40 +819,40 @@ int run_fused(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total, 
   }
   r = ensure_join_buffers(c);
   if (r) return r;
-  const bool learned = order == BMS_ORDER_LEARNED;
-  if (learned) {
-    CK(c->cand_sum.ensure(sizeof(unsigned int) * (c->q.N ? c->q.N : 1)));
-    CK(cudaMemsetAsync(c->cand_sum.p, 0, sizeof(unsigned int) * (c->q.N ? c->q.N : 1), c->st));
+  if (order == BMS_ORDER_LEARNED) CK(c->cand_sum.ensure(sizeof(unsigned int) * (c->q.N ? c->q.N : 1)));
+  // CUDA graph: the first run with a given key runs eagerly (and settles every
+  // allocation), the second captures the pipeline, later ones replay it.
+  bool graphable = c->use_graph && attempt == 0 && !log_vertices;
+  if (graphable) {
+    const PlanKey key = plan_key(c, R, mode, order, sem);
+    if (c->capture_failed) {
+      if (same_key(key, c->plan_key)) graphable = false;
+      else c->capture_failed = false;
+    }
   }
-  CK(cudaMemsetAsync(c->ctr.p, 0, sizeof(Counters), c->st));
-  CK(cudaEventRecord(c->ev[EV_START], c->st));
-  r = run_signatures(c, R);
-  if (r) return r;
-  CK(launch_label_count(c->d.dg(), c->label_count.as<unsigned long long>(), c->st));
-  CK(launch_query_prep(c->q.dg(), c->q.ds(), c->label_count.as<unsigned long long>(), c->filter_order.as<uint8_t>(),
-                       c->filter_dup.as<uint8_t>(), c->st));
-  ShellPack sp{};
-  for (uint32_t l = 0; l < 16; ++l)
-    if ((c->q.labels_lt16 >> l) & 1u) sp.pos[sp.K++] = uint8_t(l);
-  sp.PW = sp.K == 0 ? 0u : (sp.K <= 8 ? uint32_t(R + 1) / 2 : uint32_t(R));
-  CK(c->qpack.ensure(sizeof(uint64_t) * 8 * (c->q.N ? c->q.N : 1)));
-  CK(launch_pack_query_shells(c->q.dg(), c->q.ds(), sp, c->qpack.as<uint64_t>(), c->st));
-  CK(cudaEventRecord(c->ev[EV_SIG], c->st));
-  if (c->filter_kernel == BMS_FILTER_BALLOT) {
-    int r2 = run_ballot_filter(c, sp, sem);
-    if (r2) return r2;
-  } else {
-    int r2 = run_sliced_filter(c, sp, R, sem);
-    if (r2) return r2;
+  if (graphable) {
+    const PlanKey key = plan_key(c, R, mode, order, sem);
+    if (c->plan_warm && same_key(key, c->plan_key) && (c->plan_exec || capture_plan(c, R, mode, order, sem, key))) {
+      CK(cudaGraphLaunch(c->plan_exec, c->st));
+      return complete_fused(c, R, mode, order, sem, total, false, attempt, c->plan_launches);
+    }
+    drop_plan(c);
   }
-  CK(cudaEventRecord(c->ev[EV_FILTER], c->st));
-  CK(launch_scan_u32(c->vcounts.as<uint32_t>(), c->gmcr_off.as<uint32_t>(), D, c->scan_scratch.as<uint32_t>(), c->st));
-  CK(launch_pair_positions(c->recs.as<PairRec>(), c->ctr.as<Counters>(), c->rec_cap, c->valid.as<uint32_t>(), c->QW,
-                           c->gmcr_off.as<uint32_t>(), c->st));
-  CK(cudaEventRecord(c->ev[EV_MAP], c->st));
-  r = join_records(c, mode, order, sem, log_vertices);
+  r = enqueue_fused(c, R, mode, order, sem, log_vertices);
   if (r) return r;
-  r = finish_run(c, total);
+  r = complete_fused(c, R, mode, order, sem, total, log_vertices, attempt, g_launches - launches0);
+  if (graphable && (r == BMS_OK || r == BMS_EINCOMPLETE) && !c->plan_exec && !c->capture_failed) {
+    c->plan_key = plan_key(c, R, mode, order, sem);
+    c->plan_warm = true;
+  }
+  return r;
+}
+
+// Read the run's counters back (the one host synchronisation), check errors,
+// grow the buffers and rerun on overflow, fill the stats.
+int complete_fused(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total, bool log_vertices, int attempt,
+                   unsigned long long launches) {
+  int r = finish_run(c, total);
   if (r) return r;
   r = check_side_errors(c, "data", c->h_err[0]);
   if (r) {
@@ -746,6 +869,7 @@ int run_fused(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total, 
   if (order == BMS_ORDER_LEARNED && (c->d.asymmetric || c->q.asymmetric))
     return fail(c, BMS_EINVAL, "the learned order requires symmetric adjacency");
   if (c->h_err[2] & kErrOverflow) {
+    drop_plan(c);
     if (attempt >= 2) return fail(c, BMS_ENOMEM, "result buffers overflow");
     const Counters& h = *c->h_ctr;
     c->rec_cap = std::max<uint64_t>(c->rec_cap, h.recs + h.recs / 8 + 1024);
@@ -764,7 +888,7 @@ int run_fused(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total, 
   c->stats.ms_filter = elapsed(c, EV_SIG, EV_FILTER);
   c->stats.ms_refine = 0.f;
   c->stats.ms_map = elapsed(c, EV_FILTER, EV_MAP);
-  c->stats.kernel_launches = g_launches - launches0;
+  c->stats.kernel_launches = launches;
   c->stats.ms_order = elapsed(c, EV_MAP, EV_ORDER);
   c->stats.ms_join = elapsed(c, EV_ORDER, EV_JOIN);
   c->stats.ms_total = elapsed(c, EV_START, EV_END);
@@ -808,9 +932,9 @@ int bms::rejoin_timed(bms_ctx* c, int bps, int wpb, int steps, float* ms) {
   ja.sub[1] = c->sub[1].as<SubTask>();
   ja.sub_cap = c->sub_cap;
   ja.split_budget = c->split_budget;
-  CK(cudaEventRecord(c->ev[EV_ORDER], c->st));
+  CK(record_event(c, EV_ORDER));
   CK(launch_join(ja, sm_count() * bps, wpb * 32, c->st));
-  CK(cudaEventRecord(c->ev[EV_JOIN], c->st));
+  CK(record_event(c, EV_JOIN));
   CK(cudaEventSynchronize(c->ev[EV_JOIN]));
   *ms = elapsed(c, EV_ORDER, EV_JOIN);
   return BMS_OK;

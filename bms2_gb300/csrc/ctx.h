@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -11,6 +12,10 @@
 
 namespace bms {
 
+// Counts device (re)allocations and frees of every DevBuf: a captured pipeline
+// graph holds raw device pointers and stays valid only within one epoch.
+extern std::atomic<unsigned long long> g_alloc_epoch;
+
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
@@ -19,7 +24,10 @@ struct DevBuf {
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() { release(); }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      cudaFree(p);
+      ++g_alloc_epoch;
+    }
     p = nullptr;
     bytes = 0;
   }
@@ -30,6 +38,7 @@ struct DevBuf {
     cudaError_t e = cudaMalloc(&p, b);
     if (e == cudaSuccess) bytes = b;
     else p = nullptr;
+    ++g_alloc_epoch;
     return e;
   }
   template <class T>
@@ -59,12 +68,24 @@ struct Side {
 
 enum Ev { EV_START, EV_SIG, EV_FILTER, EV_MAP, EV_ORDER, EV_JOIN, EV_END, EV_COUNT };
 
+// Everything that decides what bms_run enqueues.  A captured graph of the
+// pipeline is replayed only while the key is unchanged (compared bytewise;
+// built from a zeroed object so padding compares equal).
+struct PlanKey {
+  unsigned long long load_gen, epoch;
+  int R, mode, order, sem, filter_kernel, join_steps, model_set;
+  uint32_t split_budget;
+  uint64_t sub_cap_opt, budget, rec_cap, row_cap, task_cap, sub_cap;
+  bms_schedule sched;
+};
+
 }  // namespace bms
 
 using bms::Counters;
 using bms::DevBuf;
 using bms::Side;
 using bms::EV_COUNT;
+using bms::PlanKey;
 
 struct bms_ctx {
   int device = 0;
@@ -106,6 +127,15 @@ struct bms_ctx {
   uint32_t split_budget = 1024;
   uint64_t budget = 0;
   bms_schedule sched{};
+  // CUDA graph of the fused pipeline (BMS_OPT_CUDA_GRAPH)
+  bool use_graph = true;
+  unsigned long long load_gen = 0;  // bumped by every upload
+  PlanKey plan_key{};
+  bool plan_warm = false;           // an eager run with plan_key completed
+  bool capture_failed = false;      // capturing plan_key failed: run it eagerly
+  cudaGraph_t plan_graph = nullptr;
+  cudaGraphExec_t plan_exec = nullptr;
+  unsigned long long plan_launches = 0;  // kernels in the graph
   cudaEvent_t ev[EV_COUNT] = {};
   bms_stats stats{};
 };

@@ -151,8 +151,11 @@ typedef enum {
   BMS_OPT_JOIN_STEPS = 2,    /* DFS steps a warp runs between refills (default 32) */
   BMS_OPT_SPLIT_BUDGET = 3,  /* expansions after which a join search hands its unexplored subtrees
                                 to the next round (default 1024; 0 = never split) */
-  BMS_OPT_SUBTREE_CAP = 4    /* entries of each of the two subtree buffers (88 B each); 0 = one per
+  BMS_OPT_SUBTREE_CAP = 4,   /* entries of each of the two subtree buffers (88 B each); 0 = one per
                                 record, at least 65,536 and at most 4,194,304 (default) */
+  BMS_OPT_CUDA_GRAPH = 5     /* 1 (default): bms_run captures its device work as a CUDA graph on the
+                                second run with unchanged inputs and settings, and replays it after;
+                                0: every run launches its kernels one by one */
 } bms_option;
 #define BMS_FILTER_SLICED 0 /* clause masks per data graph in shared memory, one thread per query */
 #define BMS_FILTER_BALLOT 1 /* one lane per data node, candidate rows formed by warp ballots */

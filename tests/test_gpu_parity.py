@@ -235,6 +235,49 @@ def test_join_subtree_splitting_is_exact(ctx, budget, cap):
         ctx.set_option(OPT_SUBTREE_CAP, 0)
 
 
+def test_cuda_graph_replay_equals_eager(ctx):
+    # bms_run captures its device work as a CUDA graph on the second run with
+    # unchanged inputs and settings and replays it afterwards; every replay must
+    # give the eager results, and any change (option, reload) must be honoured.
+    from bms2_gb300.native import OPT_CUDA_GRAPH, OPT_SPLIT_BUDGET
+    q, d = workloads.make("mol1k", 5, n_data=400, n_queries=20)
+    q2, d2 = workloads.make("mol1k", 6, n_data=250, n_queries=15)
+    want = oracle.run_pipeline(q, d, 3)
+    want2 = oracle.run_pipeline(q2, d2, 3)
+
+    def run_all(sem=SEM_EXACT):
+        total = ctx.run(3, COUNT_ALL, ORDER_GMCR, sem)
+        return total, ctx.pair_counts(), ctx.pair_expansions(), ctx.stats()["kernel_launches"]
+
+    try:
+        ctx.set_option(OPT_CUDA_GRAPH, 0)
+        load(ctx, q, d)
+        eager = run_all()
+        assert eager[0] == want.total and np.array_equal(eager[1], want.counts)
+        ctx.set_option(OPT_CUDA_GRAPH, 1)
+        for _ in range(4):  # eager, capture + launch, replay, replay
+            got = run_all()
+            assert got[0] == eager[0]
+            assert np.array_equal(got[1], eager[1]) and np.array_equal(got[2], eager[2])
+            assert got[3] == eager[3]
+        ctx.set_option(OPT_SPLIT_BUDGET, 2)  # a changed option is a new plan
+        for _ in range(3):
+            got = run_all()
+            assert np.array_equal(got[1], eager[1]) and np.array_equal(got[2], eager[2])
+        ctx.set_option(OPT_SPLIT_BUDGET, 1024)
+        load(ctx, q2, d2)  # new inputs of other sizes
+        for _ in range(3):
+            got = run_all()
+            assert got[0] == want2.total and np.array_equal(got[1], want2.counts)
+        want_lit = oracle.run_pipeline(q2, d2, 3, dfs_literal=True)
+        for _ in range(3):
+            got = run_all(SEM_REFERENCE_DFS)
+            assert np.array_equal(got[1], want_lit.counts)
+    finally:
+        ctx.set_option(OPT_CUDA_GRAPH, 1)
+        ctx.set_option(OPT_SPLIT_BUDGET, 1024)
+
+
 def test_many_entries_graph_reads_rows_from_global_memory(ctx):
     # a 127-leaf star with every edge listed 5 times: 1270 CSR entries (more
     # than the 1024 staged in shared memory), repeated entries, 128 nodes

@@ -189,6 +189,19 @@ def run_ours(args) -> None:
     extra = {}
     if order == ORDER_LEARNED:
         extra.update(train_cost_model(ctx, args.workload, seed=101, n_data=args.train_graphs))
+    schedule = None
+    if args.tune_graphs != 0:
+        # the join schedule per size bucket, tuned on seed-A inputs of the same shape
+        tq, td = workloads.make(args.workload, 101, n_data=args.tune_graphs if args.tune_graphs > 0 else None)
+        ctx.load(QUERY, tq)
+        ctx.load(DATA, td)
+        s = ctx.autotune(REFINE_STEPS, COUNT_ALL, order)
+        schedule = [{"max_data_nodes": s["max_data_nodes"][k], "word_bits": s["word_bits"][k],
+                     "split_depth": s["split_depth"][k], "blocks_per_sm": s["blocks_per_sm"][k],
+                     "warps_per_block": s["warps_per_block"][k], "steps": s["steps"][k],
+                     "split_budget": s["split_budget"][k], "tuned_join_ms": round(s["ms"][k], 3)}
+                    for k in range(3)]
+        del tq, td
     # evaluation workload (seed B; each rank its own shard)
     q, d = workloads.make(args.workload, 202 + rank, n_data=args.data_graphs)
     Q, D = q.n_graphs, d.n_graphs
@@ -335,6 +348,10 @@ def run_ours(args) -> None:
         line["results"]["learned_over_plain"] = line["results"]["plain_value"] and value / line["results"]["plain_value"]
         line["results"]["expansion_ratio_plain_over_learned"] = float(plain["plain_expansions"]) / max(1, st["expansions"])
     line["results"].update(extra)
+    if schedule is not None:
+        line["schedule"] = {"tuned_on": f"{args.workload} seed A, "
+                                        f"{args.tune_graphs if args.tune_graphs > 0 else 'all'} data graphs",
+                            "buckets": schedule}
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(q, d, os.cpu_count() or 1, args.cpu_budget)
     if rank == 0:
@@ -381,6 +398,8 @@ def main() -> None:
     ap.add_argument("--order", choices=["learned", "plain"], default="learned")
     ap.add_argument("--workload", choices=["mol100k", "mol1m", "mol10m"], default=WORKLOAD)
     ap.add_argument("--train-graphs", type=int, default=20000)
+    ap.add_argument("--tune-graphs", type=int, default=-1,
+                    help="seed-A data graphs for the join autotuner (-1: the workload's full size, 0: off)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--data-graphs", type=int, default=None, help="shrink the workload (profiling)")

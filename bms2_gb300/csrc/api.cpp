@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -21,6 +22,22 @@ using namespace bms;
 namespace bms {
 
 std::atomic<unsigned long long> g_alloc_epoch{0};
+
+bms_schedule default_schedule() {
+  bms_schedule s;
+  std::memset(&s, 0, sizeof s);
+  const uint32_t nodes[3] = {32, 64, 128};
+  for (int i = 0; i < 3; ++i) {
+    s.max_data_nodes[i] = nodes[i];
+    s.word_bits[i] = nodes[i];
+    s.split_depth[i] = 0;
+    s.blocks_per_sm[i] = 3;
+    s.warps_per_block[i] = 8;
+    s.steps[i] = 32;
+    s.split_budget[i] = 1024;
+  }
+  return s;
+}
 
 int fail(bms_ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg;
@@ -200,6 +217,52 @@ int ensure_join_buffers(bms_ctx* c) {
 
 DOrder order_of(bms_ctx* c) { return DOrder{c->perm.as<uint8_t>(), c->dadj.as<uint64_t>()}; }
 
+// One task per pair, or per (pair, root) where the schedule splits pairs; the
+// literal reference DFS restarts its visited set per root, so it always splits.
+bool needs_tasks(const bms_schedule& s, int sem) {
+  if (sem == BMS_SEM_REFERENCE_DFS) return true;
+  for (int k = 0; k < 3; ++k)
+    if (s.split_depth[k] >= 1) return true;
+  return false;
+}
+
+void class_launches(const bms_schedule& s, int sem, ClassLaunch cl[3]) {
+  for (int k = 0; k < 3; ++k) {
+    cl[k].blocks = sm_count() * int(s.blocks_per_sm[k] ? s.blocks_per_sm[k] : 3);
+    cl[k].threads = 32 * int(s.warps_per_block[k] ? s.warps_per_block[k] : 8);
+    cl[k].per_pair = (sem == BMS_SEM_REFERENCE_DFS || s.split_depth[k] >= 1) ? 0 : 1;
+    cl[k].steps = int(s.steps[k] ? s.steps[k] : 32);
+    cl[k].split_budget = s.split_budget[k];
+  }
+}
+
+// The join arguments shared by every record class (the per-class ones come
+// from class_launches).
+JoinArgs join_args(bms_ctx* c, int mode, int sem, bool log_vertices) {
+  JoinArgs ja{};
+  ja.q = c->q.dg();
+  ja.d = c->d.dg();
+  ja.ds = c->d.ds();
+  ja.o = order_of(c);
+  ja.recs = c->recs.as<PairRec>();
+  ja.arena = c->arena.as<uint64_t>();
+  ja.rec_cap = c->rec_cap;
+  ja.tasks = c->tasks.as<Task>();
+  ja.task_cap = c->task_cap;
+  ja.ctr = c->ctr.as<Counters>();
+  ja.pair_count = c->pair_count.as<unsigned long long>();
+  ja.pair_exp = c->pair_exp.as<unsigned long long>();
+  ja.pair_flag = c->pair_flag.as<uint32_t>();
+  ja.vertex_exp = log_vertices ? c->vertex_exp.as<unsigned long long>() : nullptr;
+  ja.budget = c->budget;
+  ja.find_first = mode == BMS_FIND_FIRST;
+  ja.literal = sem == BMS_SEM_REFERENCE_DFS;
+  ja.sub[0] = c->sub[0].as<SubTask>();
+  ja.sub[1] = c->sub[1].as<SubTask>();
+  ja.sub_cap = c->sub_cap;
+  return ja;
+}
+
 // Order, tasks, join and totals over the records already in place.
 int join_records(bms_ctx* c, int mode, int order, int sem, bool log_vertices) {
   const uint64_t Qslots = uint64_t(c->q.G ? c->q.G : 1) * kMaxQueryNodes;
@@ -217,44 +280,17 @@ int join_records(bms_ctx* c, int mode, int order, int sem, bool log_vertices) {
   CK(cudaMemsetAsync(c->pair_exp.p, 0, sizeof(unsigned long long) * c->rec_cap, c->st));
   CK(cudaMemsetAsync(c->pair_flag.p, 0, sizeof(uint32_t) * c->rec_cap, c->st));
   Counters* ctr = c->ctr.as<Counters>();
-  // one task per pair, or per (pair, root) when the schedule splits pairs; the
-  // literal reference DFS restarts its visited set per root, so it always splits
-  const int per_pair = (sem == BMS_SEM_REFERENCE_DFS || c->sched.split_depth[0] >= 1) ? 0 : 1;
-  if (!per_pair)
+  if (needs_tasks(c->sched, sem))
     CK(launch_task_emit(c->recs.as<PairRec>(), c->rec_cap, c->q.dg(), order_of(c), c->arena.as<uint64_t>(),
                         c->tasks.as<Task>(), c->task_cap, ctr, c->errflag.as<uint32_t>() + 2, c->st));
   if (log_vertices) {
     CK(c->vertex_exp.ensure(sizeof(unsigned long long) * (c->q.N ? c->q.N : 1)));
     CK(cudaMemsetAsync(c->vertex_exp.p, 0, sizeof(unsigned long long) * (c->q.N ? c->q.N : 1), c->st));
   }
-  JoinArgs ja{};
-  ja.q = c->q.dg();
-  ja.d = c->d.dg();
-  ja.ds = c->d.ds();
-  ja.o = order_of(c);
-  ja.recs = c->recs.as<PairRec>();
-  ja.arena = c->arena.as<uint64_t>();
-  ja.rec_cap = c->rec_cap;
-  ja.tasks = c->tasks.as<Task>();
-  ja.task_cap = c->task_cap;
-  ja.per_pair = per_pair;
-  ja.ctr = ctr;
-  ja.pair_count = c->pair_count.as<unsigned long long>();
-  ja.pair_exp = c->pair_exp.as<unsigned long long>();
-  ja.pair_flag = c->pair_flag.as<uint32_t>();
-  ja.vertex_exp = log_vertices ? c->vertex_exp.as<unsigned long long>() : nullptr;
-  ja.budget = c->budget;
-  ja.find_first = mode == BMS_FIND_FIRST;
-  ja.literal = sem == BMS_SEM_REFERENCE_DFS;
-  ja.steps = c->join_steps;
-  ja.sub[0] = c->sub[0].as<SubTask>();
-  ja.sub[1] = c->sub[1].as<SubTask>();
-  ja.sub_cap = c->sub_cap;
-  ja.split_budget = c->split_budget;
-  const int bucket = 0;
-  const int bps = c->sched.blocks_per_sm[bucket] ? int(c->sched.blocks_per_sm[bucket]) : 3;
-  const int wpb = c->sched.warps_per_block[bucket] ? int(c->sched.warps_per_block[bucket]) : 8;
-  CK(launch_join(ja, sm_count() * bps, wpb * 32, c->st));
+  const JoinArgs ja = join_args(c, mode, sem, log_vertices);
+  ClassLaunch cl[3];
+  class_launches(c->sched, sem, cl);
+  CK(launch_join(ja, cl, c->st));
   CK(record_event(c, EV_JOIN));
   CK(launch_totals(ctr, c->rec_cap, ja.pair_count, ja.pair_exp, ja.pair_flag, ja.find_first, ctr, c->st));
   c->last_mode = mode;
@@ -442,13 +478,7 @@ int bms_create(int device, bms_ctx** out) {
   if ((e = cudaMallocHost(&c->h_T, sizeof(uint32_t))) != cudaSuccess) return bad(e, "cudaMallocHost");
   std::memset(c->h_ctr, 0, sizeof(Counters));
   *c->h_T = 0;
-  const uint32_t bounds[BMS_SCHED_BUCKETS] = {8, 16, 32, 64};
-  for (int i = 0; i < BMS_SCHED_BUCKETS; ++i) {
-    c->sched.max_query_nodes[i] = bounds[i];
-    c->sched.split_depth[i] = 0;
-    c->sched.blocks_per_sm[i] = 3;
-    c->sched.warps_per_block[i] = 8;
-  }
+  c->sched = default_schedule();
   *out = c;
   return BMS_OK;
 }
@@ -458,6 +488,10 @@ void bms_destroy(bms_ctx* c) {
   cudaSetDevice(c->device);
   if (c->st) cudaStreamSynchronize(c->st);
   drop_plan(c);
+  for (auto& r : c->class_ev)
+    for (auto& k : r)
+      for (auto& e : k)
+        if (e) cudaEventDestroy(e);
   for (int i = 0; i < EV_COUNT; ++i)
     if (c->ev[i]) cudaEventDestroy(c->ev[i]);
   if (c->h_err) cudaFreeHost(c->h_err);
@@ -491,11 +525,11 @@ int bms_set_option(bms_ctx* c, int option, int64_t value) {
       return BMS_OK;
     case BMS_OPT_JOIN_STEPS:
       if (value < 1 || value > 4096) return fail(c, BMS_EINVAL, "join steps must be in [1, 4096]");
-      c->join_steps = int(value);
+      for (int i = 0; i < 3; ++i) c->sched.steps[i] = uint32_t(value);
       return BMS_OK;
     case BMS_OPT_SPLIT_BUDGET:
       if (value < 0 || value > (int64_t(1) << 31)) return fail(c, BMS_EINVAL, "split budget must be in [0, 2^31]");
-      c->split_budget = uint32_t(value);
+      for (int i = 0; i < 3; ++i) c->sched.split_budget[i] = uint32_t(value);
       return BMS_OK;
     case BMS_OPT_CUDA_GRAPH:
       c->use_graph = value != 0;
@@ -734,9 +768,7 @@ PlanKey plan_key(const bms_ctx* c, int R, int mode, int order, int sem) {
   k.order = order;
   k.sem = sem;
   k.filter_kernel = c->filter_kernel;
-  k.join_steps = c->join_steps;
   k.model_set = c->model_set ? 1 : 0;
-  k.split_budget = c->split_budget;
   k.sub_cap_opt = c->sub_cap_opt;
   k.budget = c->budget;
   k.rec_cap = c->rec_cap;
@@ -902,42 +934,56 @@ int complete_fused(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* to
 
 }  // namespace
 
-int bms::rejoin_timed(bms_ctx* c, int bps, int wpb, int steps, float* ms) {
+int bms::rejoin_timed(bms_ctx* c, const bms_schedule& sched, float* ms, float class_ms[3]) {
   if (!c->have_results) return fail(c, BMS_ESTATE, "run the pipeline first");
+  if (c->last_sem == BMS_SEM_REFERENCE_DFS) return fail(c, BMS_ESTATE, "timing runs use EXACT semantics");
   Counters* ctr = c->ctr.as<Counters>();
-  CK(cudaMemsetAsync(&ctr->join_head, 0, sizeof(ctr->join_head) + sizeof(ctr->sub_n), c->st));
-  CK(cudaMemsetAsync(c->pair_count.p, 0, sizeof(unsigned long long) * c->rec_cap, c->st));
-  CK(cudaMemsetAsync(c->pair_exp.p, 0, sizeof(unsigned long long) * c->rec_cap, c->st));
-  CK(cudaMemsetAsync(c->pair_flag.p, 0, sizeof(uint32_t) * c->rec_cap, c->st));
-  JoinArgs ja{};
-  ja.q = c->q.dg();
-  ja.d = c->d.dg();
-  ja.ds = c->d.ds();
-  ja.o = order_of(c);
-  ja.recs = c->recs.as<PairRec>();
-  ja.arena = c->arena.as<uint64_t>();
-  ja.rec_cap = c->rec_cap;
-  ja.tasks = c->tasks.as<Task>();
-  ja.task_cap = c->task_cap;
-  ja.per_pair = (c->last_sem == BMS_SEM_REFERENCE_DFS || c->sched.split_depth[0] >= 1) ? 0 : 1;
-  ja.ctr = ctr;
-  ja.pair_count = c->pair_count.as<unsigned long long>();
-  ja.pair_exp = c->pair_exp.as<unsigned long long>();
-  ja.pair_flag = c->pair_flag.as<uint32_t>();
-  ja.budget = c->budget;
-  ja.find_first = c->last_mode == BMS_FIND_FIRST;
-  ja.literal = c->last_sem == BMS_SEM_REFERENCE_DFS;
-  ja.steps = steps;
-  ja.sub[0] = c->sub[0].as<SubTask>();
-  ja.sub[1] = c->sub[1].as<SubTask>();
-  ja.sub_cap = c->sub_cap;
-  ja.split_budget = c->split_budget;
-  CK(record_event(c, EV_ORDER));
-  CK(launch_join(ja, sm_count() * bps, wpb * 32, c->st));
-  CK(record_event(c, EV_JOIN));
-  CK(cudaEventSynchronize(c->ev[EV_JOIN]));
+  static_assert(offsetof(Counters, sub_n) == offsetof(Counters, join_head) + sizeof(Counters::join_head),
+                "join heads and subtree counts are cleared together");
+  if (!c->class_ev[0][0][0])
+    for (auto& r : c->class_ev)
+      for (auto& k : r)
+        for (auto& e : k) CK(cudaEventCreate(&e));
+  ClassLaunch cl[3];
+  class_launches(sched, c->last_sem, cl);
+  const bool tasks = needs_tasks(sched, c->last_sem);
+  // a (pair, root) schedule may need a larger task buffer than the last run
+  // had: grow it and time again, as a pipeline run would
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    CK(cudaMemsetAsync(&ctr->join_head, 0, sizeof(ctr->join_head) + sizeof(ctr->sub_n), c->st));
+    CK(cudaMemsetAsync(c->errflag.as<uint32_t>() + 2, 0, sizeof(uint32_t), c->st));
+    CK(cudaMemsetAsync(c->pair_count.p, 0, sizeof(unsigned long long) * c->rec_cap, c->st));
+    CK(cudaMemsetAsync(c->pair_exp.p, 0, sizeof(unsigned long long) * c->rec_cap, c->st));
+    CK(cudaMemsetAsync(c->pair_flag.p, 0, sizeof(uint32_t) * c->rec_cap, c->st));
+    CK(record_event(c, EV_ORDER));
+    if (tasks) {
+      CK(cudaMemsetAsync(&ctr->tasks, 0, sizeof(ctr->tasks), c->st));
+      CK(launch_task_emit(c->recs.as<PairRec>(), c->rec_cap, c->q.dg(), order_of(c), c->arena.as<uint64_t>(),
+                          c->tasks.as<Task>(), c->task_cap, ctr, c->errflag.as<uint32_t>() + 2, c->st));
+    }
+    const JoinArgs ja = join_args(c, c->last_mode, c->last_sem, false);
+    CK(launch_join(ja, cl, c->st, c->class_ev));
+    CK(record_event(c, EV_JOIN));
+    CK(cudaMemcpyAsync(c->h_err + 2, c->errflag.as<uint32_t>() + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(&c->h_ctr->tasks, &ctr->tasks, sizeof(ctr->tasks), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    if (!(c->h_err[2] & kErrOverflow)) break;
+    if (attempt == 1) return fail(c, BMS_ENOMEM, "join task buffer overflow while timing");
+    c->task_cap = std::max<uint64_t>(c->task_cap, c->h_ctr->tasks + c->h_ctr->tasks / 8 + 16384);
+    CK(c->tasks.ensure(sizeof(Task) * c->task_cap));
+  }
   *ms = elapsed(c, EV_ORDER, EV_JOIN);
-  return BMS_OK;
+  bool splits = false;
+  for (int k = 0; k < 3; ++k) splits = splits || cl[k].split_budget != 0;
+  for (int k = 0; k < 3; ++k) {
+    class_ms[k] = 0.f;
+    for (int r = 0; r < (splits ? kJoinRounds : 1); ++r) {
+      float t = 0.f;
+      CK(cudaEventElapsedTime(&t, c->class_ev[r][k][0], c->class_ev[r][k][1]));
+      class_ms[k] += t;
+    }
+  }
+  return BMS_OK;  // the timed join recomputed the same per-record counts
 }
 
 namespace {
@@ -1067,11 +1113,17 @@ int bms_get_schedule(bms_ctx* c, bms_schedule* out) {
 int bms_set_schedule(bms_ctx* c, const bms_schedule* s) {
   GUARD(c);
   if (!s) return fail(c, BMS_EINVAL, "schedule is null");
-  for (int i = 0; i < BMS_SCHED_BUCKETS; ++i)
-    if (s->blocks_per_sm[i] > 32 || s->warps_per_block[i] == 0 || s->warps_per_block[i] > 32 ||
-        s->split_depth[i] > 1)
+  for (int i = 0; i < 3; ++i)
+    if (s->blocks_per_sm[i] == 0 || s->blocks_per_sm[i] > 32 || s->warps_per_block[i] == 0 ||
+        s->warps_per_block[i] > 8 || s->split_depth[i] > 1 || s->steps[i] == 0 || s->steps[i] > 4096 ||
+        s->split_budget[i] > (1u << 31))
       return fail(c, BMS_EINVAL, "schedule entry out of range");
+  const bms_schedule fixed = default_schedule();
   c->sched = *s;
+  for (int i = 0; i < BMS_SCHED_BUCKETS; ++i) {  // the bucket bounds and word widths are not settable
+    c->sched.max_data_nodes[i] = fixed.max_data_nodes[i];
+    c->sched.word_bits[i] = fixed.word_bits[i];
+  }
   return BMS_OK;
 }
 

@@ -73,8 +73,7 @@ enum Ev { EV_START, EV_SIG, EV_FILTER, EV_MAP, EV_ORDER, EV_JOIN, EV_END, EV_COU
 // built from a zeroed object so padding compares equal).
 struct PlanKey {
   unsigned long long load_gen, epoch;
-  int R, mode, order, sem, filter_kernel, join_steps, model_set;
-  uint32_t split_budget;
+  int R, mode, order, sem, filter_kernel, model_set;
   uint64_t sub_cap_opt, budget, rec_cap, row_cap, task_cap, sub_cap;
   bms_schedule sched;
 };
@@ -123,10 +122,9 @@ struct bms_ctx {
   bool model_set = false;
   bool log_vertices = false;
   int filter_kernel = 0;  // BMS_FILTER_SLICED or BMS_FILTER_BALLOT
-  int join_steps = 32;
-  uint32_t split_budget = 1024;
   uint64_t budget = 0;
   bms_schedule sched{};
+  cudaEvent_t class_ev[bms::kJoinRounds][3][2] = {};  // per-class join timers of the autotuner
   // CUDA graph of the fused pipeline (BMS_OPT_CUDA_GRAPH)
   bool use_graph = true;
   unsigned long long load_gen = 0;  // bumped by every upload
@@ -150,7 +148,11 @@ int learned_order(bms_ctx* c);
 // per-vertex features of the current records into c->features
 int compute_features(bms_ctx* c);
 // re-run the join over the tasks of the last run with a given launch shape
-int rejoin_timed(bms_ctx* c, int blocks_per_sm, int warps_per_block, int steps, float* ms);
+// The join alone over the current records with schedule `sched` (EXACT
+// semantics): total and per-class milliseconds.
+int rejoin_timed(bms_ctx* c, const bms_schedule& sched, float* ms, float class_ms[3]);
+// Buckets 0..2 = data graphs of <= 32, <= 64, <= 128 nodes; defaults.
+bms_schedule default_schedule();
 }  // namespace bms
 
 #define CK(call)                                                   \

@@ -254,7 +254,17 @@ struct JoinArgs {
   uint32_t split_budget;           // expansions before a search splits (0: never)
   int round;                       // set by launch_join
 };
-cudaError_t launch_join(const JoinArgs& a, int blocks, int threads, cudaStream_t st);
+// Launch shape and task settings of one record class (size bucket) of the join.
+struct ClassLaunch {
+  int blocks, threads;
+  int per_pair;           // 1: one task per record; 0: (pair, root) tasks
+  int steps;              // DFS steps between refills
+  uint32_t split_budget;  // 0: never split
+};
+// All rounds of the join; the per-class fields of `a` come from cl[class].
+// With timers, events [round][class][0/1] bracket each class's launches.
+cudaError_t launch_join(const JoinArgs& a, const ClassLaunch cl[3], cudaStream_t st,
+                        cudaEvent_t (*timers)[3][2] = nullptr);
 
 // Totals over the records (count, expansions, incomplete pairs) into ctr.
 cudaError_t launch_totals(const Counters* ctr_in, uint64_t rec_cap, const unsigned long long* pair_count,

@@ -588,17 +588,26 @@ cudaError_t launch_class(const JoinArgs& a, int blocks, int threads, cudaStream_
 
 }  // namespace
 
-cudaError_t launch_join(const JoinArgs& args, int blocks, int threads, cudaStream_t st) {
-  JoinArgs a = args;
+cudaError_t launch_join(const JoinArgs& args, const ClassLaunch cl[3], cudaStream_t st, cudaEvent_t (*timers)[3][2]) {
   // the reference DFS's visited state does not survive a split
-  const bool splits = a.split_budget != 0 && !a.literal;
+  bool splits = false;
+  for (int k = 0; k < 3; ++k) splits = splits || (cl[k].split_budget != 0 && !args.literal);
+  const int rounds = splits ? kJoinRounds : 1;
   cudaError_t e = cudaSuccess;
-  for (int r = 0; r < (splits ? kJoinRounds : 1) && e == cudaSuccess; ++r) {
-    a.round = r;
-    a.split_budget = splits && r + 1 < kJoinRounds ? args.split_budget : 0u;
-    e = launch_class<2>(a, blocks, threads, st);
-    if (e == cudaSuccess) e = launch_class<1>(a, blocks, threads, st);
-    if (e == cudaSuccess) e = launch_class<0>(a, blocks, threads, st);
+  for (int r = 0; r < rounds && e == cudaSuccess; ++r) {
+    for (int k = 2; k >= 0 && e == cudaSuccess; --k) {
+      JoinArgs a = args;
+      a.round = r;
+      a.per_pair = args.literal ? 0 : cl[k].per_pair;
+      a.steps = cl[k].steps;
+      a.split_budget = !args.literal && r + 1 < kJoinRounds ? cl[k].split_budget : 0u;
+      if (timers) e = cudaEventRecord(timers[r][k][0], st);
+      if (e != cudaSuccess) break;
+      e = k == 2 ? launch_class<2>(a, cl[k].blocks, cl[k].threads, st)
+                 : (k == 1 ? launch_class<1>(a, cl[k].blocks, cl[k].threads, st)
+                           : launch_class<0>(a, cl[k].blocks, cl[k].threads, st));
+      if (timers && e == cudaSuccess) e = cudaEventRecord(timers[r][k][1], st);
+    }
   }
   return e;
 }

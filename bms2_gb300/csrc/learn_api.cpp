@@ -290,35 +290,70 @@ int bms_model_train(bms_ctx* c, const float* x, const float* y, uint32_t n, uint
 // keeps the fastest.  Tasks are emitted once; every trial re-runs the join over
 // them from a reset work head.  The schedule table records the shape per query
 // size bucket (one shape serves all buckets of the single persistent launch).
+// Coordinate search over the join schedule, all buckets at once: every
+// candidate value of one column is tried for the three buckets together, each
+// bucket's kernels are timed on their own (best of two runs), and each bucket
+// keeps its fastest value before the next column is searched.
 int bms_autotune(bms_ctx* c, int R, int mode, int order, bms_schedule* out) {
   GUARD(c);
   uint64_t total = 0;
   int r = bms_run(c, R, mode, order, BMS_SEM_EXACT, &total);
   if (r && r != BMS_EINCOMPLETE) return r;
-  struct Shape {
-    int bps, wpb, steps;
+  bms_schedule best = c->sched;
+  float best_ms[3];
+  auto timed = [&](const bms_schedule& s, float cms[3]) -> int {
+    float ms = 0.f, a[3], b[3];
+    int rr = rejoin_timed(c, s, &ms, a);
+    if (rr) return rr;
+    rr = rejoin_timed(c, s, &ms, b);
+    if (rr) return rr;
+    for (int k = 0; k < 3; ++k) cms[k] = std::min(a[k], b[k]);
+    return BMS_OK;
   };
-  const Shape shapes[] = {{2, 8, 32}, {3, 8, 32}, {4, 8, 32}, {6, 4, 32}, {3, 8, 16}, {3, 8, 64}, {2, 16, 32}};
-  float best = 3.0e38f;
-  Shape pick = shapes[1];
-  for (const Shape& sh : shapes) {
-    float ms = 0.f, ms2 = 0.f;
-    r = rejoin_timed(c, sh.bps, sh.wpb, sh.steps, &ms);
-    if (r) return r;
-    r = rejoin_timed(c, sh.bps, sh.wpb, sh.steps, &ms2);
-    if (r) return r;
-    ms = std::min(ms, ms2);
-    if (ms < best) {
-      best = ms;
-      pick = sh;
+  r = timed(best, best_ms);
+  if (r) return r;
+  struct Shape {
+    uint32_t bps, wpb;
+  };
+  const Shape shapes[] = {{2, 8}, {3, 8}, {4, 8}, {6, 4}, {8, 4}, {12, 2}};  // <= 256 threads per block
+  const uint32_t budgets[] = {256, 1024, 4096, 0};
+  const uint32_t steps[] = {16, 32, 64};
+  const uint32_t depths[] = {0, 1};
+  auto sweep = [&](int n, auto apply) -> int {
+    for (int i = 0; i < n; ++i) {
+      bms_schedule s = best;
+      for (int k = 0; k < 3; ++k) apply(s, k, i);
+      float cms[3];
+      const int rr = timed(s, cms);
+      if (rr) return rr;
+      for (int k = 0; k < 3; ++k)
+        if (cms[k] < best_ms[k]) {
+          best_ms[k] = cms[k];
+          bms_schedule pick = best;
+          apply(pick, k, i);
+          best.blocks_per_sm[k] = pick.blocks_per_sm[k];
+          best.warps_per_block[k] = pick.warps_per_block[k];
+          best.split_budget[k] = pick.split_budget[k];
+          best.steps[k] = pick.steps[k];
+          best.split_depth[k] = pick.split_depth[k];
+        }
     }
-  }
-  for (int b = 0; b < BMS_SCHED_BUCKETS; ++b) {
-    c->sched.blocks_per_sm[b] = uint32_t(pick.bps);
-    c->sched.warps_per_block[b] = uint32_t(pick.wpb);
-    c->sched.ms[b] = best;
-  }
-  c->join_steps = pick.steps;
+    return BMS_OK;
+  };
+  r = sweep(int(sizeof(shapes) / sizeof(shapes[0])), [&](bms_schedule& s, int k, int i) {
+    s.blocks_per_sm[k] = shapes[i].bps;
+    s.warps_per_block[k] = shapes[i].wpb;
+  });
+  if (r) return r;
+  r = sweep(4, [&](bms_schedule& s, int k, int i) { s.split_budget[k] = budgets[i]; });
+  if (r) return r;
+  r = sweep(3, [&](bms_schedule& s, int k, int i) { s.steps[k] = steps[i]; });
+  if (r) return r;
+  r = sweep(2, [&](bms_schedule& s, int k, int i) { s.split_depth[k] = depths[i]; });
+  if (r) return r;
+  for (int k = 0; k < 3; ++k) best.ms[k] = best_ms[k];
+  best.ms[3] = 0.f;
+  c->sched = best;
   if (out) *out = c->sched;
   return BMS_OK;
 }

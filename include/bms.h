@@ -274,18 +274,27 @@ int bms_model_load(bms_ctx* ctx, const char* path);
 int bms_model_predict(bms_ctx* ctx, float* cost, uint8_t* order);
 
 /* ------------------------------------------------------------ scheduling */
-/* Schedule of the persistent join: task granularity (split_depth 0 = one
- * task per pair, 1 = one task per (pair, root)), launch shape and DFS steps
- * between refills.  The table has one row per query-size bucket; the single
- * persistent launch uses the shape of bucket 0.  bms_autotune times candidate
- * schedules on the loaded workload and installs the fastest. */
+/* Schedule of the persistent join, one row per size bucket.  Bucket b holds
+ * the (query, data graph) pairs whose data graph has at most max_data_nodes[b]
+ * nodes (32, 64, 128; bucket 3 is unused) and searches with bitsets of
+ * word_bits[b] bits (32, 64, 128; both fixed by the bucket).  Per bucket:
+ * task granularity (split_depth 0 = one task per pair, 1 = one per (pair,
+ * root)), launch shape, DFS steps a warp runs between refills, and the
+ * expansions after which a search hands its unexplored subtrees to the next
+ * round (0 = never).  bms_autotune times candidate schedules of every bucket
+ * on the loaded workload (each bucket's kernels timed on their own) and
+ * installs the fastest; ms[b] is the bucket's join time under the chosen row.
+ * BMS_OPT_JOIN_STEPS and BMS_OPT_SPLIT_BUDGET set their column for every bucket. */
 #define BMS_SCHED_BUCKETS 4
 typedef struct {
-  uint32_t max_query_nodes[BMS_SCHED_BUCKETS]; /* bucket upper bounds */
-  uint32_t split_depth[BMS_SCHED_BUCKETS];     /* 0 = (pair) tasks, 1 = (pair, root) tasks */
+  uint32_t max_data_nodes[BMS_SCHED_BUCKETS]; /* read-only */
+  uint32_t word_bits[BMS_SCHED_BUCKETS];      /* read-only */
+  uint32_t split_depth[BMS_SCHED_BUCKETS];
   uint32_t blocks_per_sm[BMS_SCHED_BUCKETS];
-  uint32_t warps_per_block[BMS_SCHED_BUCKETS];
-  float ms[BMS_SCHED_BUCKETS];                 /* measured by the autotuner */
+  uint32_t warps_per_block[BMS_SCHED_BUCKETS]; /* 1..8 */
+  uint32_t steps[BMS_SCHED_BUCKETS];
+  uint32_t split_budget[BMS_SCHED_BUCKETS];
+  float ms[BMS_SCHED_BUCKETS];
 } bms_schedule;
 int bms_get_schedule(bms_ctx* ctx, bms_schedule* out);
 int bms_set_schedule(bms_ctx* ctx, const bms_schedule* s);

@@ -367,19 +367,45 @@ def test_expansion_budget_marks_pairs_incomplete(ctx):
     assert full == oracle.run_pipeline(q, d, 0).total
 
 
-@pytest.mark.parametrize("split", [0, 1])
-def test_task_granularity_does_not_change_counts(ctx, wl, split):
-    q, d = wl
+@pytest.mark.parametrize("split", [(0, 0, 0), (1, 1, 1), (1, 0, 1), (0, 1, 0)])
+def test_task_granularity_does_not_change_counts(ctx, split):
+    # per size bucket: one task per pair (0) or per (pair, root) (1); data
+    # graphs of 8-120 nodes fill all three buckets
+    d = Graphs.synth_molecules(150, 31, 0, 0, 0, 8, 120, 1, 4)
+    q = Graphs.synth_queries(d, 14, 32, 3, 12)
     want = oracle.run_pipeline(q, d, 3)
     load(ctx, q, d)
     sched = ctx.schedule()
     try:
-        ctx.set_schedule({**sched, "split_depth": [split] * 4})
+        ctx.set_schedule({**sched, "split_depth": list(split) + [0]})
         assert ctx.run(3, COUNT_ALL, ORDER_GMCR, SEM_EXACT) == want.total
         assert np.array_equal(ctx.pair_counts(), want.counts)
         assert ctx.run(3, FIND_FIRST, ORDER_GMCR, SEM_EXACT) == int((want.counts > 0).sum())
     finally:
         ctx.set_schedule(sched)
+
+
+def test_autotune_picks_a_valid_schedule_and_keeps_counts(ctx):
+    d = Graphs.synth_molecules(400, 41, 0, 0, 0, 8, 120, 1, 4)
+    q = Graphs.synth_queries(d, 16, 42, 3, 14)
+    want = oracle.run_pipeline(q, d, 2)
+    load(ctx, q, d)
+    before = ctx.schedule()
+    try:
+        s = ctx.autotune(2)
+        assert s["max_data_nodes"][:3] == [32, 64, 128] and s["word_bits"][:3] == [32, 64, 128]
+        for k in range(3):
+            assert s["blocks_per_sm"][k] in (2, 3, 4, 6, 8, 12)
+            assert s["warps_per_block"][k] in (2, 4, 8)
+            assert s["steps"][k] in (16, 32, 64)
+            assert s["split_budget"][k] in (0, 256, 1024, 4096)
+            assert s["split_depth"][k] in (0, 1)
+            assert s["ms"][k] >= 0.0
+        assert ctx.schedule() == s
+        assert ctx.run(2, COUNT_ALL, ORDER_GMCR, SEM_EXACT) == want.total
+        assert np.array_equal(ctx.pair_counts(), want.counts)
+    finally:
+        ctx.set_schedule(before)
 
 
 @pytest.mark.parametrize("kernel", [0, 1])

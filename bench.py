@@ -190,7 +190,7 @@ def run_ours(args) -> None:
     if order == ORDER_LEARNED:
         extra.update(train_cost_model(ctx, args.workload, seed=101, n_data=args.train_graphs))
     schedule = None
-    if args.tune_graphs != 0:
+    if args.tune_graphs != 0 and not args.once:
         # the join schedule per size bucket, tuned on seed-A inputs of the same shape
         tq, td = workloads.make(args.workload, 101, n_data=args.tune_graphs if args.tune_graphs > 0 else None)
         ctx.load(QUERY, tq)

@@ -99,9 +99,10 @@ int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const 
   s.E = E;
   s.max_nodes = mx;
   s.h_goff.assign(v.graph_offsets, v.graph_offsets + G + 1);
-  s.labels_lt16 = 0;
-  for (uint64_t i = 0; i < N; ++i)
-    if (v.node_labels[i] < 16) s.labels_lt16 |= 1u << v.node_labels[i];
+  s.labels_lt16 = 0;  // the query side's label set packs the shell clauses
+  if (&s == &c->q)
+    for (uint64_t i = 0; i < N; ++i)
+      if (v.node_labels[i] < 16) s.labels_lt16 |= 1u << v.node_labels[i];
   if (!G) s.h_goff.assign(1, 0);
   CK(s.goff.ensure(sizeof(uint32_t) * (G + 1)));
   CK(s.rowp.ensure(sizeof(uint32_t) * (N + 1)));
@@ -148,26 +149,30 @@ void invalidate_downstream(bms_ctx* c) {
   c->have_vexp = false;
 }
 
-// data graphs grouped by size class: <= 32, <= 64, <= 128 nodes
+// Data graphs grouped by size class, largest class first (it carries the most
+// work): 65..128 nodes, 33..64, then <= 32 (empty graphs included).  One
+// counting pass and one placement pass.
 int build_classes(bms_ctx* c) {
-  std::vector<uint32_t> perm;
-  perm.reserve(c->d.G);
-  const uint32_t bounds[3] = {32, 64, 128};
-  uint32_t lo = 0;
-  for (int k = 2; k >= 0; --k) {  // largest graphs first: they carry the most work
-    const uint32_t hi = bounds[k], lo_k = k ? bounds[k - 1] : 0;
-    c->class_begin[k] = uint32_t(perm.size());
-    for (uint32_t g = 0; g < c->d.G; ++g) {
-      const uint32_t m = c->d.h_goff[g + 1] - c->d.h_goff[g];
-      if (m > lo_k && m <= hi) perm.push_back(g);
-      if (k == 0 && m == 0) perm.push_back(g);
-    }
-    c->class_end[k] = uint32_t(perm.size());
+  const uint32_t G = c->d.G;
+  const uint32_t* go = c->d.h_goff.data();
+  auto cls = [&](uint32_t g) -> int {
+    const uint32_t m = go[g + 1] - go[g];
+    return m > 64 ? 2 : (m > 32 ? 1 : 0);
+  };
+  uint32_t count[3] = {0, 0, 0};
+  for (uint32_t g = 0; g < G; ++g) ++count[cls(g)];
+  uint32_t at[3];
+  at[2] = 0;
+  at[1] = count[2];
+  at[0] = count[2] + count[1];
+  for (int k = 0; k < 3; ++k) {
+    c->class_begin[k] = at[k];
+    c->class_end[k] = at[k] + count[k];
   }
-  (void)lo;
-  CK(c->dperm.ensure(sizeof(uint32_t) * (perm.size() ? perm.size() : 1)));
-  if (!perm.empty())
-    CK(cudaMemcpyAsync(c->dperm.p, perm.data(), sizeof(uint32_t) * perm.size(), cudaMemcpyHostToDevice, c->st));
+  c->h_dperm.resize(G);
+  for (uint32_t g = 0; g < G; ++g) c->h_dperm[at[cls(g)]++] = g;
+  CK(c->dperm.ensure(sizeof(uint32_t) * (G ? G : 1)));
+  if (G) CK(cudaMemcpyAsync(c->dperm.p, c->h_dperm.data(), sizeof(uint32_t) * G, cudaMemcpyHostToDevice, c->st));
   return BMS_OK;
 }
 

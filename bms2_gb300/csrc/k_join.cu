@@ -191,12 +191,17 @@ __device__ __forceinline__ void psub(Planes<T, W>& P, Bits<T, W> borrow) {
     borrow = nb;
   }
 }
-// nodes whose count equals k (k < 2^kPlanes)
+// nodes whose count plus their bit in `add` equals k (k < 2^kPlanes): the
+// sum is formed plane by plane (ripple carry) without storing it
 template <typename T, int W>
-__device__ __forceinline__ Bits<T, W> peq(const Planes<T, W>& P, uint32_t k) {
+__device__ __forceinline__ Bits<T, W> peq_added(const Planes<T, W>& P, Bits<T, W> carry, uint32_t k) {
   Bits<T, W> m = ones<T, W>();
 #pragma unroll
-  for (int b = 0; b < kPlanes; ++b) m = ((k >> b) & 1u) ? band(m, P.p[b]) : bandn(m, P.p[b]);
+  for (int b = 0; b < kPlanes; ++b) {
+    const Bits<T, W> sum = bxor(P.p[b], carry);
+    carry = band(P.p[b], carry);
+    m = ((k >> b) & 1u) ? band(m, sum) : bandn(m, sum);
+  }
   return m;
 }
 
@@ -327,10 +332,8 @@ __device__ __forceinline__ void step_counted(Lane<T, W>& L, const JoinArgs& a, S
   c = bandn(c, mapped);
   if ((dm >> t) & 1ull) c = band(c, row);
   for (uint64_t pm = dm & ~(uint64_t(1) << t); pm; pm &= pm - 1) c = band(c, S.row[__ffsll((long long)pm) - 1]);
-  Planes<T, W> P = L.P;
-  padd(P, row);
   const uint32_t k = uint32_t(__popcll(dm));
-  c = k < (1u << kPlanes) ? band(c, peq(P, k)) : z<T, W>();
+  c = k < (1u << kPlanes) ? band(c, peq_added(L.P, row, k)) : z<T, W>();
   L.exps += 1;
   if (a.vertex_exp) S.expd[t] += 1;
   if (j + 1 == L.n) {  // depth j is the leaf level: count it without expanding
@@ -346,7 +349,7 @@ __device__ __forceinline__ void step_counted(Lane<T, W>& L, const JoinArgs& a, S
     S.F[t] = L.cur;
     S.f[t] = uint8_t(v);
     S.row[t] = row;
-    L.P = P;
+    padd(L.P, row);
     L.mapped = mapped;
     L.t = int(j);
     L.cur = c;

@@ -173,7 +173,7 @@ def run_ours(args) -> None:
     import torch
     import torch.distributed as dist
 
-    from bms2_gb300 import COUNT_ALL, DATA, ORDER_GMCR, ORDER_LEARNED, QUERY, SEM_EXACT, Context, workloads
+    from bms2_gb300 import COUNT_ALL, DATA, ORDER_GMCR, ORDER_LEARNED, QUERY, SEM_EXACT, Context, shards, workloads
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -271,11 +271,10 @@ def run_ours(args) -> None:
         dist.barrier()
     clk = clocks.stop()
     t_total = float(np.sum(ms_steps)) / 1e3
-    if world > 1:
-        tt = torch.tensor([t_total], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_total = float(tt.item())
     st = stage[-1]
+    all_total, all_valid = int(total), int(st["n_valid_pairs"])
+    if world > 1:  # shards: sum of counts, slowest rank's time
+        all_total, all_valid, t_total = shards.reduce_totals(all_total, all_valid, t_total, device=dev)
     # e2e: host buffers in, counts out, through the C ABI
     pin = {k: torch.from_numpy(v).pin_memory() for k, v in da.items()}
     qpin = {k: torch.from_numpy(v).pin_memory() for k, v in qa.items()}
@@ -340,7 +339,8 @@ def run_ours(args) -> None:
                      ("ms_signatures", "ms_filter", "ms_map", "ms_order", "ms_join", "ms_total")},
         "clocks": clk,
         "gpu_launches": int(launches),
-        "results": {"total_matches": int(total), "valid_pairs": int(T), "expansions": int(st["expansions"])},
+        "results": {"total_matches": int(total), "valid_pairs": int(T), "expansions": int(st["expansions"]),
+                    "total_matches_all_ranks": all_total, "valid_pairs_all_ranks": all_valid},
     }
     if plain is not None:
         line["results"].update(plain)

@@ -74,10 +74,14 @@ int check_side_errors(bms_ctx* c, const char* side, uint32_t e) {
   return BMS_OK;
 }
 
-int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const char* name) {
+// Upload a batch.  With `slice` the view is a window of a larger batch: its
+// offsets and column ids are global, graph_offsets[0] and row_offsets[0] give
+// the window's first node and entry, and the ids are rebased on the device.
+int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const char* name, bool slice = false) {
   if (v.n_graphs && !v.graph_offsets) return fail(c, BMS_EINVAL, "graph_offsets is null");
   const uint32_t G = v.n_graphs;
-  if (G && v.graph_offsets[0] != 0) return fail(c, BMS_EINVAL, "graph_offsets[0] must be 0");
+  const uint32_t node_base = slice && G ? v.graph_offsets[0] : 0;
+  if (G && v.graph_offsets[0] != node_base) return fail(c, BMS_EINVAL, "graph_offsets[0] must be 0");
   uint32_t mx = 0;
   for (uint32_t i = 0; i < G; ++i) {
     if (v.graph_offsets[i + 1] < v.graph_offsets[i]) return fail(c, BMS_EINVAL, "graph_offsets must be non-decreasing");
@@ -86,10 +90,11 @@ int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const 
   if (mx > limit)
     return fail(c, BMS_EUNSUPPORTED,
                 std::string(name) + " graph with " + std::to_string(mx) + " nodes exceeds the limit of " + std::to_string(limit));
-  const uint64_t N = G ? v.graph_offsets[G] : 0;
+  const uint64_t N = G ? v.graph_offsets[G] - node_base : 0;
   if (N && (!v.row_offsets || !v.node_labels)) return fail(c, BMS_EINVAL, "row_offsets or node_labels is null");
-  const uint64_t E = N ? v.row_offsets[N] : 0;
-  if (N && v.row_offsets[0] != 0) return fail(c, BMS_EINVAL, "row_offsets[0] must be 0");
+  const uint32_t entry_base = slice && N ? v.row_offsets[0] : 0;
+  const uint64_t E = N ? v.row_offsets[N] - entry_base : 0;
+  if (N && v.row_offsets[0] != entry_base) return fail(c, BMS_EINVAL, "row_offsets[0] must be 0");
   if (E && !v.column_indices) return fail(c, BMS_EINVAL, "column_indices is null");
   s.loaded = false;
   s.sig_steps = -1;
@@ -99,6 +104,8 @@ int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const 
   s.E = E;
   s.max_nodes = mx;
   s.h_goff.assign(v.graph_offsets, v.graph_offsets + G + 1);
+  if (node_base)
+    for (auto& x : s.h_goff) x -= node_base;
   s.labels_lt16 = 0;  // the query side's label set packs the shell clauses
   if (&s == &c->q)
     for (uint64_t i = 0; i < N; ++i)
@@ -131,6 +138,7 @@ int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const 
     if (v.edge_labels) CK(cudaMemcpyAsync(s.elab.p, v.edge_labels, E, cudaMemcpyHostToDevice, c->st));
     else CK(cudaMemsetAsync(s.elab.p, 0, E, c->st));
   }
+  if (N) CK(launch_rebase(s.rowp.as<uint32_t>(), N + 1, entry_base, s.col.as<uint32_t>(), E, node_base, c->st));
   CK(s.frec.ensure(sizeof(uint64_t) * kRecWords * (N ? N : 1)));
   CK(s.adj.ensure(sizeof(uint64_t) * 2 * (N ? N : 1)));
   CK(s.adjin.ensure(sizeof(uint64_t) * 2 * (N ? N : 1)));
@@ -726,6 +734,58 @@ int bms_run(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total) {
     return run_fused(c, R, mode, order, sem, total, log, 0);
   } catch (...) {
     return fail(c, BMS_ENOMEM, "host exception in bms_run");
+  }
+}
+
+int bms_run_batches(bms_ctx* c, const bms_graphs* data, uint32_t batch_graphs, int R, int mode, int order, int sem,
+                    uint64_t* total, uint64_t* per_query) {
+  GUARD(c);
+  if (!data) return fail(c, BMS_EINVAL, "data is null");
+  if (!c->q.loaded) return fail(c, BMS_ESTATE, "load the query graphs first");
+  if (batch_graphs == 0) batch_graphs = 100000;  // BMS2_batch.cpp:12
+  try {
+    const uint32_t G = data->n_graphs(), Q = c->q.G;
+    if (per_query) {
+      CK(c->per_query.ensure(sizeof(unsigned long long) * (Q ? Q : 1)));
+      CK(cudaMemsetAsync(c->per_query.p, 0, sizeof(unsigned long long) * (Q ? Q : 1), c->st));
+    }
+    uint64_t sum = 0;
+    int incomplete = 0;
+    uint32_t g0 = 0;
+    do {
+      const uint32_t g1 = std::min<uint64_t>(G, uint64_t(g0) + batch_graphs);
+      const uint32_t n0 = data->goff[g0];
+      bms_graphs_view v{};
+      v.n_graphs = g1 - g0;
+      v.graph_offsets = data->goff.data() + g0;
+      v.row_offsets = data->rowp.data() + n0;
+      v.column_indices = data->col.data() + (data->col.empty() ? 0 : data->rowp[n0]);
+      v.node_labels = data->lab.data() + n0;
+      v.edge_labels = data->elab.data() + (data->elab.empty() ? 0 : data->rowp[n0]);
+      invalidate_downstream(c);
+      int r = upload(c, c->d, v, kMaxDataNodes, "data", true);
+      if (r) return r;
+      r = build_classes(c);
+      if (r) return r;
+      uint64_t t = 0;
+      r = run_fused(c, R, mode, order, sem, &t, false, 0);
+      if (r == BMS_EINCOMPLETE) incomplete = 1;
+      else if (r) return r;
+      sum += t;
+      if (per_query)
+        CK(launch_query_totals(c->recs.as<PairRec>(), c->ctr.as<Counters>(), c->rec_cap,
+                               c->pair_count.as<unsigned long long>(), mode == BMS_FIND_FIRST, Q,
+                               c->per_query.as<unsigned long long>(), c->st));
+      g0 = g1;
+    } while (g0 < G);
+    if (per_query && Q) {
+      CK(cudaMemcpyAsync(per_query, c->per_query.p, sizeof(uint64_t) * Q, cudaMemcpyDeviceToHost, c->st));
+      CK(cudaStreamSynchronize(c->st));
+    }
+    if (total) *total = sum;
+    return incomplete ? fail(c, BMS_EINCOMPLETE, "some pairs hit the expansion budget") : BMS_OK;
+  } catch (...) {
+    return fail(c, BMS_ENOMEM, "host exception in bms_run_batches");
   }
 }
 

@@ -108,6 +108,7 @@ struct bms_ctx {
   // records and join
   DevBuf recs, arena, tasks, pair_count, pair_exp, pair_flag;
   DevBuf sub[2];  // join subtrees, ping-pong between rounds
+  DevBuf per_query;  // bms_run_batches: per-query totals
   uint64_t sub_cap = 0;
   uint64_t sub_cap_opt = 0;  // BMS_OPT_SUBTREE_CAP (0: automatic)
   uint64_t rec_cap = 0, row_cap = 0, task_cap = 0;

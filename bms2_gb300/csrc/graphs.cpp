@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <thread>
 #include <fstream>
 #include <new>
 #include <sstream>
@@ -174,7 +175,10 @@ using bms::set_thread_error;
 
 namespace {
 
-int parse_buffer(const char* text, size_t len, uint32_t max_graphs, int skip_invalid, bms_graphs** out) {
+// Serial parse of one buffer; a malformed line is reported with its number
+// counted from first_line.
+int parse_serial(const char* text, size_t len, uint32_t max_graphs, int skip_invalid, size_t first_line,
+                 bms_graphs** out) {
   if (!out) return BMS_EINVAL;
   *out = nullptr;
   bms_graphs* g = new (std::nothrow) bms_graphs();
@@ -182,7 +186,7 @@ int parse_buffer(const char* text, size_t len, uint32_t max_graphs, int skip_inv
   std::vector<uint8_t> labels;
   std::vector<bms::Edge> edges;
   std::string err;
-  size_t line_no = 0;
+  size_t line_no = first_line;
   const char* p = text;
   const char* end = text + len;
   try {
@@ -218,6 +222,80 @@ int parse_buffer(const char* text, size_t len, uint32_t max_graphs, int skip_inv
     set_thread_error("out of host memory while parsing");
     return BMS_ENOMEM;
   }
+  *out = g;
+  return BMS_OK;
+}
+
+// Append batch b to a (ids rebased); false if the 32-bit id space overflows.
+bool append_batch(bms_graphs& a, const bms_graphs& b) {
+  const uint64_t n0 = a.lab.size(), e0 = a.col.size();
+  if (n0 + b.lab.size() > 0xFFFFFFF0ull || e0 + b.col.size() > 0xFFFFFFF0ull) return false;
+  a.goff.reserve(a.goff.size() + b.n_graphs());
+  for (size_t i = 1; i < b.goff.size(); ++i) a.goff.push_back(uint32_t(n0 + b.goff[i]));
+  a.rowp.reserve(a.rowp.size() + b.lab.size());
+  for (size_t i = 1; i < b.rowp.size(); ++i) a.rowp.push_back(uint32_t(e0 + b.rowp[i]));
+  a.col.reserve(e0 + b.col.size());
+  for (uint32_t c : b.col) a.col.push_back(uint32_t(n0 + c));
+  a.lab.insert(a.lab.end(), b.lab.begin(), b.lab.end());
+  a.elab.insert(a.elab.end(), b.elab.begin(), b.elab.end());
+  a.max_nodes = std::max(a.max_nodes, b.max_nodes);
+  return true;
+}
+
+// Large buffers without a graph limit are split at line boundaries and parsed
+// by several threads; the pieces are concatenated in order, so the result (and
+// the line number of the first malformed line) equals a serial parse.
+int parse_buffer(const char* text, size_t len, uint32_t max_graphs, int skip_invalid, bms_graphs** out) {
+  constexpr size_t kMinPiece = 8u << 20;
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t pieces = std::min<size_t>(std::min<size_t>(hw, 64), len / kMinPiece);
+  if (max_graphs || pieces < 2) return parse_serial(text, len, max_graphs, skip_invalid, 0, out);
+  if (!out) return BMS_EINVAL;
+  *out = nullptr;
+  std::vector<size_t> cut{0};
+  for (size_t k = 1; k < pieces; ++k) {
+    size_t at = std::max(cut.back(), len * k / pieces);
+    const void* nl = at < len ? std::memchr(text + at, '\n', len - at) : nullptr;
+    at = nl ? size_t(static_cast<const char*>(nl) - text) + 1 : len;
+    cut.push_back(at);
+  }
+  cut.push_back(len);
+  const size_t n = cut.size() - 1;
+  std::vector<size_t> lines(n + 1, 0);  // lines before each piece
+  for (size_t k = 0; k < n; ++k) {
+    size_t c = 0;
+    for (const char* q = text + cut[k]; q < text + cut[k + 1]; ++q) c += *q == '\n';
+    lines[k + 1] = lines[k] + c;
+  }
+  std::vector<bms_graphs*> part(n, nullptr);
+  std::vector<int> status(n, BMS_OK);
+  std::vector<std::string> msg(n);
+  std::vector<std::thread> pool;
+  for (size_t k = 0; k < n; ++k)
+    pool.emplace_back([&, k] {
+      status[k] = parse_serial(text + cut[k], cut[k + 1] - cut[k], 0, skip_invalid, lines[k], &part[k]);
+      if (status[k] != BMS_OK) msg[k] = bms::thread_error();
+    });
+  for (auto& t : pool) t.join();
+  int r = BMS_OK;
+  for (size_t k = 0; k < n && r == BMS_OK; ++k)
+    if (status[k] != BMS_OK) {
+      r = status[k];
+      set_thread_error(msg[k]);
+    }
+  bms_graphs* g = r == BMS_OK ? part[0] : nullptr;
+  try {
+    for (size_t k = 1; k < n && r == BMS_OK; ++k)
+      if (!append_batch(*g, *part[k])) {
+        set_thread_error("batch exceeds 32-bit node or entry ids");
+        r = BMS_EUNSUPPORTED;
+      }
+  } catch (const std::bad_alloc&) {
+    set_thread_error("out of host memory while parsing");
+    r = BMS_ENOMEM;
+  }
+  for (size_t k = (r == BMS_OK ? 1 : 0); k < n; ++k) delete part[k];
+  if (r != BMS_OK) return r;
   *out = g;
   return BMS_OK;
 }

@@ -271,6 +271,14 @@ cudaError_t launch_totals(const Counters* ctr_in, uint64_t rec_cap, const unsign
                           const unsigned long long* pair_exp, const uint32_t* pair_flag, int find_first, Counters* ctr,
                           cudaStream_t st);
 // Per-record results into GMCR order (arrays of T entries, zero-filled first).
+// Batch slices: subtract the slice's first entry / node id from its row offsets
+// and column ids.
+cudaError_t launch_rebase(uint32_t* rowp, uint64_t n_rowp, uint32_t entry_base, uint32_t* col, uint64_t n_col,
+                          uint32_t node_base, cudaStream_t st);
+// per_query[q] += matches of the records with query q (find-first: 1 per record with a match).
+cudaError_t launch_query_totals(const PairRec* recs, const Counters* ctr, uint64_t rec_cap,
+                                const unsigned long long* pair_count, int find_first, uint32_t Q,
+                                unsigned long long* per_query, cudaStream_t st);
 cudaError_t launch_scatter(const PairRec* recs, const Counters* ctr, uint64_t rec_cap,
                            const unsigned long long* pair_count, const unsigned long long* pair_exp,
                            const uint32_t* pair_flag, int find_first, uint64_t* counts, uint64_t* exps,

@@ -280,6 +280,41 @@ __global__ void scatter_kernel(const PairRec* recs, const Counters* ctr, uint64_
   }
 }
 
+// Batch slices: row offsets and column ids of a slice arrive with global
+// values and are rebased to the slice.
+__global__ void rebase_kernel(uint32_t* rowp, uint64_t n_rowp, uint32_t entry_base, uint32_t* col, uint64_t n_col,
+                              uint32_t node_base) {
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n_rowp; i += stride) rowp[i] -= entry_base;
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n_col; i += stride) col[i] -= node_base;
+}
+
+// per_query[q] += the matches of every record with query q (find-first: the
+// records with a match); a shared-memory histogram per block when Q is small.
+__global__ void query_totals_kernel(const PairRec* recs, const Counters* ctr, uint64_t rec_cap,
+                                    const unsigned long long* pair_count, int find_first, uint32_t Q,
+                                    unsigned long long* per_query, int use_smem) {
+  extern __shared__ unsigned long long s_hist[];
+  if (use_smem) {
+    for (uint32_t i = threadIdx.x; i < Q; i += blockDim.x) s_hist[i] = 0;
+    __syncthreads();
+  }
+  const uint64_t n = min((unsigned long long)rec_cap, ctr->recs);
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+    const unsigned long long k = pair_count[i];
+    const unsigned long long v = find_first ? (k ? 1ull : 0ull) : k;
+    if (!v) continue;
+    const uint32_t q = recs[i].q;
+    if (use_smem) atomicAdd(&s_hist[q], v);
+    else atomicAdd(&per_query[q], v);
+  }
+  if (use_smem) {
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < Q; i += blockDim.x)
+      if (s_hist[i]) atomicAdd(&per_query[i], s_hist[i]);
+  }
+}
+
 }  // namespace
 
 cudaError_t launch_label_count(const DGraphs& d, unsigned long long* counts, cudaStream_t st) {
@@ -374,6 +409,25 @@ cudaError_t launch_scatter(const PairRec* recs, const Counters* ctr, uint64_t re
   if (rec_cap == 0) return cudaSuccess;
   scatter_kernel<<<grid_for(rec_cap, 256, 4), 256, 0, st>>>(recs, ctr, rec_cap, pair_count, pair_exp, pair_flag,
                                                              find_first, counts, exps, status); note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rebase(uint32_t* rowp, uint64_t n_rowp, uint32_t entry_base, uint32_t* col, uint64_t n_col,
+                          uint32_t node_base, cudaStream_t st) {
+  if (!entry_base && !node_base) return cudaSuccess;
+  rebase_kernel<<<grid_for(n_rowp > n_col ? n_rowp : n_col, 256, 4), 256, 0, st>>>(rowp, n_rowp, entry_base, col, n_col,
+                                                                                   node_base); note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_query_totals(const PairRec* recs, const Counters* ctr, uint64_t rec_cap,
+                                const unsigned long long* pair_count, int find_first, uint32_t Q,
+                                unsigned long long* per_query, cudaStream_t st) {
+  if (rec_cap == 0 || Q == 0) return cudaSuccess;
+  const size_t smem = size_t(Q) * sizeof(unsigned long long);
+  const int use_smem = smem <= (48u << 10);
+  query_totals_kernel<<<grid_for(rec_cap, 256, 4), 256, use_smem ? smem : 0, st>>>(recs, ctr, rec_cap, pair_count,
+                                                                                  find_first, Q, per_query, use_smem); note_launch();
   return cudaGetLastError();
 }
 

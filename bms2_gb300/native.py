@@ -112,6 +112,7 @@ SIGNATURES = [
     ("bms_map", C.c_int, [_vp, _u64p]),
     ("bms_join", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _u64p]),
     ("bms_run", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _u64p]),
+    ("bms_run_batches", C.c_int, [_vp, _vp, C.c_uint32, C.c_int, C.c_int, C.c_int, C.c_int, _u64p, _u64p]),
     ("bms_get_stats", C.c_int, [_vp, C.POINTER(Stats)]),
     ("bms_get_gmcr", C.c_int, [_vp, _u32p, _u32p, C.c_uint64]),
     ("bms_gmcr_offsets_static", C.c_int, [_vp, _vp, C.c_uint64, _vp]),
@@ -360,6 +361,15 @@ class Context:
         t = C.c_uint64()
         self._c(lib().bms_run(self._h, refine_steps, mode, order, semantics, C.byref(t)))
         return t.value
+
+    def run_batches(self, data: "Graphs", batch_graphs: int, refine_steps: int, mode: int = COUNT_ALL,
+                    order: int = ORDER_GMCR, semantics: int = SEM_EXACT) -> tuple[int, np.ndarray]:
+        """The loaded queries against `data` in slices of batch_graphs graphs: (total, per-query matches)."""
+        t = C.c_uint64()
+        per_query = np.zeros(max(self.stats()["n_query_graphs"], 1), dtype=np.uint64)
+        self._c(lib().bms_run_batches(self._h, data._h, batch_graphs, refine_steps, mode, order, semantics,
+                                      C.byref(t), _ptr(per_query, C.c_uint64)))
+        return t.value, per_query[:self.stats()["n_query_graphs"]]
 
     # results
     def stats(self) -> dict:

@@ -194,6 +194,15 @@ int bms_join(bms_ctx* ctx, int mode, int order, int semantics, uint64_t* total);
  * to the staged pipeline's.  The persistent join and the filter run as CUDA
  * kernels on the context's stream. */
 int bms_run(bms_ctx* ctx, int refine_steps, int mode, int order, int semantics, uint64_t* total);
+/* The batch driver (BMS2_batch.cpp:101-305): the loaded queries against a host
+ * batch of data graphs taken batch_graphs graphs at a time (0 = the
+ * reference's 100,000).  Each slice is uploaded as the data side (its global
+ * ids rebased on the device) and run through bms_run; *total receives the sum
+ * over the slices and per_query (optional, [n_query_graphs]) each query's
+ * matches (find-first: its data graphs with a match).  Afterwards the context
+ * holds the last slice as its data side and that slice's per-pair results. */
+int bms_run_batches(bms_ctx* ctx, const bms_graphs* data, uint32_t batch_graphs, int refine_steps, int mode,
+                    int order, int semantics, uint64_t* total, uint64_t* per_query);
 
 /* ------------------------------------------------------------- results */
 typedef struct {

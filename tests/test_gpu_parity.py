@@ -12,7 +12,7 @@ import pytest
 
 import oracle
 from bms2_gb300 import (COUNT_ALL, DATA, FIND_FIRST, ORDER_GMCR, QUERY, SEM_EXACT, SEM_REFERENCE_DFS, BmsError,
-                        Graphs, workloads)
+                        Graphs, shards, workloads)
 from tests.kat_graphs import C, N, O, WILD, chain, line, ring, star
 
 pytestmark = pytest.mark.gpu
@@ -276,6 +276,27 @@ def test_cuda_graph_replay_equals_eager(ctx):
     finally:
         ctx.set_option(OPT_CUDA_GRAPH, 1)
         ctx.set_option(OPT_SPLIT_BUDGET, 1024)
+
+
+@pytest.mark.parametrize("batch", [1, 37, 500, 0])
+def test_batched_run_equals_one_run(ctx, batch):
+    # the data side in slices of `batch` graphs (0: the reference's 100,000,
+    # i.e. one slice): the total and every query's matches equal the oracle
+    # over the whole batch, in count-all and find-first modes
+    d = Graphs.synth_molecules(240, 51, 0, 0, 0, 6, 100, 1, 4)
+    q = Graphs.synth_queries(d, 12, 52, 3, 10)
+    for mode in (COUNT_ALL, FIND_FIRST):
+        want = oracle.run_pipeline(q, d, 2, find_first=mode == FIND_FIRST)
+        dense = want.pair_counts_dense(q.n_graphs)
+        ctx.load(QUERY, q)
+        total, per_query = ctx.run_batches(d, batch, 2, mode, ORDER_GMCR, SEM_EXACT)
+        assert total == want.total
+        assert np.array_equal(per_query, dense.sum(axis=1).astype(np.uint64))
+    # the context keeps the last slice: its pairs equal a run over that slice
+    last = d.n_graphs - (d.n_graphs % batch or batch) if batch else 0
+    tail = Graphs.from_csr(**shards.take_graphs(d.arrays(), np.arange(last, d.n_graphs)))
+    assert ctx.stats()["n_data_graphs"] == tail.n_graphs
+    assert np.array_equal(ctx.pair_counts(), oracle.run_pipeline(q, tail, 2, find_first=True).counts)
 
 
 def test_many_entries_graph_reads_rows_from_global_memory(ctx):

@@ -83,6 +83,35 @@ def test_write_then_parse_round_trip(tmp_path):
         assert ra == rb
 
 
+def test_parallel_parse_equals_serial_parse(tmp_path):
+    # buffers above 16 MiB are split at line boundaries across threads; the
+    # pieces must concatenate to exactly the serial parse (max_graphs forces
+    # the serial path), and the first malformed line keeps its number
+    d = Graphs.synth_molecules(70_000, 17, 0, 0, 0, 10, 40, 1, 4)
+    path = tmp_path / "big.txt"
+    d.write_file(path)
+    text = path.read_bytes()
+    assert len(text) > (17 << 20)
+    par = Graphs.parse_file(path).arrays()
+    ser = Graphs.parse_file(path, max_graphs=d.n_graphs).arrays()
+    ref = d.arrays()
+    for k in ref:
+        assert np.array_equal(par[k], ser[k]), k
+        assert np.array_equal(par[k], ref[k]), k
+    lines = text.split(b"\n")
+    bad = len(lines) - 100
+    lines[bad] = b"n#2 l#1 garbage"
+    path.write_bytes(b"\n".join(lines))
+    msgs = []
+    for mg in (0, d.n_graphs + 1):
+        with pytest.raises(BmsError) as e:
+            Graphs.parse_file(path, max_graphs=mg)
+        msgs.append(str(e.value))
+    assert msgs[0] == msgs[1] and f"line {bad + 1}:" in msgs[0]
+    skipped = Graphs.parse_file(path, skip_invalid=True)
+    assert skipped.n_graphs == d.n_graphs - 1
+
+
 def test_parse_file_missing_is_eio(tmp_path):
     with pytest.raises(BmsError) as e:
         Graphs.parse_file(tmp_path / "nope.txt")

@@ -737,6 +737,48 @@ int bms_run(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total) {
   }
 }
 
+static void release_graph_pins(bms_graphs* g) {
+  for (void* p : g->pinned) cudaHostUnregister(p);
+  g->pinned.clear();
+  g->release_pins = nullptr;
+}
+
+int bms_graphs_pin(bms_graphs* g) {
+  if (!g) {
+    set_thread_error("graphs is null");
+    return BMS_EINVAL;
+  }
+  if (!g->pinned.empty()) return BMS_OK;
+  g->release_pins = release_graph_pins;
+  auto reg = [&](void* p, size_t bytes) -> cudaError_t {
+    if (!bytes) return cudaSuccess;
+    const cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterDefault);
+    if (e == cudaSuccess) g->pinned.push_back(p);
+    return e;
+  };
+  cudaError_t e = reg(g->goff.data(), g->goff.size() * sizeof(uint32_t));
+  if (e == cudaSuccess) e = reg(g->rowp.data(), g->rowp.size() * sizeof(uint32_t));
+  if (e == cudaSuccess) e = reg(g->col.data(), g->col.size() * sizeof(uint32_t));
+  if (e == cudaSuccess) e = reg(g->lab.data(), g->lab.size());
+  if (e == cudaSuccess) e = reg(g->elab.data(), g->elab.size());
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    release_graph_pins(g);
+    set_thread_error(std::string("cudaHostRegister: ") + cudaGetErrorString(e));
+    return BMS_ECUDA;
+  }
+  return BMS_OK;
+}
+
+int bms_graphs_unpin(bms_graphs* g) {
+  if (!g) {
+    set_thread_error("graphs is null");
+    return BMS_EINVAL;
+  }
+  release_graph_pins(g);
+  return BMS_OK;
+}
+
 int bms_run_batches(bms_ctx* c, const bms_graphs* data, uint32_t batch_graphs, int R, int mode, int order, int sem,
                     uint64_t* total, uint64_t* per_query) {
   GUARD(c);
@@ -751,6 +793,7 @@ int bms_run_batches(bms_ctx* c, const bms_graphs* data, uint32_t batch_graphs, i
     }
     uint64_t sum = 0;
     int incomplete = 0;
+    bms_stats acc{};
     uint32_t g0 = 0;
     do {
       const uint32_t g1 = std::min<uint64_t>(G, uint64_t(g0) + batch_graphs);
@@ -772,6 +815,16 @@ int bms_run_batches(bms_ctx* c, const bms_graphs* data, uint32_t batch_graphs, i
       if (r == BMS_EINCOMPLETE) incomplete = 1;
       else if (r) return r;
       sum += t;
+      acc.total_matches += c->stats.total_matches;
+      acc.expansions += c->stats.expansions;
+      acc.n_incomplete += c->stats.n_incomplete;
+      acc.kernel_launches += c->stats.kernel_launches;
+      acc.ms_signatures += c->stats.ms_signatures;
+      acc.ms_filter += c->stats.ms_filter;
+      acc.ms_map += c->stats.ms_map;
+      acc.ms_order += c->stats.ms_order;
+      acc.ms_join += c->stats.ms_join;
+      acc.ms_total += c->stats.ms_total;
       if (per_query)
         CK(launch_query_totals(c->recs.as<PairRec>(), c->ctr.as<Counters>(), c->rec_cap,
                                c->pair_count.as<unsigned long long>(), mode == BMS_FIND_FIRST, Q,
@@ -782,6 +835,18 @@ int bms_run_batches(bms_ctx* c, const bms_graphs* data, uint32_t batch_graphs, i
       CK(cudaMemcpyAsync(per_query, c->per_query.p, sizeof(uint64_t) * Q, cudaMemcpyDeviceToHost, c->st));
       CK(cudaStreamSynchronize(c->st));
     }
+    // stage times and counters over all slices (graph, node and valid-pair
+    // counts stay the last slice's: they size its per-pair results)
+    c->stats.total_matches = acc.total_matches;
+    c->stats.expansions = acc.expansions;
+    c->stats.n_incomplete = acc.n_incomplete;
+    c->stats.kernel_launches = acc.kernel_launches;
+    c->stats.ms_signatures = acc.ms_signatures;
+    c->stats.ms_filter = acc.ms_filter;
+    c->stats.ms_map = acc.ms_map;
+    c->stats.ms_order = acc.ms_order;
+    c->stats.ms_join = acc.ms_join;
+    c->stats.ms_total = acc.ms_total;
     if (total) *total = sum;
     return incomplete ? fail(c, BMS_EINCOMPLETE, "some pairs hit the expansion budget") : BMS_OK;
   } catch (...) {

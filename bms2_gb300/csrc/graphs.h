@@ -14,7 +14,16 @@ struct bms_graphs {
   std::vector<uint8_t> lab;       // [N]
   std::vector<uint8_t> elab;      // [E2]
   uint32_t max_nodes = 0;
+  // page-locked ranges (bms_graphs_pin) and the function that releases them
+  std::vector<void*> pinned;
+  void (*release_pins)(bms_graphs*) = nullptr;
 
+  bms_graphs() = default;
+  bms_graphs(const bms_graphs&) = delete;
+  bms_graphs& operator=(const bms_graphs&) = delete;
+  ~bms_graphs() {
+    if (release_pins) release_pins(this);
+  }
   uint32_t n_graphs() const { return uint32_t(goff.size() - 1); }
   uint64_t n_nodes() const { return lab.size(); }
 };

@@ -96,6 +96,8 @@ SIGNATURES = [
     ("bms_graphs_write_file", C.c_int, [_vp, C.c_char_p]),
     ("bms_graphs_filter_size", C.c_int, [_vp, C.c_uint32, C.c_uint32, C.POINTER(_vp)]),
     ("bms_graphs_free", None, [_vp]),
+    ("bms_graphs_pin", C.c_int, [_vp]),
+    ("bms_graphs_unpin", C.c_int, [_vp]),
     ("bms_synth_molecules", C.c_int, [C.POINTER(MolParams), C.c_uint64, C.POINTER(_vp)]),
     ("bms_synth_queries", C.c_int, [C.POINTER(QueryParams), _vp, C.c_uint64, C.POINTER(_vp)]),
     ("bms_create", C.c_int, [C.c_int, C.POINTER(_vp)]),
@@ -259,6 +261,13 @@ class Graphs:
     @property
     def max_nodes(self) -> int:
         return self.view().max_nodes
+
+    def pin(self) -> None:
+        """Page-lock the batch for asynchronous uploads (undone when freed)."""
+        _check(lib().bms_graphs_pin(self._h))
+
+    def unpin(self) -> None:
+        _check(lib().bms_graphs_unpin(self._h))
 
     def write_file(self, path) -> None:
         _check(lib().bms_graphs_write_file(self._h, str(path).encode()))

@@ -107,6 +107,12 @@ int bms_graphs_write_file(const bms_graphs* g, const char* path);
  * BMS2.cpp:27-34). */
 int bms_graphs_filter_size(const bms_graphs* g, uint32_t min_nodes, uint32_t max_nodes, bms_graphs** out);
 void bms_graphs_free(bms_graphs* g);
+/* Page-lock a host batch (no reference counterpart) so that its uploads, and
+ * every slice bms_run_batches takes from it, copy by asynchronous DMA instead
+ * of through staging buffers.  Undone by bms_graphs_unpin or bms_graphs_free.
+ * Pinning a pinned batch does nothing. */
+int bms_graphs_pin(bms_graphs* g);
+int bms_graphs_unpin(bms_graphs* g);
 
 /* ------------------------------------------- seeded synthetic molecular data */
 /* Not part of the reference (its datasets are converted from SMARTS with rdkit,
@@ -200,7 +206,9 @@ int bms_run(bms_ctx* ctx, int refine_steps, int mode, int order, int semantics, 
  * ids rebased on the device) and run through bms_run; *total receives the sum
  * over the slices and per_query (optional, [n_query_graphs]) each query's
  * matches (find-first: its data graphs with a match).  Afterwards the context
- * holds the last slice as its data side and that slice's per-pair results. */
+ * holds the last slice as its data side and that slice's per-pair results;
+ * bms_get_stats then reports stage times, launches, matches and expansions
+ * summed over the slices (graph, node and valid-pair counts: the last slice). */
 int bms_run_batches(bms_ctx* ctx, const bms_graphs* data, uint32_t batch_graphs, int refine_steps, int mode,
                     int order, int semantics, uint64_t* total, uint64_t* per_query);
 

@@ -299,6 +299,20 @@ def test_batched_run_equals_one_run(ctx, batch):
     assert np.array_equal(ctx.pair_counts(), oracle.run_pipeline(q, tail, 2, find_first=True).counts)
 
 
+def test_pinned_batch_gives_the_same_results(ctx):
+    d = Graphs.synth_molecules(300, 61, 0, 0, 0, 6, 80, 1, 4)
+    q = Graphs.synth_queries(d, 10, 62, 3, 9)
+    ctx.load(QUERY, q)
+    plain = ctx.run_batches(d, 64, 2)
+    d.pin()
+    d.pin()  # pinning twice is a no-op
+    pinned = ctx.run_batches(d, 64, 2)
+    d.unpin()
+    assert plain[0] == pinned[0] and np.array_equal(plain[1], pinned[1])
+    d.pin()  # freed while pinned: the ranges are released with the batch
+    del d
+
+
 def test_many_entries_graph_reads_rows_from_global_memory(ctx):
     # a 127-leaf star with every edge listed 5 times: 1270 CSR entries (more
     # than the 1024 staged in shared memory), repeated entries, 128 nodes

@@ -77,8 +77,16 @@ int check_side_errors(bms_ctx* c, const char* side, uint32_t e) {
 // Upload a batch.  With `slice` the view is a window of a larger batch: its
 // offsets and column ids are global, graph_offsets[0] and row_offsets[0] give
 // the window's first node and entry, and the ids are rebased on the device.
+// Drop the buffers of a side that are views of the resident batch.
+void release_views(Side& s) {
+  for (DevBuf* b : {&s.goff, &s.rowp, &s.col, &s.lab, &s.elab, &s.frec, &s.adj, &s.adjin, &s.ghist, &s.glabset,
+                    &s.maxin, &s.size_order})
+    if (!b->owned) b->release();
+}
+
 int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const char* name, bool slice = false) {
   if (v.n_graphs && !v.graph_offsets) return fail(c, BMS_EINVAL, "graph_offsets is null");
+  release_views(s);
   const uint32_t G = v.n_graphs;
   const uint32_t node_base = slice && G ? v.graph_offsets[0] : 0;
   if (G && v.graph_offsets[0] != node_base) return fail(c, BMS_EINVAL, "graph_offsets[0] must be 0");
@@ -734,6 +742,112 @@ int bms_run(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total) {
     return run_fused(c, R, mode, order, sem, total, log, 0);
   } catch (...) {
     return fail(c, BMS_ENOMEM, "host exception in bms_run");
+  }
+}
+
+int bms_load_resident(bms_ctx* c, const bms_graphs* data) {
+  GUARD(c);
+  if (!data) return fail(c, BMS_EINVAL, "data is null");
+  invalidate_downstream(c);
+  release_views(c->d);  // views of the previous resident batch
+  c->d.loaded = false;
+  bms_graphs_view v;
+  bms_graphs_view_of(data, &v);
+  return upload(c, c->dres, v, kMaxDataNodes, "data");
+}
+
+namespace {
+// The data side becomes a view of resident graphs [g0, g1): graph offsets from
+// g0 on (global node ids), every node- and entry-indexed buffer shared, the
+// per-graph arrays from g0 on.  Nothing is copied.
+void view_window(bms_ctx* c, uint32_t g0, uint32_t g1) {
+  Side& r = c->dres;
+  Side& d = c->d;
+  d.G = g1 - g0;
+  d.N = r.N;
+  d.E = r.E;
+  d.max_nodes = r.max_nodes;
+  d.h_goff.assign(r.h_goff.begin() + g0, r.h_goff.begin() + g1 + 1);
+  d.goff.alias(r.goff.as<uint32_t>() + g0, sizeof(uint32_t) * (d.G + 1));
+  d.rowp.alias(r.rowp.p, r.rowp.bytes);
+  d.col.alias(r.col.p, r.col.bytes);
+  d.lab.alias(r.lab.p, r.lab.bytes);
+  d.elab.alias(r.elab.p, r.elab.bytes);
+  d.frec.alias(r.frec.p, r.frec.bytes);
+  d.adj.alias(r.adj.p, r.adj.bytes);
+  d.adjin.alias(r.adjin.p, r.adjin.bytes);
+  d.ghist.alias(r.ghist.as<uint64_t>() + g0, sizeof(uint64_t) * (d.G ? d.G : 1));
+  d.glabset.alias(r.glabset.as<uint32_t>() + g0, sizeof(uint32_t) * (d.G ? d.G : 1));
+  d.maxin.alias(r.maxin.p, r.maxin.bytes);
+  d.sig_steps = -1;
+  d.asymmetric = false;
+  d.labels_lt16 = 0;
+  d.loaded = true;
+  ++c->load_gen;
+}
+}  // namespace
+
+int bms_run_resident(bms_ctx* c, uint32_t window_graphs, int R, int mode, int order, int sem, uint64_t* total,
+                     uint64_t* per_query) {
+  GUARD(c);
+  if (!c->dres.loaded) return fail(c, BMS_ESTATE, "load a resident data batch first");
+  if (!c->q.loaded) return fail(c, BMS_ESTATE, "load the query graphs first");
+  if (window_graphs == 0) window_graphs = 100000;
+  try {
+    const uint32_t G = c->dres.G, Q = c->q.G;
+    if (per_query) {
+      CK(c->per_query.ensure(sizeof(unsigned long long) * (Q ? Q : 1)));
+      CK(cudaMemsetAsync(c->per_query.p, 0, sizeof(unsigned long long) * (Q ? Q : 1), c->st));
+    }
+    uint64_t sum = 0;
+    int incomplete = 0;
+    bms_stats acc{};
+    uint32_t g0 = 0;
+    do {
+      const uint32_t g1 = std::min<uint64_t>(G, uint64_t(g0) + window_graphs);
+      invalidate_downstream(c);
+      view_window(c, g0, g1);
+      int r = build_classes(c);
+      if (r) return r;
+      uint64_t t = 0;
+      r = run_fused(c, R, mode, order, sem, &t, false, 0);
+      if (r == BMS_EINCOMPLETE) incomplete = 1;
+      else if (r) return r;
+      sum += t;
+      acc.total_matches += c->stats.total_matches;
+      acc.expansions += c->stats.expansions;
+      acc.n_incomplete += c->stats.n_incomplete;
+      acc.kernel_launches += c->stats.kernel_launches;
+      acc.ms_signatures += c->stats.ms_signatures;
+      acc.ms_filter += c->stats.ms_filter;
+      acc.ms_map += c->stats.ms_map;
+      acc.ms_order += c->stats.ms_order;
+      acc.ms_join += c->stats.ms_join;
+      acc.ms_total += c->stats.ms_total;
+      if (per_query)
+        CK(launch_query_totals(c->recs.as<PairRec>(), c->ctr.as<Counters>(), c->rec_cap,
+                               c->pair_count.as<unsigned long long>(), mode == BMS_FIND_FIRST, Q,
+                               c->per_query.as<unsigned long long>(), c->st));
+      g0 = g1;
+    } while (g0 < G);
+    if (per_query && Q) {
+      CK(cudaMemcpyAsync(per_query, c->per_query.p, sizeof(uint64_t) * Q, cudaMemcpyDeviceToHost, c->st));
+      CK(cudaStreamSynchronize(c->st));
+    }
+    c->stats.total_matches = acc.total_matches;
+    c->stats.expansions = acc.expansions;
+    c->stats.n_incomplete = acc.n_incomplete;
+    c->stats.kernel_launches = acc.kernel_launches;
+    c->stats.ms_signatures = acc.ms_signatures;
+    c->stats.ms_filter = acc.ms_filter;
+    c->stats.ms_map = acc.ms_map;
+    c->stats.ms_order = acc.ms_order;
+    c->stats.ms_join = acc.ms_join;
+    c->stats.ms_total = acc.ms_total;
+    if (total) *total = sum;
+    return incomplete ? fail(c, BMS_EINCOMPLETE, "some pairs hit the expansion budget") : BMS_OK;
+  } catch (...) {
+    return fail(c, BMS_ENOMEM, "host exception in bms_run_resident");
   }
 }
 

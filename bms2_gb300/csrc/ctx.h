@@ -19,20 +19,28 @@ extern std::atomic<unsigned long long> g_alloc_epoch;
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  bool owned = true;  // false: a view into another buffer (never freed here)
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() { release(); }
   void release() {
-    if (p) {
-      cudaFree(p);
-      ++g_alloc_epoch;
-    }
+    if (p && owned) cudaFree(p);
+    if (p) ++g_alloc_epoch;
     p = nullptr;
     bytes = 0;
+    owned = true;
+  }
+  // Make this buffer a view of `bytes` bytes at `q` (owned elsewhere).
+  void alias(void* q, size_t b) {
+    release();
+    p = q;
+    bytes = b;
+    owned = false;
+    ++g_alloc_epoch;
   }
   cudaError_t ensure(size_t b) {
-    if (b <= bytes && p) return cudaSuccess;
+    if (b <= bytes && p) return cudaSuccess;  // an owned buffer or a view that is large enough
     release();
     if (b == 0) b = 16;
     cudaError_t e = cudaMalloc(&p, b);
@@ -108,6 +116,7 @@ struct bms_ctx {
   // records and join
   DevBuf recs, arena, tasks, pair_count, pair_exp, pair_flag;
   DevBuf sub[2];  // join subtrees, ping-pong between rounds
+  Side dres;         // resident data batch (bms_load_resident); the data side views windows of it
   DevBuf per_query;  // bms_run_batches: per-query totals
   uint64_t sub_cap = 0;
   uint64_t sub_cap_opt = 0;  // BMS_OPT_SUBTREE_CAP (0: automatic)

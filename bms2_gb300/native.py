@@ -115,6 +115,8 @@ SIGNATURES = [
     ("bms_join", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _u64p]),
     ("bms_run", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _u64p]),
     ("bms_run_batches", C.c_int, [_vp, _vp, C.c_uint32, C.c_int, C.c_int, C.c_int, C.c_int, _u64p, _u64p]),
+    ("bms_load_resident", C.c_int, [_vp, _vp]),
+    ("bms_run_resident", C.c_int, [_vp, C.c_uint32, C.c_int, C.c_int, C.c_int, C.c_int, _u64p, _u64p]),
     ("bms_get_stats", C.c_int, [_vp, C.POINTER(Stats)]),
     ("bms_get_gmcr", C.c_int, [_vp, _u32p, _u32p, C.c_uint64]),
     ("bms_gmcr_offsets_static", C.c_int, [_vp, _vp, C.c_uint64, _vp]),
@@ -370,6 +372,20 @@ class Context:
         t = C.c_uint64()
         self._c(lib().bms_run(self._h, refine_steps, mode, order, semantics, C.byref(t)))
         return t.value
+
+    def load_resident(self, data: "Graphs") -> None:
+        """Upload a data batch once and keep it in HBM for run_resident."""
+        self._c(lib().bms_load_resident(self._h, data._h))
+
+    def run_resident(self, window_graphs: int, refine_steps: int, mode: int = COUNT_ALL, order: int = ORDER_GMCR,
+                     semantics: int = SEM_EXACT) -> tuple[int, np.ndarray]:
+        """The loaded queries over the resident data in windows: (total, per-query matches)."""
+        t = C.c_uint64()
+        nq = self.stats()["n_query_graphs"]
+        per_query = np.zeros(max(nq, 1), dtype=np.uint64)
+        self._c(lib().bms_run_resident(self._h, window_graphs, refine_steps, mode, order, semantics, C.byref(t),
+                                       _ptr(per_query, C.c_uint64)))
+        return t.value, per_query[:nq]
 
     def run_batches(self, data: "Graphs", batch_graphs: int, refine_steps: int, mode: int = COUNT_ALL,
                     order: int = ORDER_GMCR, semantics: int = SEM_EXACT) -> tuple[int, np.ndarray]:

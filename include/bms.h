@@ -211,6 +211,16 @@ int bms_run(bms_ctx* ctx, int refine_steps, int mode, int order, int semantics, 
  * summed over the slices (graph, node and valid-pair counts: the last slice). */
 int bms_run_batches(bms_ctx* ctx, const bms_graphs* data, uint32_t batch_graphs, int refine_steps, int mode,
                     int order, int semantics, uint64_t* total, uint64_t* per_query);
+/* Device-resident data (no reference counterpart; its batch driver re-reads
+ * the file each time): bms_load_resident uploads a data batch once and keeps
+ * it in HBM; bms_run_resident runs the loaded queries over it in windows of
+ * window_graphs graphs (0 = 100,000), each window a view of the resident
+ * buffers (nothing copied), with the totals, per-query matches and statistics
+ * of bms_run_batches.  Afterwards the data side is the last window.  A later
+ * bms_load_graphs / bms_load_csr of the data side replaces the views. */
+int bms_load_resident(bms_ctx* ctx, const bms_graphs* data);
+int bms_run_resident(bms_ctx* ctx, uint32_t window_graphs, int refine_steps, int mode, int order, int semantics,
+                     uint64_t* total, uint64_t* per_query);
 
 /* ------------------------------------------------------------- results */
 typedef struct {

@@ -299,6 +299,29 @@ def test_batched_run_equals_one_run(ctx, batch):
     assert np.array_equal(ctx.pair_counts(), oracle.run_pipeline(q, tail, 2, find_first=True).counts)
 
 
+@pytest.mark.parametrize("window", [1, 53, 0])
+def test_resident_windows_equal_one_run(ctx, window):
+    # the data batch stays in HBM and windows of it are views: totals and
+    # per-query matches equal the oracle, in count-all and find-first modes;
+    # loading an ordinary data side afterwards replaces the views
+    d = Graphs.synth_molecules(230, 71, 0, 0, 0, 6, 110, 1, 4)
+    q = Graphs.synth_queries(d, 11, 72, 3, 10)
+    ctx.load(QUERY, q)
+    ctx.load_resident(d)
+    for mode in (COUNT_ALL, FIND_FIRST):
+        want = oracle.run_pipeline(q, d, 2, find_first=mode == FIND_FIRST)
+        total, per_query = ctx.run_resident(window, 2, mode, ORDER_GMCR, SEM_EXACT)
+        assert total == want.total
+        assert np.array_equal(per_query, want.pair_counts_dense(q.n_graphs).sum(axis=1).astype(np.uint64))
+    res, bat = ctx.run_resident(window, 2), ctx.run_batches(d, window, 2)
+    assert res[0] == bat[0] and np.array_equal(res[1], bat[1])
+    small = Graphs.from_csr(**shards.take_graphs(d.arrays(), np.arange(40)))
+    ctx.load(DATA, small)
+    assert ctx.run(2, COUNT_ALL, ORDER_GMCR, SEM_EXACT) == oracle.run_pipeline(q, small, 2).total
+    total, _ = ctx.run_resident(window, 2)  # the resident batch is still there
+    assert total == oracle.run_pipeline(q, d, 2).total
+
+
 def test_pinned_batch_gives_the_same_results(ctx):
     d = Graphs.synth_molecules(300, 61, 0, 0, 0, 6, 80, 1, 4)
     q = Graphs.synth_queries(d, 10, 62, 3, 9)

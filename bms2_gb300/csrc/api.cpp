@@ -745,6 +745,63 @@ int bms_run(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total) {
   }
 }
 
+int bms_get_embeddings(bms_ctx* c, uint64_t pair, uint8_t* out, uint64_t max_embeddings, uint64_t* n_embeddings) {
+  GUARD(c);
+  if (!n_embeddings || (max_embeddings && !out)) return fail(c, BMS_EINVAL, "out or n_embeddings is null");
+  if (!c->have_results) return fail(c, BMS_ESTATE, "run the pipeline first");
+  if (c->last_sem != BMS_SEM_EXACT || c->last_mode != BMS_COUNT_ALL)
+    return fail(c, BMS_ESTATE, "embeddings are defined for count-all runs with EXACT semantics");
+  if (pair >= c->T) return fail(c, BMS_EINVAL, "pair index beyond the GMCR");
+  // the pair's record (pairs the join skips have none and no embedding)
+  CK(c->embed_tmp.ensure(2 * sizeof(unsigned long long)));
+  unsigned long long* dev = c->embed_tmp.as<unsigned long long>();
+  CK(cudaMemsetAsync(dev, 0xFF, sizeof(unsigned long long), c->st));
+  CK(cudaMemsetAsync(dev + 1, 0, sizeof(unsigned long long), c->st));
+  CK(launch_find_record(c->recs.as<PairRec>(), c->ctr.as<Counters>(), c->rec_cap, uint32_t(pair), dev, c->st));
+  unsigned long long h[2] = {0, 0};
+  CK(cudaMemcpyAsync(h, dev, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  *n_embeddings = 0;
+  if (h[0] == ~0ull) return BMS_OK;
+  const uint64_t rec = h[0];
+  CK(cudaMemcpy(&h[1], c->pair_count.as<unsigned long long>() + rec, sizeof(unsigned long long),
+                cudaMemcpyDeviceToHost));
+  const uint64_t total = h[1];
+  PairRec pr;
+  CK(cudaMemcpy(&pr, c->recs.as<PairRec>() + rec, sizeof(PairRec), cudaMemcpyDeviceToHost));
+  const uint32_t n = c->q.h_goff[pr.q + 1] - c->q.h_goff[pr.q];
+  if (total * n > (uint64_t(1) << 32)) return fail(c, BMS_EUNSUPPORTED, "more than 4 GiB of embeddings for one pair");
+  if (total) {
+    CK(c->embed_out.ensure(total * n));
+    EmbedArgs a{};
+    a.q = c->q.dg();
+    a.d = c->d.dg();
+    a.ds = c->d.ds();
+    a.o = order_of(c);
+    a.recs = c->recs.as<PairRec>();
+    a.rec = rec;
+    a.arena = c->arena.as<uint64_t>();
+    a.out = c->embed_out.as<uint8_t>();
+    a.cap = total;
+    a.count = dev + 1;
+    CK(launch_embed(a, c->st));
+    CK(cudaMemcpyAsync(&h[1], dev + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->st));
+    std::vector<uint8_t> all(total * n);
+    CK(cudaMemcpyAsync(all.data(), c->embed_out.p, total * n, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    if (h[1] != total) return fail(c, BMS_ECUDA, "embedding enumeration disagrees with the pair count");
+    std::vector<uint64_t> idx(total);
+    for (uint64_t k = 0; k < total; ++k) idx[k] = k;
+    std::sort(idx.begin(), idx.end(), [&](uint64_t x, uint64_t y) {
+      return std::memcmp(&all[x * n], &all[y * n], n) < 0;
+    });
+    for (uint64_t k = 0; k < std::min<uint64_t>(total, max_embeddings); ++k)
+      std::memcpy(out + k * n, &all[idx[k] * n], n);
+  }
+  *n_embeddings = total;
+  return BMS_OK;
+}
+
 int bms_load_resident(bms_ctx* c, const bms_graphs* data) {
   GUARD(c);
   if (!data) return fail(c, BMS_EINVAL, "data is null");

@@ -266,6 +266,23 @@ struct ClassLaunch {
 cudaError_t launch_join(const JoinArgs& a, const ClassLaunch cl[3], cudaStream_t st,
                         cudaEvent_t (*timers)[3][2] = nullptr);
 
+// Embeddings of one record (EXACT semantics): every mapping by query vertex.
+struct EmbedArgs {
+  DGraphs q, d;
+  DSigs ds;
+  DOrder o;
+  const PairRec* recs;
+  uint64_t rec;                // the record
+  const uint64_t* arena;
+  uint8_t* out;                // [cap * n]
+  uint64_t cap;
+  unsigned long long* count;   // embeddings found (may exceed cap)
+};
+// out = the index of the record at GMCR position gpos (unchanged if none)
+cudaError_t launch_find_record(const PairRec* recs, const Counters* ctr, uint64_t rec_cap, uint32_t gpos,
+                               unsigned long long* out, cudaStream_t st);
+cudaError_t launch_embed(const EmbedArgs& a, cudaStream_t st);
+
 // Totals over the records (count, expansions, incomplete pairs) into ctr.
 cudaError_t launch_totals(const Counters* ctr_in, uint64_t rec_cap, const unsigned long long* pair_count,
                           const unsigned long long* pair_exp, const uint32_t* pair_flag, int find_first, Counters* ctr,

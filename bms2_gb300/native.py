@@ -120,6 +120,7 @@ SIGNATURES = [
     ("bms_get_stats", C.c_int, [_vp, C.POINTER(Stats)]),
     ("bms_get_gmcr", C.c_int, [_vp, _u32p, _u32p, C.c_uint64]),
     ("bms_gmcr_offsets_static", C.c_int, [_vp, _vp, C.c_uint64, _vp]),
+    ("bms_get_embeddings", C.c_int, [_vp, C.c_uint64, C.POINTER(C.c_uint8), C.c_uint64, _u64p]),
     ("bms_get_pair_counts", C.c_int, [_vp, _u64p, C.c_uint64]),
     ("bms_get_pair_expansions", C.c_int, [_vp, _u64p, C.c_uint64]),
     ("bms_get_pair_status", C.c_int, [_vp, _u8p, C.c_uint64]),
@@ -415,6 +416,19 @@ class Context:
         out = np.zeros(max(n, 1), dtype=np.uint64)
         self._c(lib().bms_get_pair_counts(self._h, _ptr(out, C.c_uint64), len(out)))
         return out[:n]
+
+    def embeddings(self, pair: int, max_embeddings: int | None = None) -> np.ndarray:
+        """Every embedding of GMCR pair `pair` (count-all EXACT run): [k, n] local
+        data ids per query vertex, sorted lexicographically."""
+        found = C.c_uint64()
+        self._c(lib().bms_get_embeddings(self._h, pair, None, 0, C.byref(found)))
+        k = found.value if max_embeddings is None else min(found.value, max_embeddings)
+        off, qidx = self.gmcr()
+        qo = self.query_graph_offsets()
+        n = int(qo[qidx[pair] + 1] - qo[qidx[pair]])
+        out = np.zeros(max(k * n, 1), dtype=np.uint8)
+        self._c(lib().bms_get_embeddings(self._h, pair, out.ctypes.data_as(C.POINTER(C.c_uint8)), k, C.byref(found)))
+        return out[:k * n].reshape(k, n)
 
     def pair_expansions(self) -> np.ndarray:
         n = self.stats()["n_valid_pairs"]

@@ -258,6 +258,13 @@ int bms_get_gmcr(bms_ctx* ctx, uint32_t* data_graph_offsets, uint32_t* query_gra
  * the default stream); the call does not wait for it. */
 int bms_gmcr_offsets_static(const uint32_t* counts, uint32_t* offsets, uint64_t n, void* stream);
 /* Per-pair counts in GMCR order (find-first: 0/1). */
+/* Embeddings of GMCR pair `pair` after a count-all EXACT run (no reference
+ * counterpart: the reference only counts).  Every injective induced embedding
+ * the join counted, as n bytes each (n = the query's size): out[k * n + u] =
+ * local data node mapped to query vertex u; sorted lexicographically, so the
+ * output does not depend on the search order.  Writes min(found,
+ * max_embeddings) embeddings; *n_embeddings receives how many exist. */
+int bms_get_embeddings(bms_ctx* ctx, uint64_t pair, uint8_t* out, uint64_t max_embeddings, uint64_t* n_embeddings);
 int bms_get_pair_counts(bms_ctx* ctx, uint64_t* counts, uint64_t cap);
 /* Per-pair expansion counts in GMCR order. */
 int bms_get_pair_expansions(bms_ctx* ctx, uint64_t* expansions, uint64_t cap);

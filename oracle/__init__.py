@@ -7,4 +7,4 @@ checker.  Parity status: unpinned by the reference itself (it cannot be built
 here and ships no tests or golden vectors); pinned by hand-derived known-answer
 tests and an independent networkx cross-check (tests/golden/).
 """
-from .pipeline import OracleResult, Signatures, load, mlp_grad, run_pipeline, signatures  # noqa: F401
+from .pipeline import OracleResult, Signatures, load, mlp_grad, pair_embeddings, run_pipeline, signatures  # noqa: F401

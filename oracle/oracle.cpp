@@ -15,6 +15,8 @@
 //   - candidate range count / select candidates.hpp:82-158
 //   - GMCR mapping                   gmcr.hpp:35-144
 //   - join                           isomorphism.hpp:268-288, 291-472
+//   - embeddings of one pair         (no reference counterpart; the join's DFS
+//                                     in EXACT semantics, writing each mapping)
 //
 // Parity status: the reference cannot be built in this environment (SYCL
 // compiler and runtime, MPI and a network fetch of cxxopts are required; g++
@@ -536,6 +538,58 @@ int orc_join(uint32_t Qg, const uint32_t* q_goff, const uint32_t* q_rowp, const 
     }
   }
   (void)T;
+  return 0;
+}
+
+// Every injective induced embedding of GMCR pair t (EXACT semantics): the DFS
+// of orc_join in query-index order with the visited bookkeeping fixed, writing
+// each complete mapping as n bytes, out[e * n + u] = local data id of query
+// vertex u.  Writes at most cap embeddings; *found receives how many exist.
+// (The reference never emits embeddings: isomorphism.hpp:291-472 only counts.)
+int orc_pair_embeddings(const uint32_t* q_goff, const uint32_t* q_rowp, const uint32_t* q_col, const uint32_t* d_goff,
+                        const uint32_t* d_rowp, const uint32_t* d_col, uint64_t Dn, const uint32_t* cand,
+                        const uint32_t* offsets, uint32_t Dg, const uint32_t* qidx, uint64_t t, uint8_t* out,
+                        uint64_t cap, uint64_t* found) {
+  const uint64_t W = words_per_row(Dn);
+  uint32_t d = 0;
+  while (d < Dg && offsets[d + 1] <= t) ++d;
+  if (d >= Dg) return -1;
+  const uint32_t start = d_goff[d], end = d_goff[d + 1], m = end - start;
+  const uint32_t q = qidx[t], qoff = q_goff[q], n = q_goff[q + 1] - qoff;
+  std::vector<uint32_t> map(n, kNullNode);
+  std::vector<char> used(m, 0);
+  uint64_t k = 0;
+  // recursive restatement: depth i takes every candidate of query vertex i
+  // that is unused and induced-consistent with depths < i
+  std::vector<std::vector<uint32_t>> cands(n);
+  for (uint32_t i = 0; i < n; ++i)
+    for (uint32_t v = start; v < end; ++v)
+      if ((cand[(qoff + i) * W + (v >> 5)] >> (v & 31u)) & 1u) cands[i].push_back(v);
+  struct Rec {
+    static void go(uint32_t i, uint32_t n, uint32_t qoff, uint32_t start, const uint32_t* q_rowp, const uint32_t* q_col,
+                   const uint32_t* d_rowp, const uint32_t* d_col, const std::vector<std::vector<uint32_t>>& cands,
+                   std::vector<uint32_t>& map, std::vector<char>& used, uint8_t* out, uint64_t cap, uint64_t& k) {
+      if (i == n) {
+        if (k < cap)
+          for (uint32_t u = 0; u < n; ++u) out[k * n + u] = uint8_t(map[u] - start);
+        ++k;
+        return;
+      }
+      for (uint32_t v : cands[i]) {
+        if (used[v - start]) continue;
+        bool ok = true;
+        for (uint32_t j = 0; j < i && ok; ++j)
+          ok = csr_has(q_rowp, q_col, qoff + i, qoff + j) == csr_has(d_rowp, d_col, map[j], v);
+        if (!ok) continue;
+        map[i] = v;
+        used[v - start] = 1;
+        go(i + 1, n, qoff, start, q_rowp, q_col, d_rowp, d_col, cands, map, used, out, cap, k);
+        used[v - start] = 0;
+      }
+    }
+  };
+  Rec::go(0, n, qoff, start, q_rowp, q_col, d_rowp, d_col, cands, map, used, out, cap, k);
+  *found = k;
   return 0;
 }
 

@@ -49,6 +49,9 @@ def load() -> C.CDLL:
         L.orc_join.restype = C.c_int
         L.orc_join.argtypes = [C.c_uint32, _u32p, _u32p, _u32p, C.c_uint32, _u32p, _u32p, _u32p, C.c_uint64, _u32p,
                                _u32p, _u32p, C.c_int, C.c_int, C.c_int, C.c_int, _u64p, _u64p]
+        L.orc_pair_embeddings.restype = C.c_int
+        L.orc_pair_embeddings.argtypes = [_u32p, _u32p, _u32p, _u32p, _u32p, _u32p, C.c_uint64, _u32p, _u32p,
+                                          C.c_uint32, _u32p, C.c_uint64, C.POINTER(C.c_uint8), C.c_uint64, _u64p]
         L.orc_mlp_grad.restype = C.c_float
         L.orc_mlp_grad.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p,
                                    _f32p, _f32p, _f32p, _f32p, _f32p]
@@ -184,3 +187,31 @@ def mlp_grad(params: np.ndarray, x: np.ndarray, y: np.ndarray):
 
 def cpu_threads() -> int:
     return os.cpu_count() or 1
+
+
+def pair_embeddings(query, data, res: "OracleResult", t: int, cap: int = 1 << 20) -> np.ndarray:
+    """Every embedding of GMCR pair t of a run_pipeline result (EXACT semantics,
+    the candidate matrix of its last refine step): [k, n] local data ids per
+    query vertex, sorted lexicographically."""
+    L = load()
+    q, d = _csr(query), _csr(data)
+    qi = int(res.qidx[t])
+    n = int(q["graph_offsets"][qi + 1] - q["graph_offsets"][qi])
+    out = np.zeros(max(cap * n, 1), np.uint8)
+    found = C.c_uint64()
+    Dn = int(d["graph_offsets"][-1])
+    cand = np.ascontiguousarray(res.cand)
+    r = L.orc_pair_embeddings(_p(q["graph_offsets"], C.c_uint32), _p(q["row_offsets"], C.c_uint32),
+                              _p(q["column_indices"], C.c_uint32), _p(d["graph_offsets"], C.c_uint32),
+                              _p(d["row_offsets"], C.c_uint32), _p(d["column_indices"], C.c_uint32), Dn,
+                              _p(cand, C.c_uint32), _p(res.offsets, C.c_uint32), len(d["graph_offsets"]) - 1,
+                              _p(res.qidx, C.c_uint32), t, out.ctypes.data_as(C.POINTER(C.c_uint8)), cap,
+                              C.byref(found))
+    if r != 0:
+        raise ValueError("pair index out of range")
+    k = int(found.value)
+    if k > cap:
+        raise ValueError(f"{k} embeddings exceed cap {cap}")
+    e = out[:k * n].reshape(k, n)
+    return e[np.lexsort(e.T[::-1])] if k else e
+

@@ -80,6 +80,21 @@ def test_learned_order_keeps_counts_bit_exact(ctx, trained):
     assert ctx.run(6, COUNT_ALL, ORDER_LEARNED, SEM_EXACT) == want.total
 
 
+def test_learned_order_keeps_every_embedding(ctx, trained):
+    # the learned order changes how the search walks, not what it finds:
+    # every embedding of every sampled pair equals the plain order's
+    q, d = workloads.make("mol100k", 13, n_data=400, n_queries=30)
+    ctx.load(QUERY, q)
+    ctx.load(DATA, d)
+    ctx.run(6, COUNT_ALL, ORDER_GMCR, SEM_EXACT)
+    counts = ctx.pair_counts().copy()
+    picked = [t for t in range(len(counts)) if 0 < counts[t] <= 2000][:60]
+    plain = [ctx.embeddings(t) for t in picked]
+    ctx.run(6, COUNT_ALL, ORDER_LEARNED, SEM_EXACT)
+    for t, e in zip(picked, plain):
+        assert np.array_equal(ctx.embeddings(t), e), t
+
+
 def test_learned_orders_are_permutations(ctx, trained):
     q, d = workloads.make("mol1k", 13, n_data=300, n_queries=30)
     ctx.load(QUERY, q)

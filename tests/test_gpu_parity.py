@@ -322,6 +322,31 @@ def test_resident_windows_equal_one_run(ctx, window):
     assert total == oracle.run_pipeline(q, d, 2).total
 
 
+def test_embeddings_equal_the_oracle(ctx):
+    # every embedding of a pair (not only the count), sorted, against the
+    # oracle's enumeration (itself pinned against networkx); graphs of up to
+    # 110 nodes, queries of up to 10
+    d = Graphs.synth_molecules(90, 81, 0, 0, 0, 6, 110, 1, 4)
+    q = Graphs.synth_queries(d, 10, 82, 3, 10)
+    want = oracle.run_pipeline(q, d, 2)
+    load(ctx, q, d)
+    ctx.run(2, COUNT_ALL, ORDER_GMCR, SEM_EXACT)
+    assert np.array_equal(ctx.pair_counts(), want.counts)
+    picked = [t for t in range(len(want.counts)) if 0 < want.counts[t] <= 3000][:120]
+    assert len(picked) >= 40
+    for t in picked:
+        got = ctx.embeddings(t)
+        assert np.array_equal(got, oracle.pair_embeddings(q, d, want, t)), t
+    first = ctx.embeddings(picked[0], max_embeddings=1)
+    assert np.array_equal(first, ctx.embeddings(picked[0])[:1])
+    zero = [t for t in range(len(want.counts)) if want.counts[t] == 0]
+    if zero:
+        assert ctx.embeddings(zero[0]).shape[0] == 0
+    ctx.run(2, FIND_FIRST, ORDER_GMCR, SEM_EXACT)
+    with pytest.raises(BmsError):
+        ctx.embeddings(picked[0])
+
+
 def test_pinned_batch_gives_the_same_results(ctx):
     d = Graphs.synth_molecules(300, 61, 0, 0, 0, 6, 80, 1, 4)
     q = Graphs.synth_queries(d, 10, 62, 3, 9)

@@ -68,3 +68,36 @@ def test_live_networkx_cross_check():
             gm = iso.GraphMatcher(dd, qq, node_match=lambda a, b: b["l"] == 255 or a["l"] == b["l"])
             want = sum(1 for _ in gm.subgraph_isomorphisms_iter()) if qq.number_of_nodes() > 1 else 0
             assert got[qi, di] == want, (qi, di)
+
+
+def test_oracle_embeddings_match_networkx():
+    # every embedding (not only the count) of every GMCR pair at R = 2, against
+    # networkx's induced label-preserving subgraph isomorphisms
+    nx = pytest.importorskip("networkx")
+    from networkx.algorithms import isomorphism as iso
+
+    q, d = workloads.make("mol1k", 29, n_data=25, n_queries=6)
+    r = oracle.run_pipeline(q, d, 2)
+    qa, da = q.arrays(), d.arrays()
+
+    def graph(a, g):
+        go, ro, ci, nl = a["graph_offsets"], a["row_offsets"], a["column_indices"], a["node_labels"]
+        s, e = int(go[g]), int(go[g + 1])
+        G = nx.Graph()
+        G.add_nodes_from((v - s, {"l": int(nl[v])}) for v in range(s, e))
+        G.add_edges_from((v - s, int(ci[i]) - s) for v in range(s, e) for i in range(int(ro[v]), int(ro[v + 1])))
+        return G
+
+    checked = 0
+    for di in range(d.n_graphs):
+        for t in range(int(r.offsets[di]), int(r.offsets[di + 1])):
+            qi = int(r.qidx[t])
+            got = oracle.pair_embeddings(q, d, r, t)
+            assert len(got) == int(r.counts[t])
+            qq, dd = graph(qa, qi), graph(da, di)
+            gm = iso.GraphMatcher(dd, qq, node_match=lambda a, b: b["l"] == 255 or a["l"] == b["l"])
+            want = sorted(tuple(inv[u] for u in range(qq.number_of_nodes()))
+                          for inv in ({v: k for k, v in m.items()} for m in gm.subgraph_isomorphisms_iter()))
+            assert [tuple(int(x) for x in row) for row in got] == want, (qi, di)
+            checked += 1
+    assert checked > 20

@@ -52,6 +52,11 @@ namespace {
 
 constexpr int kPlanes = 3;  // counted test: counts 0..7
 
+// Run modes a join kernel is compiled for (their per-step checks vanish):
+// count-all, find-first, count-all with per-vertex expansion logging.
+constexpr int kModeCount = 0, kModeFind = 1, kModeLog = 2;
+
+
 __device__ __forceinline__ uint32_t wpop(uint32_t x) { return uint32_t(__popc(x)); }
 __device__ __forceinline__ uint32_t wpop(uint64_t x) { return uint32_t(__popcll(x)); }
 __device__ __forceinline__ uint32_t wlow(uint32_t x) { return uint32_t(__ffs(int(x)) - 1); }
@@ -237,12 +242,13 @@ struct Stack {
   uint32_t expd[kMaxQueryNodes];     // per-depth expansions (logging)
 };
 
-template <typename T, int W>
+template <typename T, int W, int kMode>
 __device__ __forceinline__ void finish(Lane<T, W>& L, const JoinArgs& a, const uint32_t* expd) {
+  constexpr bool kFindFirst = kMode == kModeFind, kLogVertices = kMode == kModeLog;
   if (L.cnt) atomicAdd(&a.pair_count[L.rec], L.cnt);
   if (L.exps) atomicAdd(&a.pair_exp[L.rec], L.exps);
-  if (a.find_first && L.cnt) atomicOr(&a.pair_flag[L.rec], 1u);
-  if (a.vertex_exp)
+  if (kFindFirst && L.cnt) atomicOr(&a.pair_flag[L.rec], 1u);
+  if (kLogVertices)
     for (uint32_t t = 0; t < L.n; ++t)
       if (expd[t]) atomicAdd(&a.vertex_exp[L.qoff + L.perm[t]], (unsigned long long)expd[t]);
   L.active = false;
@@ -279,25 +285,26 @@ __device__ bool split(Lane<T, W>& L, const JoinArgs& a, const Stack<T, W>& S) {
   return true;
 }
 
-template <typename T, int W>
+template <typename T, int W, int kMode>
 __device__ __forceinline__ bool after_step(Lane<T, W>& L, const JoinArgs& a, const Stack<T, W>& S) {
+  constexpr bool kFindFirst = kMode == kModeFind;
   const uint32_t* expd = S.expd;
   if (a.budget && L.exps > a.budget) {
     atomicOr(&a.pair_flag[L.rec], 2u);
-    finish(L, a, expd);
+    finish<T, W, kMode>(L, a, expd);
     return false;
   }
   if (a.split_budget && L.exps >= a.split_budget && !L.no_split) {
     if (split(L, a, S)) {
-      finish(L, a, expd);
+      finish<T, W, kMode>(L, a, expd);
       return false;
     }
     L.no_split = true;
   }
-  if (a.find_first && ++L.since_check >= 64) {
+  if (kFindFirst && ++L.since_check >= 64) {
     L.since_check = 0;
     if (*(volatile const uint32_t*)&a.pair_flag[L.rec] & 1u) {
-      finish(L, a, expd);
+      finish<T, W, kMode>(L, a, expd);
       return false;
     }
   }
@@ -308,12 +315,13 @@ __device__ __forceinline__ bool after_step(Lane<T, W>& L, const JoinArgs& a, con
 // One assignment: pop exhausted frames, take the next candidate v of depth t,
 // compute depth t+1 with v mapped; count it when it is the leaf level, else
 // push.  Leaf and dead-end steps write no stack state.
-template <typename T, int W>
+template <typename T, int W, int kMode>
 __device__ __forceinline__ void step_counted(Lane<T, W>& L, const JoinArgs& a, Stack<T, W>& S) {
+  constexpr bool kFindFirst = kMode == kModeFind, kLogVertices = kMode == kModeLog;
   int t = L.t;
   while (!bany(L.cur)) {  // frame t exhausted
     if (t == L.base) {
-      finish(L, a, S.expd);
+      finish<T, W, kMode>(L, a, S.expd);
       return;
     }
     --t;
@@ -335,14 +343,14 @@ __device__ __forceinline__ void step_counted(Lane<T, W>& L, const JoinArgs& a, S
   const uint32_t k = uint32_t(__popcll(dm));
   c = k < (1u << kPlanes) ? band(c, peq_added(L.P, row, k)) : z<T, W>();
   L.exps += 1;
-  if (a.vertex_exp) S.expd[t] += 1;
+  if (kLogVertices) S.expd[t] += 1;
   if (j + 1 == L.n) {  // depth j is the leaf level: count it without expanding
     const uint32_t pc = bpop(c);
     L.cnt += pc;
     L.exps += pc;
-    if (a.vertex_exp) S.expd[j] += pc;
-    if (a.find_first && pc) {
-      finish(L, a, S.expd);
+    if (kLogVertices) S.expd[j] += pc;
+    if (kFindFirst && pc) {
+      finish<T, W, kMode>(L, a, S.expd);
       return;
     }
   } else if (bany(c)) {
@@ -354,7 +362,7 @@ __device__ __forceinline__ void step_counted(Lane<T, W>& L, const JoinArgs& a, S
     L.t = int(j);
     L.cur = c;
   }
-  after_step(L, a, S);
+  after_step<T, W, kMode>(L, a, S);
 }
 
 // ----------------------------------------------------------- in-row test
@@ -377,13 +385,14 @@ __device__ __forceinline__ Bits<T, W> compute_level(const Lane<T, W>& L, uint32_
   return res;
 }
 
-template <typename T, int W>
+template <typename T, int W, int kMode>
 __device__ __forceinline__ void step_inrow(Lane<T, W>& L, const JoinArgs& a, Stack<T, W>& S) {
+  constexpr bool kFindFirst = kMode == kModeFind, kLogVertices = kMode == kModeLog;
   int t = L.t;
   while (!bany(L.cur)) {  // frame t exhausted
     if (a.literal && ((L.mpset >> t) & 1ull)) L.vis = bandn(L.vis, bbit<T, W>(S.mp[t]));
     if (t == L.base) {
-      finish(L, a, S.expd);
+      finish<T, W, kMode>(L, a, S.expd);
       return;
     }
     --t;
@@ -402,7 +411,7 @@ __device__ __forceinline__ void step_inrow(Lane<T, W>& L, const JoinArgs& a, Sta
   S.f[t] = uint8_t(v);
   L.mapped = bor(L.mapped, bbit<T, W>(v));
   L.exps += 1;
-  if (a.vertex_exp) S.expd[t] += 1;
+  if (kLogVertices) S.expd[t] += 1;
   const Bits<T, W> nf = compute_level(L, uint32_t(t) + 1, S.f, a.literal);
   if (uint32_t(t) + 2 == L.n) {
     // depth n-1 is the leaf level: count it without expanding
@@ -412,14 +421,14 @@ __device__ __forceinline__ void step_inrow(Lane<T, W>& L, const JoinArgs& a, Sta
     const uint32_t pc = bpop(acc);
     L.cnt += pc;
     L.exps += pc;
-    if (a.vertex_exp) S.expd[last] += pc;
+    if (kLogVertices) S.expd[last] += pc;
     if (a.literal && pc) {
       L.vis = bor(L.vis, acc);
       S.mp[last] = uint8_t(bhigh(acc));
       L.mpset |= uint64_t(1) << last;
     }
-    if (a.find_first && pc) {
-      finish(L, a, S.expd);
+    if (kFindFirst && pc) {
+      finish<T, W, kMode>(L, a, S.expd);
       return;
     }
     if (a.literal && ((L.mpset >> last) & 1ull)) L.vis = bandn(L.vis, bbit<T, W>(S.mp[last]));  // frame n-1 exhausted
@@ -429,14 +438,15 @@ __device__ __forceinline__ void step_inrow(Lane<T, W>& L, const JoinArgs& a, Sta
     L.t = t + 1;
     L.cur = nf;
   }
-  after_step(L, a, S);
+  after_step<T, W, kMode>(L, a, S);
 }
 
 // Record class K: 2 = data graphs of 65..128 nodes (two 64-bit words), 1 =
 // 33..64 nodes (one 64-bit word), 0 = up to 32 nodes (one 32-bit word).
 // kCounted selects the counted test (EXACT, in-degrees <= 7) or the in-row test.
-template <int K, bool kCounted>
+template <int K, bool kCounted, int kMode>
 __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
+  constexpr bool kFindFirst = kMode == kModeFind, kLogVertices = kMode == kModeLog;
   using T = typename std::conditional<K == 0, uint32_t, uint64_t>::type;
   constexpr int W = K == 2 ? 2 : 1;
   const bool counted_applies = !a.literal && *a.ds.maxin < (1u << kPlanes);
@@ -557,9 +567,9 @@ __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
             }
           }
           L.cur = roots;
-          if (a.vertex_exp)
+          if (kLogVertices)
             for (uint32_t t = 0; t < L.n; ++t) S.expd[t] = 0;
-          if (a.find_first && (*(volatile const uint32_t*)&a.pair_flag[L.rec] & 1u)) finish(L, a, S.expd);
+          if (kFindFirst && (*(volatile const uint32_t*)&a.pair_flag[L.rec] & 1u)) finish<T, W, kMode>(L, a, S.expd);
         }
       }
       qbase += took;
@@ -569,8 +579,8 @@ __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
     if (__all_sync(0xffffffffu, !L.active && L.done_fetching)) break;
     for (int s = 0; s < a.steps; ++s) {
       if (L.active) {
-        if constexpr (kCounted) step_counted(L, a, S);
-        else step_inrow(L, a, S);
+        if constexpr (kCounted) step_counted<T, W, kMode>(L, a, S);
+        else step_inrow<T, W, kMode>(L, a, S);
       }
       const uint32_t idle = __ballot_sync(0xffffffffu, !L.active && !L.done_fetching);
       if (__popc(idle) >= 4 || (idle && !__any_sync(0xffffffffu, L.active))) break;
@@ -578,15 +588,22 @@ __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
   }
 }
 
-template <int K>
-cudaError_t launch_class(const JoinArgs& a, int blocks, int threads, cudaStream_t st) {
+template <int K, int kMode>
+cudaError_t launch_mode(const JoinArgs& a, int blocks, int threads, cudaStream_t st) {
   if (!a.literal) {
-    join_kernel<K, true><<<blocks, threads, 0, st>>>(a); note_launch();
+    join_kernel<K, true, kMode><<<blocks, threads, 0, st>>>(a); note_launch();
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
-  join_kernel<K, false><<<blocks, threads, 0, st>>>(a); note_launch();
+  join_kernel<K, false, kMode><<<blocks, threads, 0, st>>>(a); note_launch();
   return cudaGetLastError();
+}
+
+template <int K>
+cudaError_t launch_class(const JoinArgs& a, int blocks, int threads, cudaStream_t st) {
+  if (a.vertex_exp) return launch_mode<K, kModeLog>(a, blocks, threads, st);
+  if (a.find_first) return launch_mode<K, kModeFind>(a, blocks, threads, st);
+  return launch_mode<K, kModeCount>(a, blocks, threads, st);
 }
 
 }  // namespace

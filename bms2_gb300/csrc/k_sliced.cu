@@ -206,6 +206,20 @@ __device__ __forceinline__ bool eval_node(const SlicedArgs& a, const GraphCtx<W>
   return many(row);
 }
 
+// 32 x 32 bit transpose across the warp: lane r holds row r (bit c = A[r][c]);
+// afterwards lane c holds column c (bit r = A[r][c]).  Five exchange stages
+// swap the off-diagonal blocks of size 16, 8, 4, 2, 1.
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x, uint32_t lane) {
+  const uint32_t keep[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const uint32_t j = 16u >> k;
+    const uint32_t y = __shfl_xor_sync(0xffffffffu, x, j);
+    x = (lane & j) ? ((x & ~keep[k]) | ((y >> j) & keep[k])) : ((x & keep[k]) | ((y << j) & ~keep[k]));
+  }
+  return x;
+}
+
 // Chunk ch (32 nodes) of the mask of clause id, if some query uses it; the
 // halves from zero_from on (past the graph's last node) are cleared.
 template <int W>
@@ -275,66 +289,58 @@ __global__ void __launch_bounds__(256) sliced_filter_kernel(SlicedArgs a) {
       s_nrec = 0;
     }
     __syncthreads();
-    // The mask table, bit-sliced: a warp takes one clause family and one
-    // 32-node chunk of the graph, lane = node; every clause of the family is
-    // one ballot, and lane i keeps the i-th ballot so the used masks are
-    // stored in parallel.  Families: labels + degrees, cycles, 8 x 32 path
-    // bits, then one per shell step (per packed label: four nibble-plane
-    // ballots, lane c-1 forms the mask of nibbles >= c).
+    // The mask table: a warp takes one clause family and one 32-node chunk of
+    // the graph, lane = node.  Each lane writes its node's 32 clause bits of
+    // the family as one word (one-hot label, degree and cycle thermometers, a
+    // 32-bit slice of the path filter, shell-count thermometers of two labels),
+    // and a 32 x 32 bit transpose across the warp leaves lane i holding the
+    // mask of the family's clause i, so the used masks are stored in parallel.
+    // Families: labels + degrees, cycles, 8 path slices, then per shell step
+    // one per pair of packed labels.
     {
       const uint32_t chunks = (m + 31) >> 5;
-      const uint32_t n_items = 10 + uint32_t(R);
+      const uint32_t shell_items = (a.sp.K + 1) / 2;
+      const uint32_t n_items = 10 + uint32_t(R) * shell_items;
       uint32_t* tab32 = reinterpret_cast<uint32_t*>(s_tab);
       for (uint32_t it = tid >> 5; it < n_items * chunks; it += blockDim.x >> 5) {
         const uint32_t item = it / chunks, ch = it - item * chunks;
         const uint32_t v = ch * 32 + lane;
         const bool in = v < m;
         const uint32_t zero_from = ch + 1 == chunks ? chunks : 2 * W;  // halves past the graph
+        uint32_t row = 0, id = 0;
+        bool used = false;
         if (item < 10) {
-          uint32_t mine = 0;
-          for (uint32_t i = 0; i < 32; ++i) {
-            bool p = false;
-            if (in) {
-              if (item == 0) {
-                p = i < 16 ? uint32_t(s_lab[v]) == i : uint32_t(s_deg[v]) >= i - 15;
-              } else if (item == 1) {
-                p = ((s_cyc[v] >> (16 * (i >> 3))) & 0xFFFFull) >= (i & 7u) + 1;
-              } else {
-                const uint32_t b = (item - 2) * 32 + i;
-                p = (s_path[4 * v + (b >> 6)] >> (b & 63u)) & 1ull;
+          if (in) {
+            if (item == 0) {
+              const uint32_t l = s_lab[v], dg = min(uint32_t(s_deg[v]), 16u);
+              row = (l < 16 ? 1u << l : 0u) | (((1u << dg) - 1u) << 16);
+            } else if (item == 1) {
+              for (int t = 0; t < 4; ++t) {
+                const uint32_t cnt = min(uint32_t((s_cyc[v] >> (16 * t)) & 0xFFFFull), 8u);
+                row |= ((1u << cnt) - 1u) << (8 * t);
               }
+            } else {
+              const uint32_t w = item - 2;
+              row = uint32_t(s_path[4 * v + (w >> 1)] >> (32 * (w & 1u)));
             }
-            const uint32_t bal = __ballot_sync(0xffffffffu, p);
-            if (lane == i) mine = bal;
           }
-          const uint32_t id = item == 0 ? kMLab + lane : (item == 1 ? kMCyc + lane : kMPath + (item - 2) * 32 + lane);
-          put_chunk<W>(tab32, s_used, s_remap, id, ch, mine, zero_from);
+          id = item == 0 ? kMLab + lane : (item == 1 ? kMCyc + lane : kMPath + (item - 2) * 32 + lane);
+          used = (s_used[id >> 5] >> (id & 31u)) & 1u;
         } else {
-          const uint32_t k = item - 10;
-          for (uint32_t j = 0; j < a.sp.K; ++j) {
-            const uint32_t id = kMShell + (k * a.sp.K + j) * 15 + lane;
-            const bool used = lane < 15 && ((s_used[id >> 5] >> (id & 31u)) & 1u);
-            if (!__any_sync(0xffffffffu, used)) continue;
-            const uint32_t nib = in ? uint32_t(s_sh[uint32_t(R) * v + k] >> (4 * a.sp.pos[j])) & 15u : 0u;
-            uint32_t x[4];
-#pragma unroll
-            for (int b = 0; b < 4; ++b) x[b] = __ballot_sync(0xffffffffu, (nib >> b) & 1u);
-            if (used) {
-              const uint32_t c = lane + 1;  // nodes whose nibble >= c
-              uint32_t gt = 0, eq = 0xFFFFFFFFu;
-#pragma unroll
-              for (int b = 3; b >= 0; --b) {
-                if ((c >> b) & 1u) {
-                  eq &= x[b];
-                } else {
-                  gt |= eq & x[b];
-                  eq &= ~x[b];
-                }
-              }
-              put_chunk<W>(tab32, s_used, s_remap, id, ch, gt | eq, zero_from);
-            }
+          const uint32_t k = (item - 10) / shell_items, j0 = 2 * ((item - 10) % shell_items);
+          const uint32_t j = j0 + (lane >> 4), c = lane & 15u;  // lane -> (label j, count c + 1)
+          id = kMShell + (k * a.sp.K + j) * 15 + c;
+          used = c < 15 && j < a.sp.K && ((s_used[id >> 5] >> (id & 31u)) & 1u);
+          if (!__any_sync(0xffffffffu, used)) continue;
+          if (in) {
+            const uint64_t sh = s_sh[uint32_t(R) * v + k];
+            const uint32_t n0 = uint32_t(sh >> (4 * a.sp.pos[j0])) & 15u;
+            const uint32_t n1 = j0 + 1 < a.sp.K ? uint32_t(sh >> (4 * a.sp.pos[j0 + 1])) & 15u : 0u;
+            row = ((1u << n0) - 1u) | (((1u << n1) - 1u) << 16);
           }
         }
+        const uint32_t mask = warp_transpose32(row, lane);
+        if (used) put_chunk<W>(tab32, s_used, s_remap, id, ch, mask, zero_from);
       }
     }
     // screening: label set, more than one node, label multiset (join)

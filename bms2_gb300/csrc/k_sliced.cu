@@ -148,6 +148,22 @@ __global__ void program_fill_kernel(DGraphs q, DSigs qs, ShellPack sp, const uin
   }
 }
 
+// One descriptor per (query, level of its filter order); see desc_vertex.
+__global__ void level_desc_kernel(DGraphs q, const uint8_t* filter_order, const uint8_t* dup, const uint32_t* prog_off,
+                                  const uint8_t* slow, uint2* desc) {
+  const uint64_t total = uint64_t(q.G) * kMaxQueryNodes;
+  for (uint64_t k = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < total; k += uint64_t(gridDim.x) * blockDim.x) {
+    const uint32_t qg = uint32_t(k / kMaxQueryNodes), level = uint32_t(k % kMaxQueryNodes);
+    const uint32_t qoff = q.goff[qg], n = q.goff[qg + 1] - qoff;
+    if (level >= n) continue;
+    const uint32_t ul = filter_order[k];
+    const uint64_t u = uint64_t(qoff) + ul;
+    const uint32_t pb = prog_off[u], pe = prog_off[u + 1];
+    const uint32_t src = dup[uint64_t(qg) * kMaxQueryNodes + ul];
+    desc[k] = make_uint2(pb / kGroup, ((pe - pb) / kGroup) | (ul << 8) | (src << 16) | (uint32_t(slow[u]) << 24));
+  }
+}
+
 // ------------------------------------------------------------- data side
 
 
@@ -161,15 +177,18 @@ struct GraphCtx {
   Mask<W> all;
 };
 
-// Candidate row of the query vertex at position `level` of query qg's filter
-// order.  A vertex whose record equals an earlier one in that order (dup)
-// repeats that row (read back from the arena when the query has rows, row0).
-// Returns whether the row is non-empty.
+// Per (query, level) descriptor, built once per run: x = first clause group of
+// the vertex's program; y = groups | vertex << 8 | dup source << 16 | slow << 24.
+__device__ __forceinline__ uint32_t desc_vertex(uint2 d) { return (d.y >> 8) & 0xFFu; }
+
+// Candidate row of the query vertex at one level of query qg's filter order
+// (its descriptor dsc).  A vertex whose record equals an earlier one in that
+// order (dup) repeats that row (read back from the arena when the query has
+// rows, row0).  Returns whether the row is non-empty.
 template <int W>
-__device__ __forceinline__ bool eval_node(const SlicedArgs& a, const GraphCtx<W>& g, uint32_t qg, uint32_t level,
+__device__ __forceinline__ bool eval_node(const SlicedArgs& a, const GraphCtx<W>& g, uint32_t qg, uint2 dsc,
                                           uint32_t row0, Mask<W>& row) {
-  const uint32_t ul = a.filter_order[uint64_t(qg) * kMaxQueryNodes + level];
-  const uint32_t src = a.dup[uint64_t(qg) * kMaxQueryNodes + ul];
+  const uint32_t ul = desc_vertex(dsc), src = (dsc.y >> 16) & 0xFFu;
   if (src != 0xFFu) {  // same record as an earlier, non-empty row
     if (row0 != kNoRow) {
       const B128 c = ld_b128(a.arena + 2 * (uint64_t(row0) + src));
@@ -179,17 +198,17 @@ __device__ __forceinline__ bool eval_node(const SlicedArgs& a, const GraphCtx<W>
     return true;
   }
   row = g.all;
-  const uint64_t u = uint64_t(a.q.goff[qg]) + ul;
-  const uint32_t pb = a.prog_off[u], pe = a.prog_off[u + 1];
-  const uint4* grp = reinterpret_cast<const uint4*>(a.prog + pb);  // pb is a multiple of 8
-  for (uint32_t k = 0; k < (pe - pb) / kGroup; ++k) {
+  const uint4* grp = reinterpret_cast<const uint4*>(a.prog) + dsc.x;
+  const uint32_t groups = dsc.y & 0xFFu;
+  for (uint32_t k = 0; k < groups; ++k) {
     const uint4 w = __ldg(grp + k);
     row = mand(row, mand(mand(g.tab[w.x & 0xFFFFu], g.tab[w.x >> 16]), mand(g.tab[w.y & 0xFFFFu], g.tab[w.y >> 16])));
     row = mand(row, mand(mand(g.tab[w.z & 0xFFFFu], g.tab[w.z >> 16]), mand(g.tab[w.w & 0xFFFFu], g.tab[w.w >> 16])));
     if (!many(row)) return false;
   }
-  const uint8_t slow = a.slow[u];
+  const uint32_t slow = dsc.y >> 24;
   if (slow && many(row)) {
+    const uint64_t u = uint64_t(a.q.goff[qg]) + ul;
     const uint64_t rec0 = a.qs.frec[uint64_t(kRecWords) * u], rec1 = a.qs.frec[uint64_t(kRecWords) * u + 1];
     const uint32_t ql = uint32_t(rec0 & 0xFFu), qd = uint32_t(rec0 >> 32);
     for (uint32_t v = 0; v < g.m; ++v) {
@@ -376,6 +395,7 @@ __global__ void __launch_bounds__(256) sliced_filter_kernel(SlicedArgs a) {
         const uint32_t i = i0 + tid;
         const bool live = i < count;
         uint32_t qg = 0, n = 0;
+        uint2 dsc0 = make_uint2(0, 0);
         bool join = false, alive = false;
         Mask<W> row = all;
         if (live) {
@@ -383,7 +403,8 @@ __global__ void __launch_bounds__(256) sliced_filter_kernel(SlicedArgs a) {
           qg = e & 0x7FFFFFFFu;
           join = (e >> 31) != 0;
           n = a.q.goff[qg + 1] - a.q.goff[qg];
-          alive = eval_node<W>(a, g, qg, 0, kNoRow, row);
+          dsc0 = __ldg(a.desc + uint64_t(qg) * kMaxQueryNodes);
+          alive = eval_node<W>(a, g, qg, dsc0, kNoRow, row);
         }
         const bool need = live && alive && join;
         uint32_t row0 = kNoRow;
@@ -405,7 +426,7 @@ __global__ void __launch_bounds__(256) sliced_filter_kernel(SlicedArgs a) {
               join = false;
             } else {
               row0 = uint32_t(b);
-              st_b128(a.arena + 2 * (uint64_t(row0) + a.filter_order[uint64_t(qg) * kMaxQueryNodes]), to128(row));
+              st_b128(a.arena + 2 * (uint64_t(row0) + desc_vertex(dsc0)), to128(row));
             }
           }
         }
@@ -441,10 +462,9 @@ __global__ void __launch_bounds__(256) sliced_filter_kernel(SlicedArgs a) {
         bool alive = true;
         for (uint32_t level = 1; level < n && alive; ++level) {
           Mask<W> row = all;
-          alive = eval_node<W>(a, g, qg, level, join ? row0 : kNoRow, row);
-          if (alive && join && row0 != kNoRow)
-            st_b128(a.arena + 2 * (uint64_t(row0) + a.filter_order[uint64_t(qg) * kMaxQueryNodes + level]),
-                    to128(row));
+          const uint2 dsc = __ldg(a.desc + uint64_t(qg) * kMaxQueryNodes + level);
+          alive = eval_node<W>(a, g, qg, dsc, join ? row0 : kNoRow, row);
+          if (alive && join && row0 != kNoRow) st_b128(a.arena + 2 * (uint64_t(row0) + desc_vertex(dsc)), to128(row));
         }
         if (alive) {
           atomicOr(&s_valid[qg >> 5], 1u << (qg & 31u));
@@ -512,6 +532,14 @@ cudaError_t launch_query_programs(const DGraphs& q, const DSigs& qs, ShellPack s
   (void)prog_cap;
   (void)prog_total_host;
   program_fill_kernel<<<blocks, 128, 0, st>>>(q, qs, sp, prog_off, remap, n_used, prog, slow); note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_level_desc(const DGraphs& q, const uint8_t* filter_order, const uint8_t* dup,
+                              const uint32_t* prog_off, const uint8_t* slow, uint2* desc, cudaStream_t st) {
+  if (q.G == 0) return cudaSuccess;
+  const uint64_t want = (uint64_t(q.G) * kMaxQueryNodes + 255) / 256, cap = uint64_t(sm_count()) * 8;
+  level_desc_kernel<<<unsigned(want < cap ? want : cap), 256, 0, st>>>(q, filter_order, dup, prog_off, slow, desc); note_launch();
   return cudaGetLastError();
 }
 

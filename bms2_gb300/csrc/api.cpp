@@ -408,6 +408,8 @@ int run_sliced_filter(bms_ctx* c, const ShellPack& sp, int R, int sem) {
                            c->prog_ids.as<uint16_t>(), c->prog_nused.as<uint32_t>(), c->prog.as<uint16_t>(),
                            c->prog_slow.as<uint8_t>(), Qn * per_node, nullptr, c->st));
   CK(c->level_desc.ensure(sizeof(uint2) * uint64_t(c->q.G ? c->q.G : 1) * kMaxQueryNodes));
+  CK(c->screen.ensure(sizeof(uint4) * (c->q.G ? c->q.G : 1)));
+  CK(launch_screen(c->q.dg(), c->q.ds(), c->q.size_order.as<uint32_t>(), c->screen.as<uint4>(), c->st));
   CK(launch_level_desc(c->q.dg(), c->filter_order.as<uint8_t>(), c->filter_dup.as<uint8_t>(),
                        c->prog_off.as<uint32_t>(), c->prog_slow.as<uint8_t>(), c->level_desc.as<uint2>(), c->st));
   SlicedArgs a{};
@@ -419,6 +421,7 @@ int run_sliced_filter(bms_ctx* c, const ShellPack& sp, int R, int sem) {
   a.dup = c->filter_dup.as<uint8_t>();
   a.qorder = c->q.size_order.as<uint32_t>();
   a.desc = c->level_desc.as<uint2>();
+  a.screen = c->screen.as<uint4>();
   a.prog_off = c->prog_off.as<uint32_t>();
   a.prog = c->prog.as<uint16_t>();
   a.slow = c->prog_slow.as<uint8_t>();

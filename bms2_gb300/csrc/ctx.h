@@ -119,6 +119,7 @@ struct bms_ctx {
   Side dres;         // resident data batch (bms_load_resident); the data side views windows of it
   DevBuf per_query;  // bms_run_batches: per-query totals
   DevBuf level_desc;  // sliced filter: per (query, level) descriptors
+  DevBuf screen;      // sliced filter: per-query screen records
   DevBuf embed_out, embed_tmp;  // bms_get_embeddings
   uint64_t sub_cap = 0;
   uint64_t sub_cap_opt = 0;  // BMS_OPT_SUBTREE_CAP (0: automatic)

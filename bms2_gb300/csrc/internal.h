@@ -180,6 +180,7 @@ struct SlicedArgs {
   const uint8_t* dup;           // [Q*64]
   const uint32_t* qorder;       // [Q] query ids by decreasing node count
   const uint2* desc;            // [Q*64] per (query, level): program groups, vertex, dup source, slow flags
+  const uint4* screen;          // [Q] screen records in screening order (launch_screen)
   const uint32_t* prog_off;     // [Qn+1]
   const uint16_t* prog;         // compact mask indices
   const uint8_t* slow;          // [Qn] clauses outside the table
@@ -209,6 +210,9 @@ cudaError_t launch_query_programs(const DGraphs& q, const DSigs& qs, ShellPack s
                                   uint32_t* n_used, uint16_t* prog, uint8_t* slow, uint64_t prog_cap,
                                   uint32_t* prog_total_host, cudaStream_t st);
 size_t sliced_smem_bytes(const SlicedArgs& a, int words);
+// Screen records of the sliced filter: query, size, label set and histogram in
+// screening order (after the query signatures).
+cudaError_t launch_screen(const DGraphs& q, const DSigs& qs, const uint32_t* qorder, uint4* screen, cudaStream_t st);
 // Per (query, level) descriptors of the sliced filter (after query_prep and the programs).
 cudaError_t launch_level_desc(const DGraphs& q, const uint8_t* filter_order, const uint8_t* dup,
                               const uint32_t* prog_off, const uint8_t* slow, uint2* desc, cudaStream_t st);

@@ -148,6 +148,17 @@ __global__ void program_fill_kernel(DGraphs q, DSigs qs, ShellPack sp, const uin
   }
 }
 
+// Screen record of the i-th query in screening order (decreasing size):
+// {query, size | label set << 16, label histogram low, high}.
+__global__ void screen_kernel(DGraphs q, DSigs qs, const uint32_t* qorder, uint4* screen) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < q.G; i += gridDim.x * blockDim.x) {
+    const uint32_t qg = qorder[i];
+    const uint32_t n = q.goff[qg + 1] - q.goff[qg];
+    const uint64_t h = qs.ghist[qg];
+    screen[i] = make_uint4(qg, (n & 0xFFFFu) | ((qs.glabset[qg] & 0xFFFFu) << 16), uint32_t(h), uint32_t(h >> 32));
+  }
+}
+
 // One descriptor per (query, level of its filter order); see desc_vertex.
 __global__ void level_desc_kernel(DGraphs q, const uint8_t* filter_order, const uint8_t* dup, const uint32_t* prog_off,
                                   const uint8_t* slow, uint2* desc) {
@@ -176,6 +187,14 @@ struct GraphCtx {
   uint32_t start, m;
   Mask<W> all;
 };
+
+// Alive-list entries: query id (24 bits), size (7 bits), join-eligible (bit 31).
+__device__ __forceinline__ uint32_t entry(uint32_t qg, uint32_t n, bool join) {
+  return qg | (n << 24) | (join ? 0x80000000u : 0u);
+}
+__device__ __forceinline__ uint32_t entry_query(uint32_t e) { return e & 0xFFFFFFu; }
+__device__ __forceinline__ uint32_t entry_size(uint32_t e) { return (e >> 24) & 0x7Fu; }
+__device__ __forceinline__ bool entry_join(uint32_t e) { return (e >> 31) != 0; }
 
 // Per (query, level) descriptor, built once per run: x = first clause group of
 // the vertex's program; y = groups | vertex << 8 | dup source << 16 | slow << 24.
@@ -366,12 +385,13 @@ __global__ void __launch_bounds__(256) sliced_filter_kernel(SlicedArgs a) {
     const uint64_t dhist = a.ds.ghist[dg];
     const uint32_t dlab = a.ds.glabset[dg];
     for (uint32_t qb = 0; qb < Q; qb += blockDim.x) {
-      const uint32_t qg = qb + tid < Q ? a.qorder[qb + tid] : Q;  // longest queries first
+      // screen records in screening order (longest queries first)
+      const uint4 sr = qb + tid < Q ? __ldg(a.screen + qb + tid) : make_uint4(Q, 0, 0, 0);
+      const uint32_t qg = sr.x, n = sr.y & 0xFFFFu;
       bool p1 = false, p2 = false;
       if (qg < Q && m > 0) {
-        const uint32_t n = a.q.goff[qg + 1] - a.q.goff[qg];
-        p1 = n > 1 && (a.qs.glabset[qg] & ~dlab) == 0;  // gmcr.hpp:64 and label presence
-        p2 = p1 && (!a.skip_by_labels || nib_le(a.qs.ghist[qg], dhist));
+        p1 = n > 1 && ((sr.y >> 16) & ~dlab) == 0;  // gmcr.hpp:64 and label presence
+        p2 = p1 && (!a.skip_by_labels || nib_le(uint64_t(sr.z) | (uint64_t(sr.w) << 32), dhist));
       }
       const uint32_t bal = __ballot_sync(0xffffffffu, p1);
       uint32_t base = 0;
@@ -379,7 +399,7 @@ __global__ void __launch_bounds__(256) sliced_filter_kernel(SlicedArgs a) {
       base = __shfl_sync(0xffffffffu, base, 0);
       if (p1) {
         const uint32_t k = base + __popc(bal & ((1u << lane) - 1u));
-        s_aq[k] = qg | (p2 ? 0x80000000u : 0u);
+        s_aq[k] = entry(qg, n, p2);
         s_as[k] = kNoRow;
       }
     }
@@ -400,9 +420,9 @@ __global__ void __launch_bounds__(256) sliced_filter_kernel(SlicedArgs a) {
         Mask<W> row = all;
         if (live) {
           const uint32_t e = s_aq[i];
-          qg = e & 0x7FFFFFFFu;
-          join = (e >> 31) != 0;
-          n = a.q.goff[qg + 1] - a.q.goff[qg];
+          qg = entry_query(e);
+          join = entry_join(e);
+          n = entry_size(e);
           dsc0 = __ldg(a.desc + uint64_t(qg) * kMaxQueryNodes);
           alive = eval_node<W>(a, g, qg, dsc0, kNoRow, row);
         }
@@ -438,7 +458,7 @@ __global__ void __launch_bounds__(256) sliced_filter_kernel(SlicedArgs a) {
           base = __shfl_sync(0xffffffffu, base, __ffs(cb) - 1);
           if (cont) {
             const uint32_t k = base + __popc(cb & ((1u << lane) - 1u));
-            s_aq[Q + k] = qg | (join ? 0x80000000u : 0u);
+            s_aq[Q + k] = entry(qg, n, join);
             s_as[Q + k] = row0;
           }
         }
@@ -455,10 +475,9 @@ __global__ void __launch_bounds__(256) sliced_filter_kernel(SlicedArgs a) {
         const uint32_t i = atomicAdd(&s_next, 1u);
         if (i >= count) break;
         const uint32_t e = s_aq[Q + i];
-        const uint32_t qg = e & 0x7FFFFFFFu;
-        const bool join = (e >> 31) != 0;
+        const uint32_t qg = entry_query(e), n = entry_size(e);
+        const bool join = entry_join(e);
         const uint32_t row0 = s_as[Q + i];
-        const uint32_t n = a.q.goff[qg + 1] - a.q.goff[qg];
         bool alive = true;
         for (uint32_t level = 1; level < n && alive; ++level) {
           Mask<W> row = all;
@@ -532,6 +551,12 @@ cudaError_t launch_query_programs(const DGraphs& q, const DSigs& qs, ShellPack s
   (void)prog_cap;
   (void)prog_total_host;
   program_fill_kernel<<<blocks, 128, 0, st>>>(q, qs, sp, prog_off, remap, n_used, prog, slow); note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_screen(const DGraphs& q, const DSigs& qs, const uint32_t* qorder, uint4* screen, cudaStream_t st) {
+  if (q.G == 0) return cudaSuccess;
+  screen_kernel<<<(q.G + 255) / 256, 256, 0, st>>>(q, qs, qorder, screen); note_launch();
   return cudaGetLastError();
 }
 

@@ -14,7 +14,7 @@
 namespace bms {
 namespace {
 
-constexpr int kWarps = 4;  // ~7.8 KB of shared memory per warp
+constexpr int kWarps = 4;  // ~9.8 KB of shared memory per warp
 constexpr int kMaxEntries = 1024;  // CSR entries staged per graph; larger rows read global memory
 
 struct WarpSmem {
@@ -25,6 +25,8 @@ struct WarpSmem {
   uint16_t row[kMaxDataNodes + 1];
   uint8_t col[kMaxEntries];
   B128 labmask[16];
+  uint32_t cyc[kMaxDataNodes][4];  // cycle closures per node (canonical enumeration)
+  uint16_t first[kMaxDataNodes + 1];  // canonical enumeration: offsets of the (s0, a) work items
 };
 
 // CSR row access of the current graph with local ids, from shared memory when
@@ -80,6 +82,81 @@ __device__ void cycles_entries(const WarpSmem& s, const Rows& r, uint32_t v, uin
       }
     }
   }
+}
+
+// Every 5- and 6-cycle of a symmetric graph without repeated entries, once:
+// from its smallest node s0, through larger nodes only, second node below the
+// last.  Each member gets +2 in the same/different-label counter of the
+// cycle's length — exactly what the per-node walk counts (the cycle in both
+// directions), so the halved signature is unchanged.  A cycle is "same" iff
+// all its nodes carry one label (the per-node rule: every node after v on the
+// path has v's label).  Counters in s.cyc; lanes take (s0, first edge) items.
+__device__ void cycles_canonical(WarpSmem& s, uint32_t m, uint32_t lane) {
+  const B128 all = b_lowmask(m);
+  // work items: (s0, a) with a an upper neighbour of s0, spread over the lanes
+  for (uint32_t v = lane; v < m; v += 32) {
+    for (int t = 0; t < 4; ++t) s.cyc[v][t] = 0;
+    s.first[v + 1] = uint16_t(b_pop(b_and(s.adj[v], b_andn(all, b_lowmask(v + 1)))));
+  }
+  __syncwarp();
+  if (lane == 0) {
+    s.first[0] = 0;
+    for (uint32_t v = 1; v <= m; ++v) s.first[v] = uint16_t(s.first[v] + s.first[v - 1]);
+  }
+  __syncwarp();
+  const uint32_t items = s.first[m];
+  for (uint32_t k = lane; k < items; k += 32) {
+    uint32_t lo = 0, hi = m;  // first[lo] <= k < first[hi]
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (s.first[mid] <= k) lo = mid;
+      else hi = mid;
+    }
+    const uint32_t s0 = lo;
+    const B128 gt = b_andn(all, b_lowmask(s0 + 1));
+    B128 up = b_and(s.adj[s0], gt);
+    for (uint32_t r = k - s.first[s0]; r > 0; --r) up = b_clear_low(up);
+    const uint32_t a = b_low(up);
+    const uint32_t l0 = s.lab[s0];
+    const B128 ns = s.adj[s0];
+    const bool s1 = s.lab[a] == l0;
+    const B128 v1 = b_bit(a);
+    const B128 above_a = b_andn(gt, b_lowmask(a + 1));  // orientation: last node > a
+    for (B128 r2 = b_andn(b_and(s.adj[a], gt), v1); b_any(r2); r2 = b_clear_low(r2)) {
+      const uint32_t b = b_low(r2);
+      const bool s2 = s1 && s.lab[b] == l0;
+      const B128 v2 = b_or(v1, b_bit(b));
+      for (B128 r3 = b_andn(b_and(s.adj[b], gt), v2); b_any(r3); r3 = b_clear_low(r3)) {
+        const uint32_t c = b_low(r3);
+        const bool s3 = s2 && s.lab[c] == l0;
+        const B128 v3 = b_or(v2, b_bit(c));
+        for (B128 r4 = b_andn(b_and(s.adj[c], gt), v3); b_any(r4); r4 = b_clear_low(r4)) {
+          const uint32_t d = b_low(r4);
+          const bool s4 = s3 && s.lab[d] == l0;
+          if (b_has(ns, d) && d > a) {
+            const int t = s4 ? 0 : 1;
+            atomicAdd(&s.cyc[s0][t], 2u);
+            atomicAdd(&s.cyc[a][t], 2u);
+            atomicAdd(&s.cyc[b][t], 2u);
+            atomicAdd(&s.cyc[c][t], 2u);
+            atomicAdd(&s.cyc[d][t], 2u);
+          }
+          const B128 v4 = b_or(v3, b_bit(d));
+          for (B128 r5 = b_and(b_andn(b_and(s.adj[d], above_a), v4), ns); b_any(r5); r5 = b_clear_low(r5)) {
+            const uint32_t e = b_low(r5);
+            const int t = (s4 && s.lab[e] == l0) ? 2 : 3;
+            atomicAdd(&s.cyc[s0][t], 2u);
+            atomicAdd(&s.cyc[a][t], 2u);
+            atomicAdd(&s.cyc[b][t], 2u);
+            atomicAdd(&s.cyc[c][t], 2u);
+            atomicAdd(&s.cyc[d][t], 2u);
+            atomicAdd(&s.cyc[e][t], 2u);
+          }
+        }
+      }
+    }
+  }
+  __syncwarp();
 }
 
 // Cycle closures through v on adjacency sets (graphs without repeated entries).
@@ -204,6 +281,9 @@ __global__ void __launch_bounds__(kWarps * 32) signatures_kernel(DGraphs g, DSig
     if (bad && lane == 0) atomicOr(err, bad);
     __syncwarp();
     const Rows rows{&s, g.rowp, g.col, start, global_rows};
+    // symmetric graphs without repeated entries: every cycle found once
+    const bool canonical = !multi && !(bad & kErrAsym);
+    if (canonical) cycles_canonical(s, m, lane);
     for (uint32_t v = lane; v < m; v += 32) {
       const uint64_t u = uint64_t(start) + v;
       const uint32_t lu = s.lab[v];
@@ -227,8 +307,13 @@ __global__ void __launch_bounds__(kWarps * 32) signatures_kernel(DGraphs g, DSig
       }
       // cycle signature
       uint32_t c[4] = {0, 0, 0, 0};
-      if (multi) cycles_entries(s, rows, v, c);
-      else cycles_sets(s, v, c);
+      if (canonical) {
+        for (int t = 0; t < 4; ++t) c[t] = s.cyc[v][t];
+      } else if (multi) {
+        cycles_entries(s, rows, v, c);
+      } else {
+        cycles_sets(s, v, c);
+      }
       const uint64_t cyc = uint64_t((c[0] & 0xFFFFu) >> 1) | (uint64_t((c[1] & 0xFFFFu) >> 1) << 16) |
                            (uint64_t((c[2] & 0xFFFFu) >> 1) << 32) | (uint64_t((c[3] & 0xFFFFu) >> 1) << 48);
       // distance shells 1..R (exact BFS levels); unused steps stay zero

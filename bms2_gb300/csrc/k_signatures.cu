@@ -42,6 +42,18 @@ struct Rows {
   __device__ uint32_t at(uint32_t i) const { return global ? col[i] - start : s->col[i]; }
 };
 
+// Saturating nibble histogram (signature.hpp:22-53) of the labels < 16 of a
+// node set: per present label, min(15, nodes of the set with that label).
+__device__ __forceinline__ uint64_t label_hist(const WarpSmem& s, uint32_t present, B128 set) {
+  uint64_t h = 0;
+  for (uint32_t pl = present; pl; pl &= pl - 1) {
+    const uint32_t l = uint32_t(__ffs(int(pl)) - 1);
+    const uint32_t c = b_pop(b_and(set, s.labmask[l]));
+    h |= uint64_t(c < 15u ? c : 15u) << (4 * l);
+  }
+  return h;
+}
+
 __device__ uint32_t mult(const Rows& r, uint32_t a, uint32_t target) {
   uint32_t k = 0;
   for (uint32_t i = r.begin(a); i < r.end(a); ++i) k += r.at(i) == target;
@@ -284,12 +296,18 @@ __global__ void __launch_bounds__(kWarps * 32) signatures_kernel(DGraphs g, DSig
     // symmetric graphs without repeated entries: every cycle found once
     const bool canonical = !multi && !(bad & kErrAsym);
     if (canonical) cycles_canonical(s, m, lane);
+    // labels < 16 present in the graph: label histograms are popcounts of their masks
+    const uint32_t present = __ballot_sync(0xffffffffu, lane < 16 && b_any(s.labmask[lane]));
     for (uint32_t v = lane; v < m; v += 32) {
       const uint64_t u = uint64_t(start) + v;
       const uint32_t lu = s.lab[v];
       // label signature: +1 per CSR entry on the neighbour's label
       uint64_t lg = 0;
-      for (uint32_t i = rows.begin(v); i < rows.end(v); ++i) nib_inc(lg, s.lab[rows.at(i)]);
+      if (multi) {
+        for (uint32_t i = rows.begin(v); i < rows.end(v); ++i) nib_inc(lg, s.lab[rows.at(i)]);
+      } else {  // every entry distinct: the row as a set
+        lg = label_hist(s, present, s.adj[v]);
+      }
       // path signature: walks v-a-w (w != v) and v-a-w-x (x != a, x != v)
       uint64_t p0 = 0, p1 = 0, p2 = 0, p3 = 0;
       for (B128 ra = s.adj[v]; b_any(ra); ra = b_clear_low(ra)) {
@@ -327,7 +345,7 @@ __global__ void __launch_bounds__(kWarps * 32) signatures_kernel(DGraphs g, DSig
           for (B128 f = frontier; b_any(f); f = b_clear_low(f)) next = b_or(next, s.adj[b_low(f)]);
           next = b_andn(next, reached);
           reached = b_or(reached, next);
-          for (B128 f = next; b_any(f); f = b_clear_low(f)) nib_inc(sh[k], s.lab[b_low(f)]);
+          sh[k] = label_hist(s, present, next);
           frontier = next;
         }
       }
@@ -350,7 +368,6 @@ __global__ void __launch_bounds__(kWarps * 32) signatures_kernel(DGraphs g, DSig
     const uint32_t nib = lane < 16 ? (cnt > 15 ? 15u : cnt) : 0u;
     const uint32_t lo = __reduce_or_sync(0xffffffffu, lane < 8 ? nib << (4 * lane) : 0u);
     const uint32_t hi = __reduce_or_sync(0xffffffffu, (lane >= 8 && lane < 16) ? nib << (4 * (lane - 8)) : 0u);
-    const uint32_t present = __ballot_sync(0xffffffffu, lane < 16 && cnt > 0);
     if (lane == 0) {
       out.ghist[gi] = uint64_t(lo) | (uint64_t(hi) << 32);
       out.glabset[gi] = present & 0xFFFFu;

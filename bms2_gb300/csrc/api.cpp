@@ -34,6 +34,7 @@ bms_schedule default_schedule() {
     s.blocks_per_sm[i] = 3;
     s.warps_per_block[i] = 8;
     s.steps[i] = 32;
+    s.refill[i] = 4;
     s.split_budget[i] = 1024;
   }
   return s;
@@ -253,6 +254,7 @@ void class_launches(const bms_schedule& s, int sem, ClassLaunch cl[3]) {
     cl[k].threads = 32 * int(s.warps_per_block[k] ? s.warps_per_block[k] : 8);
     cl[k].per_pair = (sem == BMS_SEM_REFERENCE_DFS || s.split_depth[k] >= 1) ? 0 : 1;
     cl[k].steps = int(s.steps[k] ? s.steps[k] : 32);
+    cl[k].refill = s.refill[k] ? (s.refill[k] > 32 ? 32u : s.refill[k]) : 4u;
     cl[k].split_budget = s.split_budget[k];
   }
 }
@@ -1424,6 +1426,7 @@ int bms_set_schedule(bms_ctx* c, const bms_schedule* s) {
   for (int i = 0; i < 3; ++i)
     if (s->blocks_per_sm[i] == 0 || s->blocks_per_sm[i] > 32 || s->warps_per_block[i] == 0 ||
         s->warps_per_block[i] > 8 || s->split_depth[i] > 1 || s->steps[i] == 0 || s->steps[i] > 4096 ||
+        s->refill[i] == 0 || s->refill[i] > 32 ||
         s->split_budget[i] > (1u << 31))
       return fail(c, BMS_EINVAL, "schedule entry out of range");
   const bms_schedule fixed = default_schedule();

@@ -257,6 +257,7 @@ struct JoinArgs {
   int find_first;
   int literal;                     // REFERENCE_DFS semantics
   int steps;                       // DFS steps between refills
+  uint32_t refill;                 // idle lanes of a warp that trigger a refill (1..32)
   SubTask* sub[2];                 // subtrees: round r reads sub[r & 1], writes sub[(r + 1) & 1]
   uint64_t sub_cap;                // entries of each subtree buffer
   uint32_t split_budget;           // expansions before a search splits (0: never)
@@ -267,6 +268,7 @@ struct ClassLaunch {
   int blocks, threads;
   int per_pair;           // 1: one task per record; 0: (pair, root) tasks
   int steps;              // DFS steps between refills
+  uint32_t refill;        // idle lanes that trigger a refill
   uint32_t split_budget;  // 0: never split
 };
 // All rounds of the join; the per-class fields of `a` come from cl[class].

@@ -7,8 +7,9 @@
 // scan (graph.hpp:68-73).  Here every lane of a persistent warp runs its own
 // task — a whole pair, or one (pair, root) when pairs are split — and a warp
 // takes a contiguous chunk of tasks from the global queue with one atomic
-// (chunks shrink as the queue drains).  Idle lanes are refilled as soon as a
-// few of them are waiting, so lanes never wait long for a slow neighbour.
+// (chunks shrink as the queue drains).  Idle lanes are refilled once `refill`
+// of them are waiting (a schedule column: refilling often keeps more lanes
+// busy, refilling rarely costs fewer refills).
 //
 // The search state is bitsets over the data graph's local ids: one 32-bit word
 // for graphs of <= 32 nodes, one 64-bit word up to 64, two up to 128 (records
@@ -583,7 +584,7 @@ __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
         else step_inrow<T, W, kMode>(L, a, S);
       }
       const uint32_t idle = __ballot_sync(0xffffffffu, !L.active && !L.done_fetching);
-      if (__popc(idle) >= 4 || (idle && !__any_sync(0xffffffffu, L.active))) break;
+      if (__popc(idle) >= a.refill || (idle && !__any_sync(0xffffffffu, L.active))) break;
     }
   }
 }
@@ -620,6 +621,7 @@ cudaError_t launch_join(const JoinArgs& args, const ClassLaunch cl[3], cudaStrea
       a.round = r;
       a.per_pair = args.literal ? 0 : cl[k].per_pair;
       a.steps = cl[k].steps;
+      a.refill = cl[k].refill;
       a.split_budget = !args.literal && r + 1 < kJoinRounds ? cl[k].split_budget : 0u;
       if (timers) e = cudaEventRecord(timers[r][k][0], st);
       if (e != cudaSuccess) break;

@@ -318,6 +318,7 @@ int bms_autotune(bms_ctx* c, int R, int mode, int order, bms_schedule* out) {
   const Shape shapes[] = {{2, 8}, {3, 8}, {4, 8}, {6, 4}, {8, 4}, {12, 2}};  // <= 256 threads per block
   const uint32_t budgets[] = {256, 1024, 4096, 0};
   const uint32_t steps[] = {16, 32, 64};
+  const uint32_t refills[] = {1, 2, 4, 8};
   const uint32_t depths[] = {0, 1};
   auto sweep = [&](int n, auto apply) -> int {
     for (int i = 0; i < n; ++i) {
@@ -335,6 +336,7 @@ int bms_autotune(bms_ctx* c, int R, int mode, int order, bms_schedule* out) {
           best.warps_per_block[k] = pick.warps_per_block[k];
           best.split_budget[k] = pick.split_budget[k];
           best.steps[k] = pick.steps[k];
+          best.refill[k] = pick.refill[k];
           best.split_depth[k] = pick.split_depth[k];
         }
     }
@@ -348,6 +350,8 @@ int bms_autotune(bms_ctx* c, int R, int mode, int order, bms_schedule* out) {
   r = sweep(4, [&](bms_schedule& s, int k, int i) { s.split_budget[k] = budgets[i]; });
   if (r) return r;
   r = sweep(3, [&](bms_schedule& s, int k, int i) { s.steps[k] = steps[i]; });
+  if (r) return r;
+  r = sweep(4, [&](bms_schedule& s, int k, int i) { s.refill[k] = refills[i]; });
   if (r) return r;
   r = sweep(2, [&](bms_schedule& s, int k, int i) { s.split_depth[k] = depths[i]; });
   if (r) return r;

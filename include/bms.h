@@ -313,7 +313,8 @@ int bms_model_predict(bms_ctx* ctx, float* cost, uint8_t* order);
  * nodes (32, 64, 128; bucket 3 is unused) and searches with bitsets of
  * word_bits[b] bits (32, 64, 128; both fixed by the bucket).  Per bucket:
  * task granularity (split_depth 0 = one task per pair, 1 = one per (pair,
- * root)), launch shape, DFS steps a warp runs between refills, and the
+ * root)), launch shape, DFS steps a warp runs between refills, how many idle
+ * lanes trigger a refill, and the
  * expansions after which a search hands its unexplored subtrees to the next
  * round (0 = never).  bms_autotune times candidate schedules of every bucket
  * on the loaded workload (each bucket's kernels timed on their own) and
@@ -327,6 +328,7 @@ typedef struct {
   uint32_t blocks_per_sm[BMS_SCHED_BUCKETS];
   uint32_t warps_per_block[BMS_SCHED_BUCKETS]; /* 1..8 */
   uint32_t steps[BMS_SCHED_BUCKETS];
+  uint32_t refill[BMS_SCHED_BUCKETS];          /* idle lanes of a warp that trigger a refill, 1..32 */
   uint32_t split_budget[BMS_SCHED_BUCKETS];
   float ms[BMS_SCHED_BUCKETS];
 } bms_schedule;

@@ -481,6 +481,7 @@ def test_autotune_picks_a_valid_schedule_and_keeps_counts(ctx):
             assert s["blocks_per_sm"][k] in (2, 3, 4, 6, 8, 12)
             assert s["warps_per_block"][k] in (2, 4, 8)
             assert s["steps"][k] in (16, 32, 64)
+            assert s["refill"][k] in (1, 2, 4, 8)
             assert s["split_budget"][k] in (0, 256, 1024, 4096)
             assert s["split_depth"][k] in (0, 1)
             assert s["ms"][k] >= 0.0

@@ -286,8 +286,44 @@ JoinArgs join_args(bms_ctx* c, int mode, int sem, bool log_vertices) {
   return ja;
 }
 
-// Order, tasks, join and totals over the records already in place.
-int join_records(bms_ctx* c, int mode, int order, int sem, bool log_vertices) {
+// The clustered join applies when it is switched on and query 0 has nodes
+// (the reference driver keeps the plain join for a depth of 0, BMS2.cpp:233).
+bool cs_active(const bms_ctx* c) {
+  return c->use_cs && c->q.G > 0 && c->q.h_goff.size() > 1 && c->q.h_goff[1] > c->q.h_goff[0];
+}
+
+// Clustered join over the records in place: GMCR position -> record, then one
+// warp per data graph (k_cs.cu).  `dense`: the staged pipeline's matrix.
+int cs_join(bms_ctx* c, int mode, int sem, const uint32_t* dense) {
+  CK(c->rec_of_gpos.ensure(sizeof(uint32_t) * (c->rec_cap ? c->rec_cap : 1)));
+  Counters* ctr = c->ctr.as<Counters>();
+  CK(launch_rec_of_gpos(c->recs.as<PairRec>(), ctr, c->rec_cap, c->rec_of_gpos.as<uint32_t>(), c->st));
+  CsArgs a{};
+  a.q = c->q.dg();
+  a.d = c->d.dg();
+  a.qs = c->q.ds();
+  a.ds = c->d.ds();
+  a.o = order_of(c);
+  a.recs = c->recs.as<PairRec>();
+  a.arena = c->arena.as<uint64_t>();
+  a.gmcr_off = c->gmcr_off.as<uint32_t>();
+  a.rec_of_gpos = c->rec_of_gpos.as<uint32_t>();
+  a.rec_cap = c->rec_cap;
+  a.dperm = c->dperm.as<uint32_t>();
+  a.dense = dense;
+  a.W = c->W;
+  a.end = c->q.h_goff[1] - c->q.h_goff[0];
+  a.ctr = ctr;
+  a.pair_count = c->pair_count.as<unsigned long long>();
+  a.pair_exp = c->pair_exp.as<unsigned long long>();
+  a.pair_flag = c->pair_flag.as<uint32_t>();
+  CK(launch_cs_join(a, sem == BMS_SEM_REFERENCE_DFS, mode == BMS_FIND_FIRST, c->st));
+  return BMS_OK;
+}
+
+// Order, tasks, join and totals over the records already in place.  `dense`
+// (staged pipeline) is the candidate matrix the records were gathered from.
+int join_records(bms_ctx* c, int mode, int order, int sem, bool log_vertices, const uint32_t* dense) {
   const uint64_t Qslots = uint64_t(c->q.G ? c->q.G : 1) * kMaxQueryNodes;
   CK(c->perm.ensure(Qslots));
   CK(c->dadj.ensure(sizeof(uint64_t) * Qslots));
@@ -303,6 +339,18 @@ int join_records(bms_ctx* c, int mode, int order, int sem, bool log_vertices) {
   CK(cudaMemsetAsync(c->pair_exp.p, 0, sizeof(unsigned long long) * c->rec_cap, c->st));
   CK(cudaMemsetAsync(c->pair_flag.p, 0, sizeof(uint32_t) * c->rec_cap, c->st));
   Counters* ctr = c->ctr.as<Counters>();
+  c->last_cs = cs_active(c);
+  if (c->last_cs) {
+    const int r = cs_join(c, mode, sem, dense);
+    if (r) return r;
+    CK(record_event(c, EV_JOIN));
+    CK(launch_totals(ctr, c->rec_cap, c->pair_count.as<unsigned long long>(), c->pair_exp.as<unsigned long long>(),
+                     c->pair_flag.as<uint32_t>(), mode == BMS_FIND_FIRST, ctr, c->st));
+    c->last_mode = mode;
+    c->last_order = order;
+    c->last_sem = sem;
+    return BMS_OK;
+  }
   if (needs_tasks(c->sched, sem))
     CK(launch_task_emit(c->recs.as<PairRec>(), c->rec_cap, c->q.dg(), order_of(c), c->arena.as<uint64_t>(),
                         c->tasks.as<Task>(), c->task_cap, ctr, c->errflag.as<uint32_t>() + 2, c->st));
@@ -347,6 +395,8 @@ int validate_modes(bms_ctx* c, int mode, int order, int sem) {
   if (sem != BMS_SEM_EXACT && sem != BMS_SEM_REFERENCE_DFS) return fail(c, BMS_EINVAL, "invalid semantics");
   if (sem == BMS_SEM_REFERENCE_DFS && order != BMS_ORDER_GMCR)
     return fail(c, BMS_EINVAL, "REFERENCE_DFS semantics require the GMCR order");
+  if (c->use_cs && order != BMS_ORDER_GMCR)
+    return fail(c, BMS_EINVAL, "the clustered join extends the prototype's nodes first: it requires the GMCR order");
   if (order == BMS_ORDER_LEARNED && (c->q.asymmetric || c->d.asymmetric))
     return fail(c, BMS_EINVAL, "the learned order requires symmetric adjacency");
   return BMS_OK;
@@ -374,7 +424,7 @@ int run_ballot_filter(bms_ctx* c, const ShellPack& sp, int sem) {
   pa.row_cap = c->row_cap;
   pa.ctr = c->ctr.as<Counters>();
   pa.err = c->errflag.as<uint32_t>() + 2;
-  pa.skip_by_labels = sem == BMS_SEM_EXACT;
+  pa.skip_by_labels = sem == BMS_SEM_EXACT && !c->use_cs;
   pa.cand_sum = nullptr;
   const int rounds[3] = {1, 2, 4};
   for (int k = 2; k >= 0; --k) {
@@ -444,7 +494,7 @@ int run_sliced_filter(bms_ctx* c, const ShellPack& sp, int R, int sem) {
   a.row_cap = c->row_cap;
   a.ctr = c->ctr.as<Counters>();
   a.err = c->errflag.as<uint32_t>() + 2;
-  a.skip_by_labels = sem == BMS_SEM_EXACT;
+  a.skip_by_labels = sem == BMS_SEM_EXACT && !c->use_cs;
   // two-word graphs (> 64 nodes)
   a.class_begin = c->class_begin[2];
   a.class_end = c->class_end[2];
@@ -568,6 +618,10 @@ int bms_set_option(bms_ctx* c, int option, int64_t value) {
     case BMS_OPT_SUBTREE_CAP:
       if (value < 0 || value > (int64_t(1) << 28)) return fail(c, BMS_EINVAL, "subtree capacity must be in [0, 2^28]");
       c->sub_cap_opt = uint64_t(value);
+      return BMS_OK;
+    case BMS_OPT_USE_CS:
+      if (value != 0 && value != 1) return fail(c, BMS_EINVAL, "clustered join is 0 (off) or 1 (on)");
+      c->use_cs = value != 0;
       return BMS_OK;
     default:
       return fail(c, BMS_EINVAL, "unknown option");
@@ -724,7 +778,9 @@ int bms_join(bms_ctx* c, int mode, int order, int sem, uint64_t* total) {
     CK(launch_set_counter(&c->ctr.as<Counters>()->recs, T, c->st));
     CK(launch_set_counter(&c->ctr.as<Counters>()->recs_wide, T, c->st));  // GMCR order mixes sizes
     CK(launch_set_counter(&c->ctr.as<Counters>()->recs_mid, T, c->st));
-    r = join_records(c, mode, order, sem, mode == BMS_COUNT_ALL && order == BMS_ORDER_GMCR && sem == BMS_SEM_EXACT);
+    r = join_records(c, mode, order, sem,
+                     mode == BMS_COUNT_ALL && order == BMS_ORDER_GMCR && sem == BMS_SEM_EXACT && !cs_active(c),
+                     c->cand.as<uint32_t>());
     if (r) return r;
     CK(cudaMemcpyAsync(c->h_T, c->gmcr_off.as<uint32_t>() + c->d.G, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->st));
     r = finish_run(c, total);
@@ -734,12 +790,13 @@ int bms_join(bms_ctx* c, int mode, int order, int sem, uint64_t* total) {
   }
   if (c->h_err[2] & kErrOverflow) return fail(c, BMS_ENOMEM, "join task buffer overflow");
   c->have_results = true;
-  c->have_vexp = mode == BMS_COUNT_ALL && order == BMS_ORDER_GMCR && sem == BMS_SEM_EXACT;
+  c->have_vexp = mode == BMS_COUNT_ALL && order == BMS_ORDER_GMCR && sem == BMS_SEM_EXACT && !c->last_cs;
   c->stats.ms_order = elapsed(c, EV_MAP, EV_ORDER);
   c->stats.ms_join = elapsed(c, EV_ORDER, EV_JOIN);
   c->stats.total_matches = c->h_ctr->total;
   c->stats.expansions = c->h_ctr->expansions;
   c->stats.n_incomplete = c->h_ctr->incomplete;
+  c->stats.n_partial_matches = c->h_ctr->partials;
   if (total) *total = c->h_ctr->total;
   return c->h_ctr->incomplete ? fail(c, BMS_EINCOMPLETE, "some pairs hit the expansion budget") : BMS_OK;
 }
@@ -760,6 +817,7 @@ int bms_get_embeddings(bms_ctx* c, uint64_t pair, uint8_t* out, uint64_t max_emb
   if (!c->have_results) return fail(c, BMS_ESTATE, "run the pipeline first");
   if (c->last_sem != BMS_SEM_EXACT || c->last_mode != BMS_COUNT_ALL)
     return fail(c, BMS_ESTATE, "embeddings are defined for count-all runs with EXACT semantics");
+  if (c->last_cs) return fail(c, BMS_ESTATE, "embeddings follow the plain join; switch the clustered join off");
   if (pair >= c->T) return fail(c, BMS_EINVAL, "pair index beyond the GMCR");
   // the pair's record (pairs the join skips have none and no embedding)
   CK(c->embed_tmp.ensure(2 * sizeof(unsigned long long)));
@@ -1065,7 +1123,7 @@ int enqueue_fused(bms_ctx* c, int R, int mode, int order, int sem, bool log_vert
   CK(launch_pair_positions(c->recs.as<PairRec>(), c->ctr.as<Counters>(), c->rec_cap, c->valid.as<uint32_t>(), c->QW,
                            c->gmcr_off.as<uint32_t>(), c->st));
   CK(record_event(c, EV_MAP));
-  return join_records(c, mode, order, sem, log_vertices);
+  return join_records(c, mode, order, sem, log_vertices && !cs_active(c), nullptr);
 }
 
 PlanKey plan_key(const bms_ctx* c, int R, int mode, int order, int sem) {
@@ -1079,6 +1137,7 @@ PlanKey plan_key(const bms_ctx* c, int R, int mode, int order, int sem) {
   k.sem = sem;
   k.filter_kernel = c->filter_kernel;
   k.model_set = c->model_set ? 1 : 0;
+  k.use_cs = c->use_cs ? 1 : 0;
   k.sub_cap_opt = c->sub_cap_opt;
   k.budget = c->budget;
   k.rec_cap = c->rec_cap;
@@ -1224,7 +1283,7 @@ int complete_fused(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* to
   c->mapped = true;
   c->have_qidx = false;
   c->have_results = true;
-  c->have_vexp = log_vertices;
+  c->have_vexp = log_vertices && !c->last_cs;
   c->stats.refine_steps = uint32_t(R);
   c->stats.ms_signatures = elapsed(c, EV_START, EV_SIG);
   c->stats.ms_filter = elapsed(c, EV_SIG, EV_FILTER);
@@ -1238,6 +1297,7 @@ int complete_fused(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* to
   c->stats.total_matches = c->h_ctr->total;
   c->stats.expansions = c->h_ctr->expansions;
   c->stats.n_incomplete = c->h_ctr->incomplete;
+  c->stats.n_partial_matches = c->h_ctr->partials;
   if (total) *total = c->h_ctr->total;
   return c->h_ctr->incomplete ? fail(c, BMS_EINCOMPLETE, "some pairs hit the expansion budget") : BMS_OK;
 }
@@ -1247,6 +1307,7 @@ int complete_fused(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* to
 int bms::rejoin_timed(bms_ctx* c, const bms_schedule& sched, float* ms, float class_ms[3]) {
   if (!c->have_results) return fail(c, BMS_ESTATE, "run the pipeline first");
   if (c->last_sem == BMS_SEM_REFERENCE_DFS) return fail(c, BMS_ESTATE, "timing runs use EXACT semantics");
+  if (c->last_cs) return fail(c, BMS_ESTATE, "timing runs time the plain join; switch the clustered join off");
   Counters* ctr = c->ctr.as<Counters>();
   static_assert(offsetof(Counters, sub_n) == offsetof(Counters, join_head) + sizeof(Counters::join_head),
                 "join heads and subtree counts are cleared together");

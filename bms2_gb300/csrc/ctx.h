@@ -81,7 +81,7 @@ enum Ev { EV_START, EV_SIG, EV_FILTER, EV_MAP, EV_ORDER, EV_JOIN, EV_END, EV_COU
 // built from a zeroed object so padding compares equal).
 struct PlanKey {
   unsigned long long load_gen, epoch;
-  int R, mode, order, sem, filter_kernel, model_set;
+  int R, mode, order, sem, filter_kernel, model_set, use_cs;
   uint64_t sub_cap_opt, budget, rec_cap, row_cap, task_cap, sub_cap;
   bms_schedule sched;
 };
@@ -121,6 +121,9 @@ struct bms_ctx {
   DevBuf level_desc;  // sliced filter: per (query, level) descriptors
   DevBuf screen;      // sliced filter: per-query screen records
   DevBuf embed_out, embed_tmp;  // bms_get_embeddings
+  DevBuf rec_of_gpos;           // clustered join: record of each GMCR position
+  bool use_cs = false;          // BMS_OPT_USE_CS
+  bool last_cs = false;         // the last join was the clustered join
   uint64_t sub_cap = 0;
   uint64_t sub_cap_opt = 0;  // BMS_OPT_SUBTREE_CAP (0: automatic)
   uint64_t rec_cap = 0, row_cap = 0, task_cap = 0;

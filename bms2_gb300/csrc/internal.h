@@ -99,6 +99,34 @@ struct Counters {
   // join: work-stealing head per round and record class, subtrees per round
   unsigned long long join_head[kJoinRounds][3];
   unsigned long long sub_n[kJoinRounds + 1];
+  // clustered join: prototype matches and the roots and pushes that found them,
+  // data graphs taken
+  unsigned long long partials;
+  unsigned long long partial_exps;
+  unsigned int cs_head;
+};
+
+// Clustered join (the reference driver's --use-cs): query 0 is the prototype,
+// `end` its node count.  One warp per data graph enumerates the prototype's
+// matches from its candidate rows, then extends each with every query of the
+// graph's GMCR row.
+struct CsArgs {
+  DGraphs q, d;
+  DSigs qs, ds;
+  DOrder o;                    // the plain order (position = query vertex)
+  const PairRec* recs;
+  const uint64_t* arena;
+  const uint32_t* gmcr_off;    // [D + 1]
+  const uint32_t* rec_of_gpos; // record of each GMCR position, kNoRecord if none
+  uint64_t rec_cap;            // entries of rec_of_gpos (positions beyond: a run that overflowed)
+  const uint32_t* dperm;       // data graphs in work order
+  const uint32_t* dense;       // staged pipeline: dense candidate matrix (rows of a one-node prototype)
+  uint64_t W;                  // its words per row
+  uint32_t end;
+  Counters* ctr;
+  unsigned long long* pair_count;
+  unsigned long long* pair_exp;
+  uint32_t* pair_flag;
 };
 
 // ----------------------------------------------------------------- launchers
@@ -289,6 +317,9 @@ struct EmbedArgs {
   unsigned long long* count;   // embeddings found (may exceed cap)
 };
 // out = the index of the record at GMCR position gpos (unchanged if none)
+cudaError_t launch_rec_of_gpos(const PairRec* recs, const Counters* ctr, uint64_t rec_cap, uint32_t* rec_of_gpos,
+                               cudaStream_t st);
+cudaError_t launch_cs_join(const CsArgs& a, bool literal, bool find_first, cudaStream_t st);
 cudaError_t launch_find_record(const PairRec* recs, const Counters* ctr, uint64_t rec_cap, uint32_t gpos,
                                unsigned long long* out, cudaStream_t st);
 cudaError_t launch_embed(const EmbedArgs& a, cudaStream_t st);

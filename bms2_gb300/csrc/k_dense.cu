@@ -154,21 +154,6 @@ __global__ void pair_nodes_kernel(DGraphs q, const uint32_t* qidx, uint64_t T, u
   }
 }
 
-// bits [s, s+m) of a dense row as a 128-bit local row
-__device__ __forceinline__ B128 extract_row(const uint32_t* row, uint64_t W, uint32_t s, uint32_t m) {
-  uint32_t part[4] = {0, 0, 0, 0};
-  for (uint32_t k = 0; k < 4 && 32 * k < m; ++k) {
-    const uint32_t pos = s + 32 * k;
-    const uint32_t wi = pos >> 5, sh = pos & 31u;
-    uint32_t x = row[wi] >> sh;
-    if (sh && wi + 1 < W) x |= row[wi + 1] << (32 - sh);
-    const uint32_t rem = m - 32 * k;
-    if (rem < 32) x &= (1u << rem) - 1u;
-    part[k] = x;
-  }
-  return {uint64_t(part[0]) | (uint64_t(part[1]) << 32), uint64_t(part[2]) | (uint64_t(part[3]) << 32)};
-}
-
 // One warp per data graph: its GMCR pairs in order.
 __global__ void gather_pairs_kernel(DGraphs q, DGraphs d, const uint32_t* cand, uint64_t W, const uint32_t* offsets,
                                     const uint32_t* qidx, const uint32_t* row_off, PairRec* recs, uint64_t* arena) {

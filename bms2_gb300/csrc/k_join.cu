@@ -371,17 +371,26 @@ template <typename T, int W>
 __device__ __forceinline__ Bits<T, W> compute_level(const Lane<T, W>& L, uint32_t j, const uint8_t* f, bool literal) {
   Bits<T, W> c = bload<T, W>(L.crow + 2 * uint64_t(__ldg(L.perm + j)));
   if (!literal) c = bandn(c, L.mapped);
+  const uint64_t adj = __ldg(reinterpret_cast<const unsigned long long*>(L.dadj) + j);
   Bits<T, W> pset = z<T, W>();
-  for (uint64_t pm = __ldg(reinterpret_cast<const unsigned long long*>(L.dadj) + j); pm; pm &= pm - 1) {
+  for (uint64_t pm = adj; pm; pm &= pm - 1) {
     const uint32_t x = f[__ffsll((long long)pm) - 1];
     c = band(c, bload<T, W>(L.arow + 2 * uint64_t(x)));
     pset = bor(pset, bbit<T, W>(x));
   }
+  // images of the earlier non-neighbours: EXACT paths are injective (mapped
+  // minus pset); a literal path can hold a node twice (a stale clear unmarks a
+  // path node), so it collects them position by position
+  Bits<T, W> nset = bandn(L.mapped, pset);
+  if (literal) {
+    nset = z<T, W>();
+    for (uint64_t nm = ~adj & ((uint64_t(1) << j) - 1); nm; nm &= nm - 1)
+      nset = bor(nset, bbit<T, W>(f[__ffsll((long long)nm) - 1]));
+  }
   Bits<T, W> res = z<T, W>();
   for (Bits<T, W> r = c; bany(r); r = bclear_low(r)) {
     const uint32_t v = blow(r);
-    const Bits<T, W> bad = bandn(band(bload<T, W>(L.irow + 2 * uint64_t(v)), L.mapped), pset);
-    if (!bany(bad)) res = bor(res, bbit<T, W>(v));
+    if (!bany(band(bload<T, W>(L.irow + 2 * uint64_t(v)), nset))) res = bor(res, bbit<T, W>(v));
   }
   return res;
 }

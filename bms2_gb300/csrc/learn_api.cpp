@@ -296,6 +296,7 @@ int bms_model_train(bms_ctx* c, const float* x, const float* y, uint32_t n, uint
 // keeps its fastest value before the next column is searched.
 int bms_autotune(bms_ctx* c, int R, int mode, int order, bms_schedule* out) {
   GUARD(c);
+  if (c->use_cs) return bms::fail(c, BMS_EINVAL, "the autotuner times the plain join; switch the clustered join off");
   uint64_t total = 0;
   int r = bms_run(c, R, mode, order, BMS_SEM_EXACT, &total);
   if (r && r != BMS_EINCOMPLETE) return r;

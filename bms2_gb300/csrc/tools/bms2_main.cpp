@@ -9,6 +9,7 @@
 //   --skip-join            stop after the mapping
 //   -p                     print candidates per query node (staged pipeline)
 //   --skip-candidates-analysis
+//   --use-cs               clustered join: query 0 is the prototype (BMS2.cpp:218-296)
 // and the engine's own:
 //   --staged               run the reference-shaped staged pipeline (dense matrix)
 //   --order gmcr|learned   search order (learned needs --model FILE)
@@ -33,6 +34,7 @@ struct Args {
   std::string qfile, dfile, order = "gmcr", semantics = "exact", model;
   int steps = 0, device = 0;
   bool find_all = false, skip_join = false, print_cand = false, skip_cand = false, staged = false, json = false;
+  bool use_cs = false;
   size_t max_data = 1000000, max_query = 1000, mul_data = 1, mul_query = 1;
   bool qfilter = false;
   uint32_t qmin = 0, qmax = 0xFFFFFFFFu;
@@ -43,6 +45,7 @@ struct Args {
   std::fprintf(stderr,
                "usage: bms2 -Q queries -D data [-i steps] [--find-all] [--max-data-graphs N] [--max-query-graphs N]\n"
                "            [--query-filter A[:B]] [-m K|-d K|-q K] [--skip-join] [-p] [--skip-candidates-analysis]\n"
+               "            [--use-cs]\n"
                "            [--staged] [--order gmcr|learned --model FILE] [--semantics exact|reference] [--device N]\n"
                "            [--json]\n");
   std::exit(2);
@@ -61,6 +64,7 @@ Args parse(int argc, char** argv) {
     else if (s == "-i" || s == "--iterations") a.steps = std::atoi(need(i));
     else if (s == "--find-all") a.find_all = true;
     else if (s == "--skip-join") a.skip_join = true;
+    else if (s == "--use-cs") a.use_cs = true;
     else if (s == "-p" || s == "--print-candidates") a.print_cand = true;
     else if (s == "--skip-candidates-analysis") a.skip_cand = true;
     else if (s == "--max-data-graphs") a.max_data = std::strtoull(need(i), nullptr, 10);
@@ -137,6 +141,7 @@ int main(int argc, char** argv) {
       if (a.model.empty()) usage("--order learned needs --model FILE");
       check(bms_model_load(queue.ctx(), a.model.c_str()), queue.ctx());
     }
+    if (a.use_cs) check(bms_set_option(queue.ctx(), BMS_OPT_USE_CS, 1), queue.ctx());
     size_t matches = 0;
     uint64_t pairs = 0;
     std::vector<uint32_t> cand_counts;
@@ -204,6 +209,7 @@ int main(int argc, char** argv) {
       if (a.print_cand)
         for (size_t u = 0; u < cand_counts.size(); ++u) std::fprintf(stderr, "Node %zu: %u\n", u, cand_counts[u]);
     }
+    if (!a.skip_join && a.use_cs) std::printf("# Partial matches: %llu\n", (unsigned long long)st.n_partial_matches);
     if (!a.skip_join) std::printf("# GMCR pairs: %llu\n# Matches: %zu\n", (unsigned long long)pairs, matches);
     return 0;
   } catch (const std::exception& e) {

@@ -26,7 +26,7 @@ SIZE_UNIFORM, SIZE_NORMAL, SIZE_LOGNORMAL = 0, 1, 2
 NUM_FEATURES = 12
 MLP_PARAMS = 64 * 12 + 64 + 64 * 64 + 64 + 64 + 1
 SCHED_BUCKETS = 4
-OPT_FILTER_KERNEL, OPT_JOIN_STEPS, OPT_SPLIT_BUDGET, OPT_SUBTREE_CAP, OPT_CUDA_GRAPH = 1, 2, 3, 4, 5
+OPT_FILTER_KERNEL, OPT_JOIN_STEPS, OPT_SPLIT_BUDGET, OPT_SUBTREE_CAP, OPT_CUDA_GRAPH, OPT_USE_CS = 1, 2, 3, 4, 5, 6
 FILTER_SLICED, FILTER_BALLOT = 0, 1
 
 
@@ -61,7 +61,7 @@ class Stats(C.Structure):
                 ("refine_steps", C.c_uint32), ("last_mode", C.c_uint32), ("last_order", C.c_uint32),
                 ("last_semantics", C.c_uint32), ("ms_signatures", C.c_float), ("ms_filter", C.c_float),
                 ("ms_refine", C.c_float), ("ms_map", C.c_float), ("ms_order", C.c_float), ("ms_join", C.c_float),
-                ("ms_total", C.c_float), ("kernel_launches", C.c_uint64)]
+                ("ms_total", C.c_float), ("kernel_launches", C.c_uint64), ("n_partial_matches", C.c_uint64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -52,3 +52,129 @@ def make(name: str, seed: int = 1, n_data: int | None = None, n_queries: int | N
     queries = Graphs.synth_queries(data, n_queries or w.n_queries, seed + 1000003, w.q_min, w.q_max, w.frac_carbon,
                                    w.frac_adversarial)
     return queries, data
+
+
+# ------------------------------------------------------------------ clusters
+def _graph_at(v, g: int):
+    """(labels, rows, edge labels) of graph g of a GraphsView, local ids; rows[u]
+    lists u's neighbours in CSR order."""
+    import numpy as np
+
+    go = np.ctypeslib.as_array(v.graph_offsets, shape=(v.n_graphs + 1,))
+    s, e = int(go[g]), int(go[g + 1])
+    ro = np.ctypeslib.as_array(v.row_offsets, shape=(v.n_nodes + 1,))
+    ci = np.ctypeslib.as_array(v.column_indices, shape=(max(v.n_entries, 1),))
+    el = np.ctypeslib.as_array(v.edge_labels, shape=(max(v.n_entries, 1),))
+    nl = np.ctypeslib.as_array(v.node_labels, shape=(max(v.n_nodes, 1),))
+    rows, elab = [], []
+    for u in range(s, e):
+        a, b = int(ro[u]), int(ro[u + 1])
+        rows.append([int(x) - s for x in ci[a:b]])
+        elab.append([int(x) for x in el[a:b]])
+    return [int(x) for x in nl[s:e]], rows, elab
+
+
+def _grow(rng, rows, nodes: list, k: int) -> list:
+    """Add up to k nodes to `nodes`, each a random neighbour of the set so far."""
+    out = list(nodes)
+    inside = set(out)
+    for _ in range(k):
+        frontier = sorted({w for u in out for w in rows[u] if w not in inside})
+        if not frontier:
+            break
+        w = frontier[int(rng.integers(len(frontier)))]
+        out.append(w)
+        inside.add(w)
+    return out
+
+
+def _find_induced(p_lab, p_adj, lab, rows, cap: int = 20000):
+    """One label-preserving induced embedding of the prototype (its nodes in
+    order, each after a neighbour) in a graph, or None; gives up after `cap` tries."""
+    adj = [set(r) for r in rows]
+    n, m = len(p_lab), len(lab)
+    assign: list[int] = []
+    tries = [0]
+
+    def rec(i: int) -> bool:
+        if i == n:
+            return True
+        prev = [j for j in p_adj[i] if j < i]
+        pool = sorted(adj[assign[prev[0]]]) if prev else range(m)
+        for v in pool:
+            tries[0] += 1
+            if tries[0] > cap:
+                return False
+            if lab[v] != p_lab[i] or v in assign:
+                continue
+            if all((j in p_adj[i]) == (assign[j] in adj[v]) for j in range(i)):
+                assign.append(v)
+                if rec(i + 1):
+                    return True
+                assign.pop()
+        return False
+
+    return list(assign) if rec(0) else None
+
+
+def make_cluster(data: Graphs, n_members: int, seed: int, proto_nodes: tuple[int, int] = (5, 8),
+                 extra_nodes: tuple[int, int] = (1, 12), n_sources: int = 24) -> Graphs:
+    """A query cluster in the layout of the reference's cluster files
+    (generate_cs.py:338-362, 555-577): graph 0 is the prototype P, a connected
+    induced subgraph of a random data graph numbered in discovery order; each
+    member is P plus 1..12 further atoms grown around an induced occurrence of P
+    in one of up to n_sources data graphs, with P's nodes first, in P's order.
+    (The reference clusters real molecules by maximum common substructure with
+    rdkit, which is absent here; this keeps its file convention.)"""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    v = data.view()
+    G = v.n_graphs
+    go = np.ctypeslib.as_array(v.graph_offsets, shape=(G + 1,))
+    sizes = go[1:].astype(np.int64) - go[:-1]
+    want = proto_nodes[1] + extra_nodes[1]
+    big = np.nonzero(sizes >= want)[0]
+    pool = big if len(big) else np.array([int(np.argmax(sizes))])
+    g0 = int(pool[int(rng.integers(len(pool)))])
+    lab0, rows0, el0 = _graph_at(v, g0)
+    p = int(rng.integers(proto_nodes[0], proto_nodes[1] + 1))
+    proto = _grow(rng, rows0, [int(rng.integers(len(lab0)))], p - 1)
+    p_lab = [lab0[u] for u in proto]
+    pos = {u: i for i, u in enumerate(proto)}
+    p_adj = [{pos[w] for w in rows0[u] if w in pos} for u in proto]
+    occ = [(g0, proto)]
+    for g in rng.permutation(G)[: 50 * n_sources]:
+        if len(occ) >= n_sources:
+            break
+        g = int(g)
+        if g == g0 or sizes[g] < p:
+            continue
+        lab, rows, _ = _graph_at(v, g)
+        emb = _find_induced(p_lab, p_adj, lab, rows)
+        if emb is not None:
+            occ.append((g, emb))
+    cache = {g0: (lab0, rows0, el0)}
+    graphs = [(g0, proto)]
+    for _ in range(n_members):
+        g, emb = occ[int(rng.integers(len(occ)))]
+        if g not in cache:
+            cache[g] = _graph_at(v, g)
+        k = int(rng.integers(extra_nodes[0], extra_nodes[1] + 1))
+        graphs.append((g, _grow(rng, cache[g][1], emb, k)))
+    # induced subgraphs, CSR entries in each source row's order
+    goff, roff, cols, labs, elabs = [0], [0], [], [], []
+    for g, nodes in graphs:
+        lab, rows, el = cache[g]
+        local = {u: i for i, u in enumerate(nodes)}
+        base = goff[-1]
+        for u in nodes:
+            for w, l in zip(rows[u], el[u]):
+                if w in local:
+                    cols.append(base + local[w])
+                    elabs.append(l)
+            roff.append(len(cols))
+            labs.append(lab[u])
+        goff.append(base + len(nodes))
+    return Graphs.from_csr(np.array(goff, np.uint32), np.array(roff, np.uint32), np.array(cols, np.uint32),
+                           np.array(labs, np.uint8), np.array(elabs, np.uint8))

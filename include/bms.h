@@ -159,10 +159,27 @@ typedef enum {
                                 to the next round (default 1024; 0 = never split) */
   BMS_OPT_SUBTREE_CAP = 4,   /* entries of each of the two subtree buffers (88 B each); 0 = one per
                                 record, at least 65,536 and at most 4,194,304 (default) */
-  BMS_OPT_CUDA_GRAPH = 5     /* 1 (default): bms_run captures its device work as a CUDA graph on the
+  BMS_OPT_CUDA_GRAPH = 5,    /* 1 (default): bms_run captures its device work as a CUDA graph on the
                                 second run with unchanged inputs and settings, and replays it after;
                                 0: every run launches its kernels one by one */
+  BMS_OPT_USE_CS = 6         /* 1: the clustered join of the reference driver's --use-cs
+                                (BMS2.cpp:218-296) replaces the join of bms_join, bms_run and the batch
+                                drivers; 0 (default): the plain join.  See below. */
 } bms_option;
+/* Clustered join.  The loaded queries are one cluster in the layout of the
+ * reference's cluster files (generate_cs.py:338-362, 555-577): query 0 is the
+ * prototype P and every member lists P's nodes first, in P's order.  Step 1
+ * (join::joinPartialCandidates2, isomorphism.hpp:1021-1178) finds every match of
+ * P's nodes in every data graph over P's own candidate rows; step 2
+ * (join::joinWithPartialMatches, isomorphism.hpp:756-977) extends each match with
+ * every query of its data graph's GMCR row: a query smaller than P adds 0, one of
+ * P's size adds 1, a larger one adds its completions from node |V(P)| on over
+ * its own candidate rows.  Requires BMS_ORDER_GMCR; both semantics and both
+ * modes apply (REFERENCE_DFS restates both reference DFS loops literally).  With
+ * an empty query 0 the plain join runs, as in the reference driver.  The label
+ * screen of the fused filter is off in this mode (every GMCR pair gets its
+ * candidate rows), the expansion budget and the join schedule do not apply, and
+ * bms_stats.n_partial_matches reports step 1's matches. */
 #define BMS_FILTER_SLICED 0 /* clause masks per data graph in shared memory, one thread per query */
 #define BMS_FILTER_BALLOT 1 /* one lane per data node, candidate rows formed by warp ballots */
 int bms_set_option(bms_ctx* ctx, int option, int64_t value);
@@ -236,6 +253,7 @@ typedef struct {
   /* device time of the last stage calls, milliseconds (CUDA events) */
   float ms_signatures, ms_filter, ms_refine, ms_map, ms_order, ms_join, ms_total;
   uint64_t kernel_launches;  /* CUDA kernels launched by the last pipeline call */
+  uint64_t n_partial_matches; /* clustered join: prototype matches over all data graphs */
 } bms_stats;
 int bms_get_stats(bms_ctx* ctx, bms_stats* out);
 

@@ -14,6 +14,7 @@
 //   isomorphism::filter::refineCandidates (isomorphism.hpp:106)  filter::refineCandidates
 //   isomorphism::mapping::GMCR::generateGMCR (gmcr.hpp:35)       mapping::GMCR::generateGMCR
 //   isomorphism::join::joinCandidates (isomorphism.hpp:291)      join::joinCandidates
+//   joinPartialCandidates2 + joinWithPartialMatches (:1021, :756) join::joinWithPartialMatches
 //
 // The reference's stage objects each own device memory; here one Queue owns a
 // bms_ctx and the stage objects are views on it.  Signatures are computed for
@@ -229,6 +230,26 @@ inline void joinCandidates(Queue& q, const DeviceBatchedCSRGraph&, const DeviceB
   uint64_t total = 0;
   check(bms_join(q.ctx(), find_first ? BMS_FIND_FIRST : BMS_COUNT_ALL, order, semantics, &total), q.ctx());
   *num_matches += size_t(total);
+}
+
+// The --use-cs pair joinPartialCandidates2 (isomorphism.hpp:1021-1178) +
+// joinWithPartialMatches (:756-977) as one call: query 0 is the prototype, the
+// partial matches stay on the device; *num_partial_matches (nullable) receives
+// their number.  The context's plain-join setting is restored afterwards.
+inline void joinWithPartialMatches(Queue& q, const DeviceBatchedCSRGraph&, const DeviceBatchedCSRGraph&,
+                                   candidates::Candidates&, mapping::GMCR&, size_t* num_matches, bool find_first = true,
+                                   int semantics = BMS_SEM_EXACT, size_t* num_partial_matches = nullptr) {
+  check(bms_set_option(q.ctx(), BMS_OPT_USE_CS, 1), q.ctx());
+  uint64_t total = 0;
+  const int st = bms_join(q.ctx(), find_first ? BMS_FIND_FIRST : BMS_COUNT_ALL, BMS_ORDER_GMCR, semantics, &total);
+  bms_set_option(q.ctx(), BMS_OPT_USE_CS, 0);
+  check(st, q.ctx());
+  *num_matches += size_t(total);
+  if (num_partial_matches) {
+    bms_stats s{};
+    check(bms_get_stats(q.ctx(), &s), q.ctx());
+    *num_partial_matches = size_t(s.n_partial_matches);
+  }
 }
 }  // namespace join
 }  // namespace isomorphism

@@ -593,6 +593,196 @@ int orc_pair_embeddings(const uint32_t* q_goff, const uint32_t* q_rowp, const ui
   return 0;
 }
 
+// ---------------------------------------------------------------- clustered join
+// The driver's --use-cs flow (BMS2.cpp:218-296): query 0 is the prototype P of a
+// cluster whose members list P's nodes first (generate_cs.py:338-362, 555-577);
+// depth = |V(P)|.
+//   step 1, join::joinPartialCandidates2 (isomorphism.hpp:1021-1178): in every
+//     data graph, every "partial match" = mapping of P's nodes 0..depth-1 found by
+//     the join DFS over P's candidate rows and P's adjacency;
+//   step 2, join::joinWithPartialMatches (isomorphism.hpp:756-977): for every
+//     partial match of data graph d and every query q of d's GMCR row:
+//     depth > |V(q)| adds nothing, depth == |V(q)| adds 1, otherwise every
+//     candidate b of q's node `depth` that is not in the partial match and passes
+//     the induced test against it roots a DFS over q's rows for nodes depth+1..;
+//     each completed mapping adds 1.  Find-first reports min(count, 1) per pair.
+// dfs_literal = 1 restates both DFS loops verbatim (the visited bit of a
+// candidate a frame moves past is never cleared; an exhausted frame clears the
+// bit of mapping[k]; at depth == end step 1 records the match and pops without
+// touching visited), with mapping[] beyond the fixed prefix reset to NULL_NODE
+// per root, as orc_join reads it.  dfs_literal = 0 counts every injective induced
+// extension of every injective induced prototype match (the exact reading).
+// Generalized reading only (bitsets as wide as the graph).
+// Outputs: counts[t] and expansions[t] per GMCR pair (expansions: branch roots
+// plus successful pushes of step 2 for that pair), *n_partial = partial matches
+// over all data graphs, *partial_exps = roots plus pushes of step 1 (counted
+// where every prototype node has a candidate; elsewhere no match exists and the
+// search is skipped, as orc_join skips such pairs).
+// Returns -2 when there is no prototype (no queries, or query 0 is empty): the
+// driver then runs the plain join.
+int orc_join_cs(uint32_t Qg, const uint32_t* q_goff, const uint32_t* q_rowp, const uint32_t* q_col, uint32_t Dg,
+                const uint32_t* d_goff, const uint32_t* d_rowp, const uint32_t* d_col, uint64_t Dn, const uint32_t* cand,
+                const uint32_t* offsets, const uint32_t* qidx, int find_first, int dfs_literal, int threads,
+                uint64_t* counts, uint64_t* expansions, uint64_t* n_partial, uint64_t* partial_exps) {
+  if (Qg == 0 || q_goff[1] == q_goff[0]) return -2;
+  const uint64_t W = words_per_row(Dn);
+  const uint32_t end = q_goff[1] - q_goff[0];
+  const int nt = nthreads_or_default(threads);
+  (void)nt;
+  uint64_t parts_all = 0, pexps_all = 0;
+  struct Fr {
+    uint32_t depth, idx;
+  };
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt) reduction(+ : parts_all, pexps_all)
+  for (int64_t di = 0; di < int64_t(Dg); ++di) {
+    const uint32_t d = uint32_t(di);
+    const uint32_t start = d_goff[d], stop = d_goff[d + 1], m = stop - start;
+    auto vbit = [&](uint32_t node) -> int64_t {
+      if (node == kNullNode || node < start || node >= stop) return -1;
+      return int64_t(node - start);
+    };
+    // isValidMapping_fast_bitwise (isomorphism.hpp:266-285)
+    auto valid = [&](uint32_t qoff, uint32_t depth, const std::vector<uint32_t>& map, uint32_t v) {
+      for (uint32_t i = 0; i < depth; ++i)
+        if (csr_has(q_rowp, q_col, qoff + depth, qoff + i) != csr_has(d_rowp, d_col, map[i], v)) return false;
+      return true;
+    };
+    // ---- step 1: partial matches of P (query 0) in d
+    std::vector<std::vector<uint32_t>> parts;
+    {
+      const uint32_t qoff = q_goff[0];
+      std::vector<uint32_t> cnt(end);
+      bool possible = true;
+      for (uint32_t i = 0; i < end; ++i) {
+        cnt[i] = range_count(cand + (qoff + i) * W, start, stop);
+        possible = possible && cnt[i] > 0;
+      }
+      std::vector<uint32_t> map(end);
+      std::vector<Fr> st(end + 1);
+      // a node without candidates admits no match: skipped, as orc_join skips such pairs
+      for (uint32_t c0 = 0; possible && c0 < cnt[0]; ++c0) {
+        Bits vis(m);
+        std::fill(map.begin(), map.end(), kNullNode);
+        map[0] = range_select(cand + qoff * W, c0, start, stop);
+        vis.set(size_t(vbit(map[0])));
+        ++pexps_all;
+        uint32_t top = 0;
+        st[top++] = {1, 0};
+        while (top > 0) {
+          const Fr fr = st[top - 1];
+          const uint32_t qd = fr.depth;
+          if (qd == end) {  // isomorphism.hpp:1118-1129: record and pop
+            parts.push_back(map);
+            --top;
+            if (!dfs_literal) {
+              const int64_t bb = vbit(map[end - 1]);
+              if (bb >= 0) vis.clr(size_t(bb));
+            }
+            continue;
+          }
+          if (fr.idx >= cnt[qd]) {
+            --top;
+            if (dfs_literal) {
+              const int64_t bb = vbit(map[qd]);
+              if (bb >= 0) vis.clr(size_t(bb));
+            } else if (top > 0) {
+              const int64_t bb = vbit(map[qd - 1]);
+              if (bb >= 0) vis.clr(size_t(bb));
+            }
+            continue;
+          }
+          const uint32_t v = range_select(cand + (qoff + qd) * W, fr.idx, start, stop);
+          st[top - 1].idx++;
+          if (vis.get(size_t(vbit(v)))) continue;
+          if (valid(qoff, qd, map, v)) {
+            map[qd] = v;
+            vis.set(size_t(vbit(v)));
+            ++pexps_all;
+            st[top++] = {qd + 1, 0};
+          }
+        }
+      }
+    }
+    parts_all += parts.size();
+    // ---- step 2: every query of d's GMCR row against every partial match
+    for (uint32_t t = offsets[d]; t < offsets[d + 1]; ++t) {
+      const uint32_t q = qidx[t];
+      const uint32_t qoff = q_goff[q], n = q_goff[q + 1] - qoff;
+      uint64_t found = 0, exps = 0;
+      if (n <= end) {
+        if (n == end) found = parts.size();
+      } else {
+        std::vector<uint32_t> cnt(n);
+        for (uint32_t i = 0; i < n; ++i) cnt[i] = range_count(cand + (qoff + i) * W, start, stop);
+        std::vector<uint32_t> lm(n);
+        std::vector<Fr> st(n + 1);
+        for (const auto& pm : parts) {
+          if (find_first && found) break;
+          for (uint32_t ci = 0; ci < cnt[end]; ++ci) {
+            const uint32_t b = range_select(cand + (qoff + end) * W, ci, start, stop);
+            bool conflict = false;
+            for (uint32_t i = 0; i < end && !conflict; ++i) conflict = pm[i] == b;
+            if (conflict || !valid(qoff, end, pm, b)) continue;
+            Bits vis(m);
+            std::fill(lm.begin(), lm.end(), kNullNode);
+            for (uint32_t i = 0; i < end; ++i) {
+              lm[i] = pm[i];
+              vis.set(size_t(vbit(pm[i])));
+            }
+            lm[end] = b;
+            vis.set(size_t(vbit(b)));
+            ++exps;
+            uint64_t tm = 0;
+            uint32_t top = 0;
+            st[top++] = {end + 1, 0};
+            while (top > 0) {
+              const Fr fr = st[top - 1];
+              const uint32_t qd = fr.depth;
+              if (qd == n) {
+                ++tm;
+                --top;
+                if (!dfs_literal) {
+                  const int64_t bb = vbit(lm[n - 1]);
+                  if (bb >= 0 && n - 1 > end) vis.clr(size_t(bb));
+                }
+                if (find_first) break;
+                continue;
+              }
+              if (fr.idx >= cnt[qd]) {
+                --top;
+                if (dfs_literal) {
+                  const int64_t bb = vbit(lm[qd]);
+                  if (bb >= 0) vis.clr(size_t(bb));
+                } else if (top > 0) {
+                  const int64_t bb = vbit(lm[qd - 1]);
+                  if (bb >= 0) vis.clr(size_t(bb));
+                }
+                continue;
+              }
+              const uint32_t v = range_select(cand + (qoff + qd) * W, fr.idx, start, stop);
+              st[top - 1].idx++;
+              if (vis.get(size_t(vbit(v)))) continue;
+              if (valid(qoff, qd, lm, v)) {
+                lm[qd] = v;
+                vis.set(size_t(vbit(v)));
+                ++exps;
+                st[top++] = {qd + 1, 0};
+              }
+            }
+            found += tm;
+            if (find_first && tm) break;
+          }
+        }
+      }
+      counts[t] = find_first ? (found ? 1 : 0) : found;
+      if (expansions) expansions[t] = exps;
+    }
+  }
+  if (n_partial) *n_partial = parts_all;
+  if (partial_exps) *partial_exps = pexps_all;
+  return 0;
+}
+
 // ---------------------------------------------------------------- MLP oracle
 // Learned-order cost model (no reference counterpart): 12 -> 64 -> 64 -> 1, ReLU,
 // weights rounded to bfloat16 (round-to-nearest-even), fp32 accumulation.

@@ -49,6 +49,9 @@ def load() -> C.CDLL:
         L.orc_join.restype = C.c_int
         L.orc_join.argtypes = [C.c_uint32, _u32p, _u32p, _u32p, C.c_uint32, _u32p, _u32p, _u32p, C.c_uint64, _u32p,
                                _u32p, _u32p, C.c_int, C.c_int, C.c_int, C.c_int, _u64p, _u64p]
+        L.orc_join_cs.restype = C.c_int
+        L.orc_join_cs.argtypes = [C.c_uint32, _u32p, _u32p, _u32p, C.c_uint32, _u32p, _u32p, _u32p, C.c_uint64,
+                                  _u32p, _u32p, _u32p, C.c_int, C.c_int, C.c_int, _u64p, _u64p, _u64p, _u64p]
         L.orc_pair_embeddings.restype = C.c_int
         L.orc_pair_embeddings.argtypes = [_u32p, _u32p, _u32p, _u32p, _u32p, _u32p, C.c_uint64, _u32p, _u32p,
                                           C.c_uint32, _u32p, C.c_uint64, C.POINTER(C.c_uint8), C.c_uint64, _u64p]
@@ -101,6 +104,8 @@ class OracleResult:
     qidx: np.ndarray | None = None
     counts: np.ndarray | None = None
     expansions: np.ndarray | None = None
+    n_partial: int = 0      # clustered join: prototype matches over all data graphs
+    partial_exps: int = 0   # clustered join: roots and pushes of its first step
 
     @property
     def cand(self) -> np.ndarray:
@@ -121,8 +126,12 @@ class OracleResult:
 
 
 def run_pipeline(query, data, R: int, find_first: bool = False, x86: bool = False, dfs_literal: bool = False,
-                 threads: int = 0, keep_steps: bool = True, join: bool = True) -> OracleResult:
-    """The reference driver's flow (BMS2.cpp:131-234) on the CPU."""
+                 threads: int = 0, keep_steps: bool = True, join: bool = True, cs: bool = False) -> OracleResult:
+    """The reference driver's flow (BMS2.cpp:131-234) on the CPU; cs=True runs
+    the clustered join of its --use-cs flag (BMS2.cpp:218-296, query 0 the
+    prototype), falling back to the plain join when query 0 is empty."""
+    if cs and x86:
+        raise ValueError("the clustered join has the generalized reading only")
     L = load()
     q, d = _csr(query), _csr(data)
     qs = signatures(q, R, x86, threads)
@@ -153,6 +162,20 @@ def run_pipeline(query, data, R: int, find_first: bool = False, x86: bool = Fals
     L.orc_gmcr(Qg, _p(q["graph_offsets"], C.c_uint32), Dg, _p(d["graph_offsets"], C.c_uint32), Dn, _p(cand, C.c_uint32),
                threads, _p(offsets, C.c_uint32), _p(qidx, C.c_uint32), len(qidx), C.byref(total))
     res.offsets, res.qidx = offsets, qidx[:T]
+    if join and cs:
+        counts = np.zeros(max(T, 1), np.uint64)
+        exps = np.zeros(max(T, 1), np.uint64)
+        npart, pexps = C.c_uint64(), C.c_uint64()
+        r = L.orc_join_cs(Qg, _p(q["graph_offsets"], C.c_uint32), _p(q["row_offsets"], C.c_uint32),
+                          _p(q["column_indices"], C.c_uint32), Dg, _p(d["graph_offsets"], C.c_uint32),
+                          _p(d["row_offsets"], C.c_uint32), _p(d["column_indices"], C.c_uint32), Dn,
+                          _p(cand, C.c_uint32), _p(offsets, C.c_uint32), _p(qidx, C.c_uint32), int(find_first),
+                          int(dfs_literal), threads, _p(counts, C.c_uint64), _p(exps, C.c_uint64), C.byref(npart),
+                          C.byref(pexps))
+        if r == 0:
+            res.counts, res.expansions = counts[:T], exps[:T]
+            res.n_partial, res.partial_exps = int(npart.value), int(pexps.value)
+            return res
     if join:
         counts = np.zeros(max(T, 1), np.uint64)
         exps = np.zeros(max(T, 1), np.uint64)

@@ -131,6 +131,22 @@ def test_fused_run_bit_exact(ctx, wl, R, mode, sem):
     assert st["n_pairs"] == q.n_graphs * d.n_graphs
 
 
+@pytest.mark.parametrize("seed", [17, 32])
+def test_literal_dfs_paths_that_repeat_a_node(ctx, seed):
+    # in these seeded workloads the reference DFS's stale clear unmarks a node
+    # on the path and the search maps that node a second time (pairs found by a
+    # search over seeds); the induced test then has to compare position by
+    # position, as isValidMapping_fast_bitwise does (isomorphism.hpp:266-285)
+    q, d = workloads.make("mol1k", seed, n_data=60, n_queries=12)
+    for mode in (COUNT_ALL, FIND_FIRST):
+        want = oracle.run_pipeline(q, d, 0, find_first=mode == FIND_FIRST, dfs_literal=True)
+        load(ctx, q, d)
+        assert ctx.run(0, mode, ORDER_GMCR, SEM_REFERENCE_DFS) == want.total
+        assert np.array_equal(ctx.pair_counts(), want.counts)
+        if mode == COUNT_ALL:
+            assert np.array_equal(ctx.pair_expansions(), want.expansions)
+
+
 def test_fused_expansions_match_oracle_exact_plain_order(ctx, wl):
     # oracle expansions count the reference DFS's successful pushes per pair;
     # the engine's bitset DFS makes the same assignments in EXACT mode

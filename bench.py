@@ -11,6 +11,7 @@ A) and evaluated (seed B).  mol100k (100,000 graphs of N(28, 9) atoms x 600
 queries of 5-30 nodes, 30% pure-carbon) is the plain-method GPU configuration.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--order learned|plain] [--workload mol100k|mol1m]
+  python bench.py --workload mol1m-cs [--cluster-members M]   # the clustered join (--use-cs)
   python bench.py --impl reference ...   # the CPU restatement of the reference
 
 With the learned order (the default) the cost model is first trained on a
@@ -120,9 +121,10 @@ def algorithmic_filter_bytes(qn: int, dn: int, R: int) -> float:
     return qn * dn / 8.0 + (dn + qn) * (45.0 + 8.0 * R)
 
 
-def cpu_baseline(q, d, threads: int, budget_s: float = 15.0) -> dict:
+def cpu_baseline(q, d, threads: int, budget_s: float = 15.0, cs: bool = False) -> dict:
     """The CPU restatement of the reference pipeline (OpenMP over nodes, words,
-    pairs) on a bounded sample: all queries x the first k data graphs."""
+    pairs) on a bounded sample: all queries x the first k data graphs (cs: the
+    clustered join of the driver's --use-cs)."""
     import oracle
     from bms2_gb300 import Graphs
 
@@ -133,7 +135,7 @@ def cpu_baseline(q, d, threads: int, budget_s: float = 15.0) -> dict:
     while True:
         sub = _head(a, k)
         t0 = time.perf_counter()
-        res = oracle.run_pipeline(q, sub, REFINE_STEPS, threads=threads, keep_steps=False)
+        res = oracle.run_pipeline(q, sub, REFINE_STEPS, threads=threads, keep_steps=False, cs=cs)
         t = time.perf_counter() - t0
         if t > budget_s / 4 or k >= len(a["graph_offsets"]) - 1:
             t_one = t
@@ -142,7 +144,7 @@ def cpu_baseline(q, d, threads: int, budget_s: float = 15.0) -> dict:
     del Graphs
     return {"value": Q * k / t_one, "unit": "pairs/s", "cores": threads, "kind": "port",
             "sample": f"{Q} queries x first {k} of {len(a['graph_offsets']) - 1} data graphs, R={REFINE_STEPS}, "
-                      f"count-all, {t_one:.2f} s", "matches": int(res.total)}
+                      f"count-all{', clustered join' if cs else ''}, {t_one:.2f} s", "matches": int(res.total)}
 
 
 def _head(a: dict, k: int) -> dict:
@@ -478,6 +480,154 @@ def run_streamed(args) -> None:
         dist.destroy_process_group()
 
 
+def run_clustered(args) -> None:
+    """mol1m-cs: the reference driver's --use-cs phase (run.sh: -i 6 --find-all,
+    one cluster file per run, BMS2.cpp:218-296) on GB300.  One seeded cluster
+    (query 0 the prototype of 5-8 nodes, --cluster-members members listing its
+    nodes first) against the mol1m seed-B data graphs.  value: steps of bms_run
+    with the clustered join (count-all, EXACT, GMCR order); results.plain_*: the
+    plain join on the same inputs and settings, timed the same way."""
+    import ctypes
+
+    import torch
+    import torch.distributed as dist
+
+    from bms2_gb300 import (COUNT_ALL, DATA, OPT_USE_CS, ORDER_GMCR, QUERY, SEM_EXACT, Context, native, shards,
+                            workloads)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    ctx = Context(local)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    _, d = workloads.make("mol1m", 202 + rank, n_data=args.data_graphs)
+    q = workloads.make_cluster(d, args.cluster_members, 303, proto_nodes=(5, 8), proto=args.cluster_proto)
+    Q, D = q.n_graphs, d.n_graphs
+    qa, da = q.arrays(), d.arrays()
+    ctx.load(QUERY, q)
+    ctx.load(DATA, d)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+
+    def step(cs=True, R=REFINE_STEPS):
+        ctx.set_option(OPT_USE_CS, int(cs))
+        return ctx.run(R, COUNT_ALL, ORDER_GMCR, SEM_EXACT)
+
+    def timed(cs, k):
+        ms, stages = [], []
+        for _ in range(k):
+            flush.fill_(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            tot = step(cs)
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            stages.append(ctx.stats())
+        return ms, stages, tot
+
+    # at two refinement steps every filter is sound for induced embeddings and
+    # both joins count the same embeddings, pair by pair
+    step(False, 2)
+    r2_plain = ctx.pair_counts()
+    step(True, 2)
+    r2_equal = bool(np.array_equal(ctx.pair_counts(), r2_plain))
+    for _ in range(args.warmup):
+        step(False)
+    p_ms, p_stage, p_total = timed(False, args.steps)
+    p_counts = ctx.pair_counts()
+    for _ in range(args.warmup):
+        step(True)
+    clocks = Clocks(local)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    clocks.start()
+    ms_steps, stage, total = timed(True, args.steps)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    launches = sum(s["kernel_launches"] for s in stage)
+    st = stage[-1]
+    c_counts = ctx.pair_counts()
+    t_total = float(np.sum(ms_steps)) / 1e3
+    all_total, all_valid = int(total), int(st["n_valid_pairs"])
+    if world > 1:
+        all_total, all_valid, t_total = shards.reduce_totals(all_total, all_valid, t_total, device=dev)
+    # e2e: pinned host CSR in, per-pair counts out, through the C ABI
+    pin = {k: torch.from_numpy(v).pin_memory() for k, v in da.items()}
+    qpin = {k: torch.from_numpy(v).pin_memory() for k, v in qa.items()}
+    T = st["n_valid_pairs"]
+    out = torch.empty(max(T, 1), dtype=torch.int64).pin_memory()
+    L = native.lib()
+    h2d = sum(int(v.numel() * v.element_size()) for v in list(pin.values()) + list(qpin.values()))
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for kind, p in ((QUERY, qpin), (DATA, pin)):
+            ctx.load_csr_ptrs(kind, len(p["graph_offsets"]) - 1, p["graph_offsets"].data_ptr(),
+                              p["row_offsets"].data_ptr(), p["column_indices"].data_ptr(), p["node_labels"].data_ptr(),
+                              p["edge_labels"].data_ptr())
+        step(True)
+        native._check(L.bms_get_pair_counts(ctx.handle, ctypes.cast(out.data_ptr(), native._u64p), out.numel()),
+                      ctx.handle)
+        torch.cuda.synchronize(dev)
+        if i >= args.warmup:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_s = float(np.mean(e2e_ms)) / 1e3
+    pairs = Q * D
+    value = world * pairs * args.steps / t_total
+    plain_value = world * pairs / (float(np.mean(p_ms)) / 1e3)
+    peak, peak_kind = peaks()
+    fbytes = algorithmic_filter_bytes(st["n_query_nodes"], st["n_data_nodes"], REFINE_STEPS)
+    f_ms = float(np.mean([s["ms_filter"] for s in stage]))
+    achieved = fbytes / (f_ms / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_total * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": f"mol1m-cs: {D} data graphs x one cluster of {Q} queries ({args.cluster_proto} "
+                               f"prototype of {int(qa['graph_offsets'][1])} atoms + {Q - 1} members) per GPU, "
+                               f"refine steps {REFINE_STEPS}, count-all, EXACT, clustered join (--use-cs)",
+                   "data_graphs_per_gpu": D, "queries": Q, "refine_steps": REFINE_STEPS, "order": "plain",
+                   "l2": "flushed between steps (512 MiB write outside the timed events)",
+                   "parallelism": f"data-graph shards x{world}"},
+        "e2e": {"value": world * pairs / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": int(T * 8)},
+        "roofline": {"kernel": "sliced_filter (fused filter + refine + GMCR validity)", "bound": "hbm",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "peak_kind": f"{peak_kind} hbm_gbs", "algorithmic_bytes": fbytes, "ms": f_ms,
+                     "equivalent": True},
+        "stage_ms": {k: float(np.mean([s[k] for s in stage])) for k in
+                     ("ms_signatures", "ms_filter", "ms_map", "ms_order", "ms_join", "ms_total")},
+        "clocks": clk,
+        "gpu_launches": int(launches),
+        "results": {"total_matches": int(total), "valid_pairs": int(T), "expansions": int(st["expansions"]),
+                    "partial_matches": int(st["n_partial_matches"]),
+                    "total_matches_all_ranks": all_total, "valid_pairs_all_ranks": all_valid,
+                    "plain_value": plain_value, "clustered_over_plain": value / plain_value,
+                    "plain_total_matches": int(p_total), "plain_expansions": int(p_stage[-1]["expansions"]),
+                    "plain_ms_per_step": float(np.mean(p_ms)),
+                    "plain_join_ms": float(np.mean([s["ms_join"] for s in p_stage])),
+                    "counts_equal_every_pair": bool(np.array_equal(c_counts, p_counts)),
+                    "counts_equal_every_pair_at_2_refine_steps": r2_equal},
+    }
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(q, d, os.cpu_count() or 1, args.cpu_budget, cs=True)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
 def run_reference(args) -> None:
     """The reference's CPU path: its SYCL CPU build cannot be built here, so the
     oracle (a C++ restatement of the reference kernels, OpenMP over all host
@@ -487,12 +637,17 @@ def run_reference(args) -> None:
         return
     from bms2_gb300 import workloads
 
-    q, d = workloads.make(args.workload, 202)
+    cs = args.workload == "mol1m-cs"
+    if cs:
+        _, d = workloads.make("mol1m", 202)
+        q = workloads.make_cluster(d, args.cluster_members, 303, proto_nodes=(5, 8), proto=args.cluster_proto)
+    else:
+        q, d = workloads.make(args.workload, 202)
     threads = os.cpu_count() or 1
     cb = None
     vals = []
     for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(q, d, threads, budget_s=args.cpu_budget if i >= args.warmup else 4.0)
+        cb = cpu_baseline(q, d, threads, budget_s=args.cpu_budget if i >= args.warmup else 4.0, cs=cs)
         if i >= args.warmup:
             vals.append(cb["value"])
     v = float(np.mean(vals))
@@ -513,7 +668,10 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--order", choices=["learned", "plain"], default="learned")
-    ap.add_argument("--workload", choices=["mol100k", "mol1m", "mol10m"], default=WORKLOAD)
+    ap.add_argument("--workload", choices=["mol100k", "mol1m", "mol10m", "mol1m-cs"], default=WORKLOAD)
+    ap.add_argument("--cluster-members", type=int, default=100, help="mol1m-cs: members of the query cluster")
+    ap.add_argument("--cluster-proto", choices=["ring", "grow"], default="ring",
+                    help="mol1m-cs: a carbon-ring prototype or a grown 5-8 atom fragment")
     ap.add_argument("--slice", type=int, default=500_000, help="mol10m: data graphs per streamed slice")
     ap.add_argument("--latency-sample", type=int, default=16, help="mol10m: queries timed alone")
     ap.add_argument("--train-graphs", type=int, default=20000)
@@ -531,6 +689,8 @@ def main() -> None:
         run_reference(args)
     elif args.workload == "mol10m":
         run_streamed(args)
+    elif args.workload == "mol1m-cs":
+        run_clustered(args)
     else:
         run_ours(args)
 

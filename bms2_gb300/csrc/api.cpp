@@ -292,12 +292,39 @@ bool cs_active(const bms_ctx* c) {
   return c->use_cs && c->q.G > 0 && c->q.h_goff.size() > 1 && c->q.h_goff[1] > c->q.h_goff[0];
 }
 
-// Clustered join over the records in place: GMCR position -> record, then one
-// warp per data graph (k_cs.cu).  `dense`: the staged pipeline's matrix.
+// Clustered join over the records in place: GMCR position -> record, then
+// EXACT: round 0 of the join kernels takes data graphs (prototype matches
+// extended by the join's own steps, long searches split into later rounds);
+// REFERENCE_DFS: one warp per data graph restating both reference loops
+// (k_cs.cu).  `dense`: the staged pipeline's matrix.
 int cs_join(bms_ctx* c, int mode, int sem, const uint32_t* dense) {
-  CK(c->rec_of_gpos.ensure(sizeof(uint32_t) * (c->rec_cap ? c->rec_cap : 1)));
+  CK(c->pos_desc.ensure(sizeof(uint4) * (c->rec_cap ? c->rec_cap : 1)));
   Counters* ctr = c->ctr.as<Counters>();
-  CK(launch_rec_of_gpos(c->recs.as<PairRec>(), ctr, c->rec_cap, c->rec_of_gpos.as<uint32_t>(), c->st));
+  CK(launch_pos_desc(c->recs.as<PairRec>(), ctr, c->rec_cap, c->q.dg(), c->pos_desc.as<uint4>(), c->st));
+  const uint32_t end = c->q.h_goff[1] - c->q.h_goff[0];
+  if (sem == BMS_SEM_EXACT) {
+    JoinArgs ja = join_args(c, mode, sem, false);
+    ja.cs_end = end;
+    ja.gmcr_off = c->gmcr_off.as<uint32_t>();
+    ja.pos_desc = c->pos_desc.as<uint4>();
+    ja.dperm = c->dperm.as<uint32_t>();
+    ja.qs = c->q.ds();
+    ja.dense = dense;
+    ja.dense_w = c->W;
+    // entries: header + the match's bytes padded to 8, one array per class
+    ja.cs_stride = uint32_t(sizeof(CsEntry)) + ((end + 7u) & ~7u);
+    if (c->cs_cap == 0) c->cs_cap = std::max<uint64_t>(1 << 16, c->rec_cap);
+    ja.cs_cap = c->cs_cap;
+    for (int k = 0; k < 3; ++k) {
+      CK(c->cs_ent[k].ensure(uint64_t(ja.cs_stride) * c->cs_cap));
+      ja.cs_ent[k] = c->cs_ent[k].as<uint8_t>();
+    }
+    ja.err = c->errflag.as<uint32_t>() + 2;
+    ClassLaunch cl[3];
+    class_launches(c->sched, sem, cl);
+    CK(launch_join(ja, cl, c->st));
+    return BMS_OK;
+  }
   CsArgs a{};
   a.q = c->q.dg();
   a.d = c->d.dg();
@@ -307,17 +334,17 @@ int cs_join(bms_ctx* c, int mode, int sem, const uint32_t* dense) {
   a.recs = c->recs.as<PairRec>();
   a.arena = c->arena.as<uint64_t>();
   a.gmcr_off = c->gmcr_off.as<uint32_t>();
-  a.rec_of_gpos = c->rec_of_gpos.as<uint32_t>();
+  a.pos_desc = c->pos_desc.as<uint4>();
   a.rec_cap = c->rec_cap;
   a.dperm = c->dperm.as<uint32_t>();
   a.dense = dense;
   a.W = c->W;
-  a.end = c->q.h_goff[1] - c->q.h_goff[0];
+  a.end = end;
   a.ctr = ctr;
   a.pair_count = c->pair_count.as<unsigned long long>();
   a.pair_exp = c->pair_exp.as<unsigned long long>();
   a.pair_flag = c->pair_flag.as<uint32_t>();
-  CK(launch_cs_join(a, sem == BMS_SEM_REFERENCE_DFS, mode == BMS_FIND_FIRST, c->st));
+  CK(launch_cs_join(a, mode == BMS_FIND_FIRST, c->st));
   return BMS_OK;
 }
 
@@ -787,6 +814,8 @@ int bms_join(bms_ctx* c, int mode, int order, int sem, uint64_t* total) {
     if (r) return r;
     if (!(c->h_err[2] & kErrOverflow)) break;
     c->task_cap = std::max<uint64_t>(c->h_ctr->tasks + 1, c->task_cap * 2);
+    for (unsigned long long n : c->h_ctr->cs_n)
+      if (c->cs_cap && n > c->cs_cap) c->cs_cap = std::max<uint64_t>(c->cs_cap, n + n / 8 + 1024);
   }
   if (c->h_err[2] & kErrOverflow) return fail(c, BMS_ENOMEM, "join task buffer overflow");
   c->have_results = true;
@@ -1143,6 +1172,7 @@ PlanKey plan_key(const bms_ctx* c, int R, int mode, int order, int sem) {
   k.rec_cap = c->rec_cap;
   k.row_cap = c->row_cap;
   k.task_cap = c->task_cap;
+  k.cs_cap = c->cs_cap;
   k.sub_cap = c->sub_cap;
   k.sched = c->sched;
   return k;
@@ -1276,7 +1306,13 @@ int complete_fused(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* to
     c->rec_cap = std::max<uint64_t>(c->rec_cap, h.recs + h.recs / 8 + 1024);
     c->row_cap = std::max<uint64_t>(c->row_cap, h.rows + h.rows / 8 + 16384);
     c->task_cap = std::max<uint64_t>(c->task_cap, h.tasks + h.tasks / 8 + 16384);
-    if (h.recs <= c->rec_cap && h.rows <= c->row_cap && h.tasks < c->task_cap / 2) c->task_cap *= 2;
+    bool cs_over = false;  // the clustered entries explain the overflow
+    for (unsigned long long n : h.cs_n)
+      if (c->cs_cap && n > c->cs_cap) {
+        cs_over = true;
+        c->cs_cap = std::max<uint64_t>(c->cs_cap, n + n / 8 + 1024);
+      }
+    if (!cs_over && h.recs <= c->rec_cap && h.rows <= c->row_cap && h.tasks < c->task_cap / 2) c->task_cap *= 2;
     return run_fused(c, R, mode, order, sem, total, log_vertices, attempt + 1);
   }
   c->T = *c->h_T;

@@ -82,7 +82,7 @@ enum Ev { EV_START, EV_SIG, EV_FILTER, EV_MAP, EV_ORDER, EV_JOIN, EV_END, EV_COU
 struct PlanKey {
   unsigned long long load_gen, epoch;
   int R, mode, order, sem, filter_kernel, model_set, use_cs;
-  uint64_t sub_cap_opt, budget, rec_cap, row_cap, task_cap, sub_cap;
+  uint64_t sub_cap_opt, budget, rec_cap, row_cap, task_cap, sub_cap, cs_cap;
   bms_schedule sched;
 };
 
@@ -121,7 +121,9 @@ struct bms_ctx {
   DevBuf level_desc;  // sliced filter: per (query, level) descriptors
   DevBuf screen;      // sliced filter: per-query screen records
   DevBuf embed_out, embed_tmp;  // bms_get_embeddings
-  DevBuf rec_of_gpos;           // clustered join: record of each GMCR position
+  DevBuf pos_desc;              // clustered join: descriptor of each GMCR position
+  DevBuf cs_ent[3];             // clustered join (EXACT): entries per size class
+  uint64_t cs_cap = 0;          // entries each of cs_ent holds (grown on overflow)
   bool use_cs = false;          // BMS_OPT_USE_CS
   bool last_cs = false;         // the last join was the clustered join
   uint64_t sub_cap = 0;

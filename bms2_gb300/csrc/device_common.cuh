@@ -136,6 +136,34 @@ __device__ __forceinline__ B128 extract_row(const uint32_t* row, uint64_t W, uin
   return {uint64_t(part[0]) | (uint64_t(part[1]) << 32), uint64_t(part[2]) | (uint64_t(part[3]) << 32)};
 }
 
+// Candidates of a one-node prototype (global query node u) in data graph
+// [start, start+m): its row of the dense matrix (staged pipeline), or the
+// filter and refine tests of u against every data node (isomorphism.hpp:30-104,
+// 106-203: label or wildcard, degree, path superset, cycle counts, shells
+// 1..R).  Warp-uniform: every lane returns the whole row.
+__device__ __forceinline__ B128 prototype_row(const uint64_t* qfrec, const uint64_t* dfrec, int R,
+                                              const uint32_t* dense, uint64_t W, uint32_t u, uint32_t start,
+                                              uint32_t m) {
+  if (dense) return extract_row(dense + uint64_t(u) * W, W, start, m);
+  const uint64_t* qr = qfrec + uint64_t(kRecWords) * u;
+  const uint64_t w0 = qr[0], qc = qr[1], q0 = qr[2], q1 = qr[3], q2 = qr[4], q3 = qr[5];
+  const uint32_t ql = uint32_t(w0 & 0xFFu), qd = uint32_t(w0 >> 32);
+  uint32_t part[4] = {0, 0, 0, 0};
+  for (uint32_t k = 0; k < 4 && 32 * k < m; ++k) {
+    const uint32_t v = 32 * k + (threadIdx.x & 31u);
+    bool ok = false;
+    if (v < m) {
+      const uint64_t* r = dfrec + uint64_t(kRecWords) * (start + v);
+      const uint32_t dl = uint32_t(r[0] & 0xFFu), dd = uint32_t(r[0] >> 32);
+      ok = (ql == dl || ql == kWildcard) && qd <= dd && (r[2] & q0) == q0 && (r[3] & q1) == q1 &&
+           (r[4] & q2) == q2 && (r[5] & q3) == q3 && cyc_ge(r[1], qc);
+      for (int s = 0; s < R && ok; ++s) ok = nib_le(qr[6 + s], r[6 + s]);
+    }
+    part[k] = __ballot_sync(0xffffffffu, ok);
+  }
+  return {uint64_t(part[0]) | (uint64_t(part[1]) << 32), uint64_t(part[2]) | (uint64_t(part[3]) << 32)};
+}
+
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 
 // graph id of a global node id: upper bound search on graph offsets

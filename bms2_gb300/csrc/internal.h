@@ -104,12 +104,15 @@ struct Counters {
   unsigned long long partials;
   unsigned long long partial_exps;
   unsigned int cs_head;
+  unsigned int cs_ghead;          // clustered join (EXACT): data graphs taken by the enumeration
+  unsigned long long cs_n[3];     // clustered entries written per class
 };
 
-// Clustered join (the reference driver's --use-cs): query 0 is the prototype,
-// `end` its node count.  One warp per data graph enumerates the prototype's
-// matches from its candidate rows, then extends each with every query of the
-// graph's GMCR row.
+// Clustered join (the reference driver's --use-cs), REFERENCE_DFS semantics:
+// query 0 is the prototype, `end` its node count.  One warp per data graph
+// enumerates the prototype's matches from its candidate rows, then extends
+// each with every query of the graph's GMCR row.  (EXACT runs in the join
+// kernels: JoinArgs.cs_end.)
 struct CsArgs {
   DGraphs q, d;
   DSigs qs, ds;
@@ -117,8 +120,8 @@ struct CsArgs {
   const PairRec* recs;
   const uint64_t* arena;
   const uint32_t* gmcr_off;    // [D + 1]
-  const uint32_t* rec_of_gpos; // record of each GMCR position, kNoRecord if none
-  uint64_t rec_cap;            // entries of rec_of_gpos (positions beyond: a run that overflowed)
+  const uint4* pos_desc;       // per GMCR position {record (kNoRecord: none), first row, query nodes, query}
+  uint64_t rec_cap;            // entries of pos_desc (positions beyond: a run that overflowed)
   const uint32_t* dperm;       // data graphs in work order
   const uint32_t* dense;       // staged pipeline: dense candidate matrix (rows of a one-node prototype)
   uint64_t W;                  // its words per row
@@ -290,7 +293,29 @@ struct JoinArgs {
   uint64_t sub_cap;                // entries of each subtree buffer
   uint32_t split_budget;           // expansions before a search splits (0: never)
   int round;                       // set by launch_join
+  // Clustered join (EXACT): with cs_end > 0, round 0 first writes every
+  // prototype match as entries (match, first member, data graph) per size
+  // class, then the class kernels start each entry's members like subtrees
+  // with the match as prefix.
+  uint32_t cs_end;                 // prototype size (query 0), 0: plain join
+  const uint32_t* gmcr_off;        // [D + 1]
+  const uint4* pos_desc;           // per GMCR position {record (kNoRecord: none), first row, query nodes, query}
+  const uint32_t* dperm;           // data graphs, largest class first
+  DSigs qs;                        // query signatures (a one-node prototype's row)
+  const uint32_t* dense;           // staged pipeline: dense candidate matrix, else null
+  uint64_t dense_w;                // its words per row
+  uint8_t* cs_ent[3];              // entries of each class: CsEntry header + the match's bytes
+  uint64_t cs_cap;                 // entries each array holds
+  uint32_t cs_stride;              // bytes per entry
+  uint32_t* err;                   // overflow flag (kErrOverflow)
 };
+// Clustered entry: data graph, first member (index into the graph's GMCR row);
+// the match's end bytes follow (padded to 8).
+struct CsEntry {
+  uint32_t d;
+  uint32_t j0;
+};
+constexpr uint32_t kCsMembers = 32;  // members of the graph's GMCR row per entry
 // Launch shape and task settings of one record class (size bucket) of the join.
 struct ClassLaunch {
   int blocks, threads;
@@ -317,9 +342,11 @@ struct EmbedArgs {
   unsigned long long* count;   // embeddings found (may exceed cap)
 };
 // out = the index of the record at GMCR position gpos (unchanged if none)
-cudaError_t launch_rec_of_gpos(const PairRec* recs, const Counters* ctr, uint64_t rec_cap, uint32_t* rec_of_gpos,
+// Descriptor of every GMCR position: {record, its first candidate row, query
+// nodes, query}; positions without a record read kNoRecord.
+cudaError_t launch_pos_desc(const PairRec* recs, const Counters* ctr, uint64_t rec_cap, const DGraphs& q, uint4* desc,
                                cudaStream_t st);
-cudaError_t launch_cs_join(const CsArgs& a, bool literal, bool find_first, cudaStream_t st);
+cudaError_t launch_cs_join(const CsArgs& a, bool find_first, cudaStream_t st);  // REFERENCE_DFS
 cudaError_t launch_find_record(const PairRec* recs, const Counters* ctr, uint64_t rec_cap, uint32_t gpos,
                                unsigned long long* out, cudaStream_t st);
 cudaError_t launch_embed(const EmbedArgs& a, cudaStream_t st);

@@ -1,4 +1,6 @@
-// Clustered join: the reference driver's --use-cs flow (BMS2.cpp:218-296).
+// Clustered join, REFERENCE_DFS semantics: the reference driver's --use-cs
+// flow (BMS2.cpp:218-296) restated literally.  (EXACT runs inside the join
+// kernels, k_join.cu, as round 0 of the join.)
 //
 // The query batch is one cluster: query 0 is the prototype P, and every member
 // lists P's nodes first, in P's order (generate_cs.py:338-362, 555-577).  The
@@ -9,22 +11,17 @@
 // graph's GMCR row.  Here one warp owns a data graph from start to end: its
 // lanes enumerate P's matches (each lane a share of the roots) into a 64-entry
 // shared-memory buffer, then the whole warp extends the buffered matches, one
-// (match, query) item per lane, before it refills the buffer.  No match leaves
-// the SM and the items of a graph spread over all 32 lanes.
+// (match, query) item per lane, before it refills the buffer.
 //
 // Per item (match of graph d, query q of d's GMCR row, n = |V(q)|): n < end
-// adds nothing, n == end adds 1, otherwise the DFS over q's candidate rows from
-// depth `end` with the match as the fixed prefix counts the completed mappings.
-// Rows are the pair's 128-bit candidate rows (the prototype's own pair for P),
-// the induced test is the in-row test (one adjacency word per candidate).
-//
-// EXACT counts every injective induced extension of every injective induced
-// prototype match.  REFERENCE_DFS (literal) restates both reference DFS loops:
-// a frame never clears the visited bit of a candidate it moves past, an
+// adds nothing, n == end adds 1, otherwise every branch root (a candidate of
+// q's node `end` outside the match that passes the induced test against it)
+// starts a DFS over q's candidate rows.  Both loops are the reference's: a
+// frame never clears the visited bit of a candidate it moves past, an
 // exhausted frame clears the bit of mapping[k] (the last value written at depth
 // k in this root's search, nothing before the first write), step 1 records a
 // match at depth `end` and pops without touching visited, and step 2 starts
-// each branch root with visited = prefix + root.
+// each branch root with visited = match + root.
 #include "device_common.cuh"
 
 namespace bms {
@@ -34,39 +31,29 @@ constexpr int kCsWarps = 4;     // warps per block
 constexpr int kCsBuf = 64;      // prototype matches buffered per warp
 constexpr int kCsChunk = 4;     // data graphs taken per work-queue atomic
 
-__global__ void rec_of_gpos_kernel(const PairRec* recs, const Counters* ctr, uint64_t rec_cap, uint32_t* out) {
+__global__ void pos_desc_kernel(const PairRec* recs, const Counters* ctr, uint64_t rec_cap, DGraphs q, uint4* out) {
   const uint64_t n = min((unsigned long long)rec_cap, ctr->recs);
   for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
-    const uint32_t g = recs[i].gpos;
-    if (g < rec_cap) out[g] = uint32_t(i);
+    const PairRec r = recs[i];
+    if (r.gpos < rec_cap) out[r.gpos] = make_uint4(uint32_t(i), r.c_row, q.goff[r.q + 1] - q.goff[r.q], r.q);
   }
 }
 
 // Candidates at depth j of a query (rows `crow`, order adjacency `dadj`) given
 // the path f[0..j-1]: v is kept iff it is in the rows of the images of j's
 // earlier query neighbours and in no row of the images of its earlier
-// non-neighbours (isValidMapping_fast_bitwise, isomorphism.hpp:266-285).
-// EXACT also drops the path nodes (`mapped`); its path is injective, so the
-// non-neighbour images are mapped minus the neighbour images.  The literal
-// reading can hold a node twice on its path (a stale clear unmarks a path
-// node), so it collects the non-neighbour images position by position.
+// non-neighbours (isValidMapping_fast_bitwise, isomorphism.hpp:266-285).  The
+// path may hold a node twice (a stale clear unmarks a path node), so the
+// non-neighbour images are collected position by position; path nodes are
+// left to the visited set.
 __device__ __forceinline__ B128 level(const uint64_t* crow, const uint64_t* dadj, const uint64_t* arow,
-                                      const uint64_t* irow, uint32_t j, const uint8_t* f, B128 mapped, bool literal) {
+                                      const uint64_t* irow, uint32_t j, const uint8_t* f) {
   B128 c = ld_b128(crow + 2 * uint64_t(j));
-  if (!literal) c = b_andn(c, mapped);
   const uint64_t adj = __ldg(reinterpret_cast<const unsigned long long*>(dadj) + j);
-  B128 pset{0, 0};
-  for (uint64_t pm = adj; pm; pm &= pm - 1) {
-    const uint32_t x = f[__ffsll((long long)pm) - 1];
-    c = b_and(c, ld_b128(arow + 2 * uint64_t(x)));
-    pset = b_or(pset, b_bit(x));
-  }
-  B128 nset = b_andn(mapped, pset);
-  if (literal) {
-    nset = B128{0, 0};
-    for (uint64_t nm = ~adj & ((uint64_t(1) << j) - 1); nm; nm &= nm - 1)
-      nset = b_or(nset, b_bit(f[__ffsll((long long)nm) - 1]));
-  }
+  for (uint64_t pm = adj; pm; pm &= pm - 1) c = b_and(c, ld_b128(arow + 2 * uint64_t(f[__ffsll((long long)pm) - 1])));
+  B128 nset{0, 0};
+  for (uint64_t nm = ~adj & ((uint64_t(1) << j) - 1); nm; nm &= nm - 1)
+    nset = b_or(nset, b_bit(f[__ffsll((long long)nm) - 1]));
   B128 res{0, 0};
   for (B128 r = c; b_any(r); r = b_clear_low(r)) {
     const uint32_t v = b_low(r);
@@ -75,42 +62,15 @@ __device__ __forceinline__ B128 level(const uint64_t* crow, const uint64_t* dadj
   return res;
 }
 
-// Candidates of a one-node prototype in data graph [start, start+m): its row
-// of the dense matrix (staged pipeline), or the filter and refine tests of
-// node u against every data node (isomorphism.hpp:30-104, 106-203: label or
-// wildcard, degree, path superset, cycle counts, shells 1..R).  Warp-uniform.
-__device__ B128 single_row(const CsArgs& a, uint32_t u, uint32_t start, uint32_t m) {
-  if (a.dense) return extract_row(a.dense + uint64_t(u) * a.W, a.W, start, m);
-  const uint64_t* qr = a.qs.frec + uint64_t(kRecWords) * u;
-  const uint64_t w0 = qr[0], qc = qr[1], q0 = qr[2], q1 = qr[3], q2 = qr[4], q3 = qr[5];
-  const uint32_t ql = uint32_t(w0 & 0xFFu), qd = uint32_t(w0 >> 32);
-  uint32_t part[4] = {0, 0, 0, 0};
-  for (uint32_t k = 0; k < 4 && 32 * k < m; ++k) {
-    const uint32_t v = 32 * k + lane_id();
-    bool ok = false;
-    if (v < m) {
-      const uint64_t* r = a.ds.frec + uint64_t(kRecWords) * (start + v);
-      const uint32_t dl = uint32_t(r[0] & 0xFFu), dd = uint32_t(r[0] >> 32);
-      ok = (ql == dl || ql == kWildcard) && qd <= dd && (r[2] & q0) == q0 && (r[3] & q1) == q1 &&
-           (r[4] & q2) == q2 && (r[5] & q3) == q3 && cyc_ge(r[1], qc);
-      for (int s = 0; s < a.ds.R && ok; ++s) ok = nib_le(qr[6 + s], r[6 + s]);
-    }
-    part[k] = __ballot_sync(0xffffffffu, ok);
-  }
-  return {uint64_t(part[0]) | (uint64_t(part[1]) << 32), uint64_t(part[2]) | (uint64_t(part[3]) << 32)};
-}
-
 // A lane's enumeration of prototype matches (joinPartialCandidates2's DFS).
 struct Enum {
-  B128 roots;   // roots not started yet
-  B128 mapped;  // path nodes below the current depth
-  B128 vis;     // literal: the visited set
+  B128 roots;  // roots not started yet
+  B128 vis;    // the visited set
   uint64_t mpset;
-  int t;        // current depth, -1 = start the next root
+  int t;       // current depth, -1 = start the next root
   bool done;
 };
 
-template <bool kLiteral>
 __device__ __forceinline__ bool next_match(Enum& e, uint32_t end, const uint64_t* crow, const uint64_t* dadj,
                                            const uint64_t* arow, const uint64_t* irow, uint8_t* f, B128* F, uint8_t* mp,
                                            unsigned long long& exps) {
@@ -122,82 +82,33 @@ __device__ __forceinline__ bool next_match(Enum& e, uint32_t end, const uint64_t
       f[0] = uint8_t(v0);
       ++exps;
       if (end == 1) return true;
-      e.mapped = b_bit(v0);
-      if (kLiteral) {
-        e.vis = e.mapped;
-        e.mpset = 0;
-      }
-      F[1] = level(crow, dadj, arow, irow, 1, f, e.mapped, kLiteral);
+      e.vis = b_bit(v0);
+      e.mpset = 0;
+      F[1] = level(crow, dadj, arow, irow, 1, f);
       e.t = 1;
     }
     int t = e.t;
-    if (!b_any(F[t])) {  // frame t exhausted
-      if (kLiteral && ((e.mpset >> t) & 1ull)) e.vis = b_andn(e.vis, b_bit(mp[t]));
+    if (!b_any(F[t])) {  // frame t exhausted: mapping[t] leaves visited
+      if ((e.mpset >> t) & 1ull) e.vis = b_andn(e.vis, b_bit(mp[t]));
       if (t == 1) {
         e.t = -1;
         continue;
       }
-      e.t = --t;
-      e.mapped = b_andn(e.mapped, b_bit(f[t]));
+      e.t = t - 1;
       continue;
     }
     const uint32_t v = b_low(F[t]);
     F[t] = b_clear_low(F[t]);
-    if (kLiteral) {
-      if (b_has(e.vis, v)) continue;
-      mp[t] = uint8_t(v);
-      e.mpset |= uint64_t(1) << t;
-      e.vis = b_or(e.vis, b_bit(v));
-    }
+    if (b_has(e.vis, v)) continue;
+    mp[t] = uint8_t(v);
+    e.mpset |= uint64_t(1) << t;
+    e.vis = b_or(e.vis, b_bit(v));
     f[t] = uint8_t(v);
     ++exps;
     if (uint32_t(t) + 1 == end) return true;  // depth `end`: recorded, popped at once
-    e.mapped = b_or(e.mapped, b_bit(v));
-    F[t + 1] = level(crow, dadj, arow, irow, uint32_t(t) + 1, f, e.mapped, kLiteral);
+    F[t + 1] = level(crow, dadj, arow, irow, uint32_t(t) + 1, f);
     e.t = t + 1;
   }
-}
-
-// EXACT extension of prefix f[0..end-1] to the n nodes of a query.
-template <bool kFind>
-__device__ unsigned long long extend_exact(uint32_t end, uint32_t n, const uint64_t* crow, const uint64_t* dadj,
-                                           const uint64_t* arow, const uint64_t* irow, uint8_t* f, B128* F,
-                                           unsigned long long& exps) {
-  B128 mapped{0, 0};
-  for (uint32_t k = 0; k < end; ++k) mapped = b_or(mapped, b_bit(f[k]));
-  const B128 c = level(crow, dadj, arow, irow, end, f, mapped, false);
-  if (end + 1 == n) {
-    const uint32_t pc = b_pop(c);
-    exps += pc;
-    return pc;
-  }
-  unsigned long long cnt = 0;
-  uint32_t t = end;
-  F[t] = c;
-  for (;;) {
-    if (!b_any(F[t])) {
-      if (t == end) break;
-      --t;
-      mapped = b_andn(mapped, b_bit(f[t]));
-      continue;
-    }
-    const uint32_t v = b_low(F[t]);
-    F[t] = b_clear_low(F[t]);
-    f[t] = uint8_t(v);
-    mapped = b_or(mapped, b_bit(v));
-    ++exps;
-    const B128 nf = level(crow, dadj, arow, irow, t + 1, f, mapped, false);
-    if (t + 2 == n) {  // the leaf level is counted, not expanded
-      const uint32_t pc = b_pop(nf);
-      cnt += pc;
-      exps += pc;
-      mapped = b_andn(mapped, b_bit(v));
-      if (kFind && cnt) return cnt;
-      continue;
-    }
-    F[++t] = nf;
-  }
-  return cnt;
 }
 
 // Literal extension (joinWithPartialMatches' loop over branch roots and its DFS).
@@ -208,7 +119,7 @@ __device__ unsigned long long extend_literal(uint32_t end, uint32_t n, const uin
   B128 pre{0, 0};
   for (uint32_t k = 0; k < end; ++k) pre = b_or(pre, b_bit(f[k]));
   // branch roots: induced-consistent with the prefix and not in it
-  const B128 roots = b_andn(level(crow, dadj, arow, irow, end, f, pre, true), pre);
+  const B128 roots = b_andn(level(crow, dadj, arow, irow, end, f), pre);
   unsigned long long cnt = 0;
   for (B128 rr = roots; b_any(rr); rr = b_clear_low(rr)) {
     const uint32_t b = b_low(rr);
@@ -219,11 +130,10 @@ __device__ unsigned long long extend_literal(uint32_t end, uint32_t n, const uin
       continue;
     }
     f[end] = uint8_t(b);
-    B128 mapped = b_or(pre, b_bit(b));
-    B128 vis = mapped;
+    B128 vis = b_or(pre, b_bit(b));
     uint64_t mpset = 0;
     uint32_t t = end + 1;
-    F[t] = level(crow, dadj, arow, irow, t, f, mapped, true);
+    F[t] = level(crow, dadj, arow, irow, t, f);
     if (t + 1 == n) {  // the first frame is the leaf frame
       const uint32_t pc = b_pop(b_andn(F[t], vis));
       cnt += pc;
@@ -236,7 +146,6 @@ __device__ unsigned long long extend_literal(uint32_t end, uint32_t n, const uin
         if ((mpset >> t) & 1ull) vis = b_andn(vis, b_bit(mp[t]));
         if (t == end + 1) break;
         --t;
-        mapped = b_andn(mapped, b_bit(f[t]));
         continue;
       }
       const uint32_t v = b_low(F[t]);
@@ -246,9 +155,8 @@ __device__ unsigned long long extend_literal(uint32_t end, uint32_t n, const uin
       mp[t] = uint8_t(v);
       mpset |= uint64_t(1) << t;
       vis = b_or(vis, b_bit(v));
-      mapped = b_or(mapped, b_bit(v));
       ++exps;
-      const B128 nf = level(crow, dadj, arow, irow, t + 1, f, mapped, true);
+      const B128 nf = level(crow, dadj, arow, irow, t + 1, f);
       if (t + 2 == n) {
         // frame n-1: every unvisited candidate is pushed and popped at depth n
         const uint32_t last = n - 1;
@@ -263,7 +171,6 @@ __device__ unsigned long long extend_literal(uint32_t end, uint32_t n, const uin
           mpset |= uint64_t(1) << last;
         }
         if ((mpset >> last) & 1ull) vis = b_andn(vis, b_bit(mp[last]));  // frame n-1 exhausted
-        mapped = b_andn(mapped, b_bit(v));                               // frame t moves on
         continue;
       }
       F[++t] = nf;
@@ -272,7 +179,7 @@ __device__ unsigned long long extend_literal(uint32_t end, uint32_t n, const uin
   return cnt;
 }
 
-template <bool kLiteral, bool kFind>
+template <bool kFind>
 __global__ void __launch_bounds__(kCsWarps * 32) cs_join_kernel(CsArgs a) {
   __shared__ __align__(16) uint8_t s_buf[kCsWarps][kCsBuf * kMaxQueryNodes];
   const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
@@ -295,7 +202,7 @@ __global__ void __launch_bounds__(kCsWarps * 32) cs_join_kernel(CsArgs a) {
       const uint64_t* crow_p = nullptr;
       B128 roots;
       if (end == 1) {
-        roots = single_row(a, p_off, start, m);
+        roots = prototype_row(a.qs.frec, a.ds.frec, a.ds.R, a.dense, a.W, p_off, start, m);
         if (vcount == 0) {  // no query to extend: only the matches are counted
           if (lane == 0) {
             parts += b_pop(roots);
@@ -305,9 +212,9 @@ __global__ void __launch_bounds__(kCsWarps * 32) cs_join_kernel(CsArgs a) {
         }
       } else {
         // the prototype's own pair heads the row when it is valid (query ids ascend)
-        const uint32_t r0 = vcount && g0 < a.rec_cap ? a.rec_of_gpos[g0] : kNoRecord;
-        if (r0 == kNoRecord || a.recs[r0].q != 0) continue;
-        crow_p = a.arena + 2 * uint64_t(a.recs[r0].c_row);
+        const uint4 p0 = vcount && g0 < a.rec_cap ? a.pos_desc[g0] : make_uint4(kNoRecord, 0, 0, 0);
+        if (p0.x == kNoRecord || p0.w != 0) continue;
+        crow_p = a.arena + 2 * uint64_t(p0.y);
         roots = ld_b128(crow_p);
       }
       const uint64_t* arow = a.ds.adj + 2 * uint64_t(start);
@@ -319,7 +226,7 @@ __global__ void __launch_bounds__(kCsWarps * 32) cs_join_kernel(CsArgs a) {
         for (B128 r = roots; b_any(r); r = b_clear_low(r), ++k)
           if ((k & 31u) == lane) e.roots = b_or(e.roots, b_bit(b_low(r)));
       }
-      e.mapped = e.vis = B128{0, 0};
+      e.vis = B128{0, 0};
       e.mpset = 0;
       e.t = -1;
       e.done = false;
@@ -329,7 +236,7 @@ __global__ void __launch_bounds__(kCsWarps * 32) cs_join_kernel(CsArgs a) {
         for (;;) {
           bool have = false;
           if (!e.done) {
-            have = next_match<kLiteral>(e, end, crow_p, a.o.dadj, arow, irow, fa, Fa, mpa, pexps);
+            have = next_match(e, end, crow_p, a.o.dadj, arow, irow, fa, Fa, mpa, pexps);
             e.done = !have;
           }
           const uint32_t bal = __ballot_sync(0xffffffffu, have);
@@ -347,20 +254,18 @@ __global__ void __launch_bounds__(kCsWarps * 32) cs_join_kernel(CsArgs a) {
         for (uint32_t k = lane; k < items; k += 32) {
           const uint32_t p = k / vcount, j = k - p * vcount;
           if (uint64_t(g0) + j >= a.rec_cap) continue;
-          const uint32_t rec = a.rec_of_gpos[g0 + j];
+          const uint4 pd = a.pos_desc[g0 + j];
+          const uint32_t rec = pd.x, n = pd.z;
           if (rec == kNoRecord) continue;
-          const PairRec r = a.recs[rec];
-          const uint32_t n = a.q.goff[r.q + 1] - a.q.goff[r.q];
           if (n < end) continue;
           if (kFind && (a.pair_flag[rec] & 1u)) continue;
           unsigned long long cnt = 1, ex = 0;
           if (n > end) {
             const uint8_t* src = buf + p * kMaxQueryNodes;
             for (uint32_t t = 0; t < end; ++t) fb[t] = src[t];
-            const uint64_t* crow = a.arena + 2 * uint64_t(r.c_row);
-            const uint64_t* dadj = a.o.dadj + uint64_t(r.q) * kMaxQueryNodes;
-            cnt = kLiteral ? extend_literal<kFind>(end, n, crow, dadj, arow, irow, fb, Fb, mpb, ex)
-                           : extend_exact<kFind>(end, n, crow, dadj, arow, irow, fb, Fb, ex);
+            const uint64_t* crow = a.arena + 2 * uint64_t(pd.y);
+            const uint64_t* dadj = a.o.dadj + uint64_t(pd.w) * kMaxQueryNodes;
+            cnt = extend_literal<kFind>(end, n, crow, dadj, arow, irow, fb, Fb, mpb, ex);
           }
           if (cnt) {
             if (kFind) {
@@ -393,25 +298,20 @@ __global__ void __launch_bounds__(kCsWarps * 32) cs_join_kernel(CsArgs a) {
 
 }  // namespace
 
-cudaError_t launch_rec_of_gpos(const PairRec* recs, const Counters* ctr, uint64_t rec_cap, uint32_t* rec_of_gpos,
+cudaError_t launch_pos_desc(const PairRec* recs, const Counters* ctr, uint64_t rec_cap, const DGraphs& q, uint4* desc,
                                cudaStream_t st) {
   if (rec_cap == 0) return cudaSuccess;
-  cudaError_t e = cudaMemsetAsync(rec_of_gpos, 0xFF, sizeof(uint32_t) * rec_cap, st);
+  cudaError_t e = cudaMemsetAsync(desc, 0xFF, sizeof(uint4) * rec_cap, st);
   if (e != cudaSuccess) return e;
-  rec_of_gpos_kernel<<<sm_count() * 4, 256, 0, st>>>(recs, ctr, rec_cap, rec_of_gpos); note_launch();
+  pos_desc_kernel<<<sm_count() * 4, 256, 0, st>>>(recs, ctr, rec_cap, q, desc); note_launch();
   return cudaGetLastError();
 }
 
-cudaError_t launch_cs_join(const CsArgs& a, bool literal, bool find_first, cudaStream_t st) {
+cudaError_t launch_cs_join(const CsArgs& a, bool find_first, cudaStream_t st) {
   if (a.d.G == 0 || a.end == 0) return cudaSuccess;
   const int blocks = sm_count() * 8, threads = kCsWarps * 32;
-  if (literal) {
-    if (find_first) cs_join_kernel<true, true><<<blocks, threads, 0, st>>>(a);
-    else cs_join_kernel<true, false><<<blocks, threads, 0, st>>>(a);
-  } else {
-    if (find_first) cs_join_kernel<false, true><<<blocks, threads, 0, st>>>(a);
-    else cs_join_kernel<false, false><<<blocks, threads, 0, st>>>(a);
-  }
+  if (find_first) cs_join_kernel<true><<<blocks, threads, 0, st>>>(a);
+  else cs_join_kernel<false><<<blocks, threads, 0, st>>>(a);
   note_launch();
   return cudaGetLastError();
 }

@@ -451,6 +451,347 @@ __device__ __forceinline__ void step_inrow(Lane<T, W>& L, const JoinArgs& a, Sta
   after_step<T, W, kMode>(L, a, S);
 }
 
+// ----------------------------------------------------------- clustered join
+// The clustered join, EXACT semantics (the reference driver's --use-cs,
+// BMS2.cpp:218-296): joinPartialCandidates2 (isomorphism.hpp:1021-1178) finds
+// the prototype's matches, joinWithPartialMatches (:756-977) extends each with
+// every query of its data graph's GMCR row.  Here round 0 of the join is
+//   cs_enum_kernel: one warp per data graph; its lanes enumerate the matches
+//     of query 0 over its own candidate rows (each lane a share of the roots)
+//     and write one entry per (match, run of up to kCsMembers members) into
+//     the array of the graph's size class;
+//   cs_extend_kernel<K>: the class's entries by work stealing; a lane builds
+//     the match's prefix state once and starts the entry's members one after
+//     the other with the steps, refills and splits of the plain join (a
+//     member of the prototype's size counts one, a smaller one nothing).
+// Later rounds run the subtrees that long searches handed over, as for the
+// plain join.
+
+// EXACT candidates at depth j (plain order) given the path f[0..j-1] = `mapped`.
+template <typename T, int W>
+__device__ __forceinline__ Bits<T, W> cs_level(const uint64_t* crow, const uint64_t* dadj, const uint64_t* arow,
+                                               const uint64_t* irow, uint32_t j, const uint8_t* f, Bits<T, W> mapped) {
+  Bits<T, W> c = bandn(bload<T, W>(crow + 2 * uint64_t(j)), mapped);
+  Bits<T, W> pset = z<T, W>();
+  for (uint64_t pm = __ldg(reinterpret_cast<const unsigned long long*>(dadj) + j); pm; pm &= pm - 1) {
+    const uint32_t x = f[__ffsll((long long)pm) - 1];
+    c = band(c, bload<T, W>(arow + 2 * uint64_t(x)));
+    pset = bor(pset, bbit<T, W>(x));
+  }
+  const Bits<T, W> nset = bandn(mapped, pset);
+  Bits<T, W> res = z<T, W>();
+  for (Bits<T, W> r = c; bany(r); r = bclear_low(r)) {
+    const uint32_t v = blow(r);
+    if (!bany(band(bload<T, W>(irow + 2 * uint64_t(v)), nset))) res = bor(res, bbit<T, W>(v));
+  }
+  return res;
+}
+
+// A lane's enumeration of prototype matches.
+template <typename T, int W>
+struct CsEnum {
+  Bits<T, W> roots;   // roots not started yet
+  Bits<T, W> mapped;  // path nodes below the current depth
+  int t;              // current depth, -1: start the next root
+  bool done;
+  uint8_t f[kMaxQueryNodes];
+  Bits<T, W> F[kMaxQueryNodes];
+};
+
+// The next match into e.f[0..end-1]; false when the lane's roots are exhausted.
+template <typename T, int W>
+__device__ bool cs_next(CsEnum<T, W>& e, uint32_t end, const uint64_t* crow, const uint64_t* dadj,
+                        const uint64_t* arow, const uint64_t* irow, unsigned long long& exps) {
+  for (;;) {
+    if (e.t < 0) {
+      if (!bany(e.roots)) return false;
+      const uint32_t v0 = blow(e.roots);
+      e.roots = bclear_low(e.roots);
+      e.f[0] = uint8_t(v0);
+      ++exps;
+      if (end == 1) return true;
+      e.mapped = bbit<T, W>(v0);
+      e.F[1] = cs_level<T, W>(crow, dadj, arow, irow, 1, e.f, e.mapped);
+      e.t = 1;
+    }
+    int t = e.t;
+    if (!bany(e.F[t])) {  // frame t exhausted
+      if (t == 1) {
+        e.t = -1;
+        continue;
+      }
+      e.t = --t;
+      e.mapped = bandn(e.mapped, bbit<T, W>(e.f[t]));
+      continue;
+    }
+    const uint32_t v = blow(e.F[t]);
+    e.F[t] = bclear_low(e.F[t]);
+    e.f[t] = uint8_t(v);
+    ++exps;
+    if (uint32_t(t) + 1 == end) return true;
+    e.mapped = bor(e.mapped, bbit<T, W>(v));
+    e.F[t + 1] = cs_level<T, W>(crow, dadj, arow, irow, uint32_t(t) + 1, e.f, e.mapped);
+    e.t = t + 1;
+  }
+}
+
+__global__ void __launch_bounds__(256) cs_enum_kernel(JoinArgs a) {
+  using T = uint64_t;
+  constexpr int W = 2;
+  const uint32_t lane = lane_id();
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  const uint32_t end = a.cs_end, D = a.d.G;
+  CsEnum<T, W> E;
+  unsigned long long parts = 0, pexps = 0;
+  for (;;) {
+    uint32_t i = 0;
+    if (lane == 0) i = atomicAdd(&a.ctr->cs_ghead, 1u);
+    i = __shfl_sync(0xffffffffu, i, 0);
+    if (i >= D) break;
+    const uint32_t d = a.dperm[i];
+    const uint32_t d_start = a.d.goff[d], m = a.d.goff[d + 1] - d_start;
+    const uint32_t g0 = a.gmcr_off[d], vcount = a.gmcr_off[d + 1] - g0;
+    if (m == 0) continue;
+    const uint64_t* crow_p = nullptr;
+    B128 roots;
+    if (end == 1) {
+      roots = prototype_row(a.qs.frec, a.ds.frec, a.ds.R, a.dense, a.dense_w, a.q.goff[0], d_start, m);
+      if (vcount == 0) {  // nothing to extend: only the matches are counted
+        if (lane == 0) {
+          parts += b_pop(roots);
+          pexps += b_pop(roots);
+        }
+        continue;
+      }
+    } else {
+      // the prototype's own pair heads the row when it is valid (query ids ascend)
+      const uint4 p0 = vcount && g0 < a.rec_cap ? a.pos_desc[g0] : make_uint4(kNoRecord, 0, 0, 0);
+      if (p0.x == kNoRecord || p0.w != 0) continue;
+      crow_p = a.arena + 2 * uint64_t(p0.y);
+      roots = ld_b128(crow_p);
+    }
+    const int cls = m > 64 ? 2 : (m > 32 ? 1 : 0);
+    const uint32_t nchunk = (vcount + kCsMembers - 1) / kCsMembers;
+    uint8_t* out = a.cs_ent[cls];
+    const uint64_t* arow = a.ds.adj + 2 * uint64_t(d_start);
+    const uint64_t* irow = a.ds.adjin + 2 * uint64_t(d_start);
+    E.roots = z<T, W>();
+    {  // this lane's roots: every 32nd set bit from its rank on
+      uint32_t k = 0;
+      for (B128 r = roots; b_any(r); r = b_clear_low(r), ++k)
+        if ((k & 31u) == lane) E.roots = bor(E.roots, bbit<T, W>(b_low(r)));
+    }
+    E.t = -1;
+    E.done = !bany(E.roots);
+    while (!__all_sync(0xffffffffu, E.done)) {
+      bool got = false;
+      if (!E.done) {
+        got = cs_next<T, W>(E, end, crow_p, a.o.dadj, arow, irow, pexps);
+        E.done = !got;
+      }
+      const uint32_t bal = __ballot_sync(0xffffffffu, got);
+      if (!bal) continue;
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(&a.ctr->cs_n[cls], (unsigned long long)__popc(bal) * nchunk);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (got) {
+        ++parts;
+        const unsigned long long k0 = base + (unsigned long long)__popc(bal & lt_mask) * nchunk;
+        for (uint32_t c = 0; c < nchunk; ++c) {
+          if (k0 + c >= a.cs_cap) {
+            atomicOr(a.err, kErrOverflow);
+            break;
+          }
+          uint8_t* e = out + (k0 + c) * a.cs_stride;
+          *reinterpret_cast<CsEntry*>(e) = CsEntry{d, c * kCsMembers};
+          for (uint32_t t = 0; t < end; ++t) e[sizeof(CsEntry) + t] = E.f[t];
+        }
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    parts += __shfl_down_sync(0xffffffffu, parts, o);
+    pexps += __shfl_down_sync(0xffffffffu, pexps, o);
+  }
+  if (lane == 0) {
+    if (parts) atomicAdd(&a.ctr->partials, parts);
+    if (pexps) {
+      atomicAdd(&a.ctr->partial_exps, pexps);
+      atomicAdd(&a.ctr->expansions, pexps);
+    }
+  }
+}
+
+// A lane's clustered work: members [j, jend) of the graph's GMCR row against
+// one match.  The prefix state (S.f, S.row, planes and mapped at depth `end`)
+// is built once per entry and survives every search that ends at depth `end`.
+struct CsWork {
+  uint32_t j, jend;
+  bool ready;  // the lane's prefix state is the entry's
+};
+
+template <typename T, int W, bool kCounted>
+__device__ __forceinline__ void cs_prefix(Lane<T, W>& L, Stack<T, W>& S, uint32_t end, const uint8_t* pre,
+                                          const uint64_t* arow) {
+  L.mapped = z<T, W>();
+#pragma unroll
+  for (int b = 0; b < kPlanes; ++b) L.P.p[b] = z<T, W>();
+  for (uint32_t j = 0; j < end; ++j) {
+    const uint32_t x = pre[j];
+    S.f[j] = uint8_t(x);
+    L.mapped = bor(L.mapped, bbit<T, W>(x));
+    if constexpr (kCounted) {
+      const Bits<T, W> row = bload<T, W>(arow + 2 * uint64_t(x));
+      S.row[j] = row;
+      padd(L.P, row);
+    }
+  }
+}
+
+// Start the lane on the next member of its work whose search needs a lane;
+// members of the prototype's size are counted, members with no candidate at
+// depth `end` (or whose depth `end` is the leaf level) are settled on the way.
+template <typename T, int W, bool kCounted, int kMode>
+__device__ void cs_next_member(Lane<T, W>& L, Stack<T, W>& S, CsWork& w, const JoinArgs& a, const uint8_t* pre,
+                               uint32_t g0, uint32_t d_start) {
+  constexpr bool kFindFirst = kMode == kModeFind, kLogVertices = kMode == kModeLog;
+  const uint32_t end = a.cs_end;
+  const uint64_t* arow = a.ds.adj + 2 * uint64_t(d_start);
+  if (L.t != L.base) w.ready = false;  // the last search stopped below the prefix: rebuild
+  while (w.j < w.jend) {
+    const uint32_t j = w.j++;
+    if (uint64_t(g0) + j >= a.rec_cap) continue;
+    const uint4 pd = a.pos_desc[g0 + j];  // {record, first row, query nodes, query}
+    const uint32_t rec = pd.x, n = pd.z;
+    if (rec == kNoRecord) continue;
+    if (n < end) continue;
+    if (kFindFirst && (*(volatile const uint32_t*)&a.pair_flag[rec] & 1u)) continue;
+    if (n == end) {
+      atomicAdd(&a.pair_count[rec], 1ull);
+      if (kFindFirst) atomicOr(&a.pair_flag[rec], 1u);
+      continue;
+    }
+    if (!w.ready) {
+      cs_prefix<T, W, kCounted>(L, S, end, pre, arow);
+      L.t = L.base = int(end);
+      w.ready = true;
+    }
+    L.crow = a.arena + 2 * uint64_t(pd.y);
+    L.perm = a.o.perm + uint64_t(pd.w) * kMaxQueryNodes;
+    L.dadj = a.o.dadj + uint64_t(pd.w) * kMaxQueryNodes;
+    Bits<T, W> c;
+    if constexpr (kCounted) {
+      const uint64_t dm = __ldg(reinterpret_cast<const unsigned long long*>(L.dadj) + end);
+      c = bandn(bload<T, W>(L.crow + 2 * uint64_t(__ldg(L.perm + end))), L.mapped);
+      for (uint64_t pm = dm; pm && bany(c); pm &= pm - 1) c = band(c, S.row[__ffsll((long long)pm) - 1]);
+      const uint32_t k = uint32_t(__popcll(dm));
+      if (bany(c)) c = k < (1u << kPlanes) ? band(c, peq_added(L.P, z<T, W>(), k)) : z<T, W>();
+    } else {
+      c = cs_level<T, W>(L.crow, L.dadj, arow, a.ds.adjin + 2 * uint64_t(d_start), end, S.f, L.mapped);
+    }
+    if (!bany(c)) continue;  // no branch root: nothing to count, no expansion
+    if (end + 1 == n) {      // depth `end` is the leaf level
+      const uint32_t pc = bpop(c);
+      atomicAdd(&a.pair_count[rec], (unsigned long long)pc);
+      atomicAdd(&a.pair_exp[rec], (unsigned long long)pc);
+      if (kFindFirst) atomicOr(&a.pair_flag[rec], 1u);
+      continue;
+    }
+    L.rec = rec;
+    L.qoff = a.q.goff[pd.w];
+    L.n = n;
+    L.arow = arow;
+    L.irow = a.ds.adjin + 2 * uint64_t(d_start);
+    L.cnt = 0;
+    L.exps = 0;
+    L.since_check = 0;
+    L.no_split = false;
+    L.vis = z<T, W>();
+    L.mpset = 0;
+    if (kLogVertices)
+      for (uint32_t t = 0; t < n; ++t) S.expd[t] = 0;
+    L.cur = c;
+    L.active = true;
+    return;
+  }
+}
+
+template <int K, bool kCounted, int kMode>
+__global__ void __launch_bounds__(256) cs_extend_kernel(JoinArgs a) {
+  using T = typename std::conditional<K == 0, uint32_t, uint64_t>::type;
+  constexpr int W = K == 2 ? 2 : 1;
+  const bool counted_applies = *a.ds.maxin < (1u << kPlanes);
+  if (counted_applies != kCounted) return;  // the other variant runs this class
+  const uint32_t lane = lane_id();
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  const unsigned long long ntasks = min((unsigned long long)a.cs_cap, a.ctr->cs_n[K]);
+  if (ntasks == 0) return;
+  const uint8_t* ent = a.cs_ent[K];
+  unsigned long long* head = &a.ctr->join_head[0][K];
+  const unsigned long long nwarps = (unsigned long long)(gridDim.x * blockDim.x) >> 5;
+  Lane<T, W> L;
+  L.active = false;
+  L.done_fetching = false;
+  L.t = L.base = 0;
+  Stack<T, W> S;
+  CsWork w{0, 0, false};
+  const uint8_t* pre = nullptr;
+  uint32_t g0 = 0, d_start = 0;
+  unsigned long long qbase = 0, qend = 0;  // this warp's chunk of the queue (warp-uniform)
+  bool queue_empty = false;
+  for (;;) {
+    uint32_t need = __ballot_sync(0xffffffffu, !L.active && w.j >= w.jend && !L.done_fetching);
+    while (need) {
+      if (qbase >= qend) {
+        if (queue_empty) break;
+        unsigned long long base = 0, chunk = 0;
+        if (lane == 0) {
+          const unsigned long long h = *(volatile const unsigned long long*)head;
+          const unsigned long long left = h < ntasks ? ntasks - h : 0;
+          chunk = left / (8 * nwarps);  // entries carry up to 32 members: small chunks
+          chunk = chunk < 4 ? 4 : (chunk > 32 ? 32 : chunk);
+          base = atomicAdd(head, chunk);
+        }
+        base = __shfl_sync(0xffffffffu, base, 0);
+        chunk = __shfl_sync(0xffffffffu, chunk, 0);
+        qbase = base < ntasks ? base : ntasks;
+        qend = base + chunk < ntasks ? base + chunk : ntasks;
+        if (qbase >= qend) {
+          queue_empty = true;
+          break;
+        }
+      }
+      const unsigned long long avail = qend - qbase;
+      const uint32_t rank = __popc(need & lt_mask);
+      const uint32_t took = uint64_t(__popc(need)) < avail ? uint32_t(__popc(need)) : uint32_t(avail);
+      if (((need >> lane) & 1u) && rank < avail) {
+        const uint8_t* e = ent + (qbase + rank) * a.cs_stride;
+        const CsEntry h = *reinterpret_cast<const CsEntry*>(e);
+        pre = e + sizeof(CsEntry);
+        d_start = a.d.goff[h.d];
+        g0 = a.gmcr_off[h.d];
+        w.j = h.j0;
+        w.jend = min(a.gmcr_off[h.d + 1] - g0, h.j0 + kCsMembers);
+        w.ready = false;
+        cs_next_member<T, W, kCounted, kMode>(L, S, w, a, pre, g0, d_start);
+      }
+      qbase += took;
+      need = __ballot_sync(0xffffffffu, !L.active && w.j >= w.jend && !L.done_fetching);
+    }
+    if (queue_empty && !L.active && w.j >= w.jend) L.done_fetching = true;
+    if (__all_sync(0xffffffffu, !L.active && w.j >= w.jend && L.done_fetching)) break;
+    for (int s = 0; s < a.steps; ++s) {
+      if (L.active) {
+        if constexpr (kCounted) step_counted<T, W, kMode>(L, a, S);
+        else step_inrow<T, W, kMode>(L, a, S);
+      }
+      if (!L.active && w.j < w.jend) cs_next_member<T, W, kCounted, kMode>(L, S, w, a, pre, g0, d_start);
+      const uint32_t idle = __ballot_sync(0xffffffffu, !L.active && w.j >= w.jend && !L.done_fetching);
+      if (__popc(idle) >= a.refill || (idle && !__any_sync(0xffffffffu, L.active || w.j < w.jend))) break;
+    }
+  }
+}
+
 // Record class K: 2 = data graphs of 65..128 nodes (two 64-bit words), 1 =
 // 33..64 nodes (one 64-bit word), 0 = up to 32 nodes (one 32-bit word).
 // kCounted selects the counted test (EXACT, in-degrees <= 7) or the in-row test.
@@ -600,6 +941,15 @@ __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
 
 template <int K, int kMode>
 cudaError_t launch_mode(const JoinArgs& a, int blocks, int threads, cudaStream_t st) {
+  if constexpr (kMode != kModeLog) {
+    if (a.cs_end && a.round == 0) {  // the clustered entries of this class
+      cs_extend_kernel<K, true, kMode><<<blocks, threads, 0, st>>>(a); note_launch();
+      const cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+      cs_extend_kernel<K, false, kMode><<<blocks, threads, 0, st>>>(a); note_launch();
+      return cudaGetLastError();
+    }
+  }
   if (!a.literal) {
     join_kernel<K, true, kMode><<<blocks, threads, 0, st>>>(a); note_launch();
     const cudaError_t e = cudaGetLastError();
@@ -625,6 +975,10 @@ cudaError_t launch_join(const JoinArgs& args, const ClassLaunch cl[3], cudaStrea
   const int rounds = splits ? kJoinRounds : 1;
   cudaError_t e = cudaSuccess;
   for (int r = 0; r < rounds && e == cudaSuccess; ++r) {
+    if (r == 0 && args.cs_end) {  // clustered join: the prototype's matches first
+      cs_enum_kernel<<<sm_count() * 8, 256, 0, st>>>(args); note_launch();
+      e = cudaGetLastError();
+    }
     for (int k = 2; k >= 0 && e == cudaSuccess; --k) {
       JoinArgs a = args;
       a.round = r;

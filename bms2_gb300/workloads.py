@@ -117,15 +117,38 @@ def _find_induced(p_lab, p_adj, lab, rows, cap: int = 20000):
     return list(assign) if rec(0) else None
 
 
+def _find_ring(lab, rows, label: int = 8, sizes=(6, 5)):
+    """A chordless ring of `label` atoms (6 atoms, else 5) in ring order, or None."""
+    adj = [set(r) for r in rows]
+    for size in sizes:
+        for s in range(len(lab)):
+            if lab[s] != label:
+                continue
+            stack = [[s]]
+            while stack:
+                path = stack.pop()
+                u = path[-1]
+                if len(path) == size:
+                    if s in adj[u] and all(path[j] not in adj[path[i]] for i in range(size)
+                                           for j in range(i + 2, size) if not (i == 0 and j == size - 1)):
+                        return path
+                    continue
+                stack.extend(path + [w] for w in sorted(adj[u]) if w > s and w not in path and lab[w] == label)
+    return None
+
+
 def make_cluster(data: Graphs, n_members: int, seed: int, proto_nodes: tuple[int, int] = (5, 8),
-                 extra_nodes: tuple[int, int] = (1, 12), n_sources: int = 24) -> Graphs:
+                 extra_nodes: tuple[int, int] = (1, 12), n_sources: int = 24, proto: str = "grow") -> Graphs:
     """A query cluster in the layout of the reference's cluster files
-    (generate_cs.py:338-362, 555-577): graph 0 is the prototype P, a connected
-    induced subgraph of a random data graph numbered in discovery order; each
-    member is P plus 1..12 further atoms grown around an induced occurrence of P
-    in one of up to n_sources data graphs, with P's nodes first, in P's order.
-    (The reference clusters real molecules by maximum common substructure with
-    rdkit, which is absent here; this keeps its file convention.)"""
+    (generate_cs.py:338-362, 555-577): graph 0 is the prototype P; each member
+    is P plus 1..12 further atoms grown around an induced occurrence of P in one
+    of up to n_sources data graphs, with P's nodes first, in P's order.
+    proto="grow": P is a connected induced subgraph of proto_nodes atoms of a
+    random data graph, numbered in discovery order; proto="ring": P is a
+    chordless carbon ring of 6 (else 5) atoms in ring order, the reference's
+    pure-ring clusters (generate_cs.py:259, 323: listed first).  (The reference
+    clusters real molecules by maximum common substructure with rdkit, which is
+    absent here; this keeps its file convention.)"""
     import numpy as np
 
     rng = np.random.default_rng(seed)
@@ -136,10 +159,24 @@ def make_cluster(data: Graphs, n_members: int, seed: int, proto_nodes: tuple[int
     want = proto_nodes[1] + extra_nodes[1]
     big = np.nonzero(sizes >= want)[0]
     pool = big if len(big) else np.array([int(np.argmax(sizes))])
-    g0 = int(pool[int(rng.integers(len(pool)))])
-    lab0, rows0, el0 = _graph_at(v, g0)
-    p = int(rng.integers(proto_nodes[0], proto_nodes[1] + 1))
-    proto = _grow(rng, rows0, [int(rng.integers(len(lab0)))], p - 1)
+    if proto == "ring":
+        ring = None
+        for g in rng.permutation(pool)[:2000]:
+            g0 = int(g)
+            lab0, rows0, el0 = _graph_at(v, g0)
+            ring = _find_ring(lab0, rows0)
+            if ring is not None:
+                break
+        if ring is None:
+            raise ValueError("no carbon ring of 5 or 6 atoms in the sampled data graphs")
+        proto_list = ring
+    else:
+        g0 = int(pool[int(rng.integers(len(pool)))])
+        lab0, rows0, el0 = _graph_at(v, g0)
+        p = int(rng.integers(proto_nodes[0], proto_nodes[1] + 1))
+        proto_list = _grow(rng, rows0, [int(rng.integers(len(lab0)))], p - 1)
+    proto = proto_list
+    p = len(proto)
     p_lab = [lab0[u] for u in proto]
     pos = {u: i for i, u in enumerate(proto)}
     p_adj = [{pos[w] for w in rows0[u] if w in pos} for u in proto]

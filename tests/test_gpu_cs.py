@@ -68,6 +68,15 @@ def test_fused_clustered_join_bit_exact(cs, cluster, R, mode, sem):
     assert want.n_partial > 0 and want.total > 0
 
 
+@pytest.mark.parametrize("R", [2, 6])
+@pytest.mark.parametrize("mode,sem", MODES)
+def test_ring_prototype_cluster_bit_exact(cs, R, mode, sem):
+    d = Graphs.synth_molecules(800, 23, 0, 0, 0, 6, 110, 1, 4)
+    c = workloads.make_cluster(d, 30, 23, proto="ring")
+    want = check(cs, c, d, R, mode, sem)
+    assert want.n_partial > 0 and want.total > 0
+
+
 @pytest.mark.parametrize("mode,sem", MODES)
 def test_staged_clustered_join_bit_exact(cs, cluster, mode, sem):
     q, d = cluster

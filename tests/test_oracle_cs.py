@@ -74,6 +74,20 @@ def test_exact_clustered_equals_plain_join_at_two_refine_steps(seed):
         assert int(b.expansions.sum()) + b.partial_exps < int(a.expansions.sum())
 
 
+def test_ring_prototype_cluster():
+    # a pure carbon ring prototype (the reference's ring clusters): its members
+    # keep the ring first, and the shared ring search halves the work
+    _, d = workloads.make("mol1k", 3, n_data=600, n_queries=2)
+    c = workloads.make_cluster(d, 30, 5, proto="ring")
+    a = c.arrays()
+    p = int(a["graph_offsets"][1])
+    assert p in (5, 6) and (a["node_labels"][:p] == 8).all()
+    x = oracle.run_pipeline(c, d, 2)
+    y = oracle.run_pipeline(c, d, 2, cs=True)
+    assert np.array_equal(x.counts, y.counts) and y.total > 0
+    assert int(y.expansions.sum()) + y.partial_exps < int(x.expansions.sum())
+
+
 def test_find_first_is_existence_of_a_clustered_match():
     _, d = workloads.make("mol1k", 5, n_data=300, n_queries=2)
     c = workloads.make_cluster(d, 25, 5, proto_nodes=(3, 5))

@@ -15,6 +15,7 @@
 //   - candidate range count / select candidates.hpp:82-158
 //   - GMCR mapping                   gmcr.hpp:35-144
 //   - join                           isomorphism.hpp:268-288, 291-472
+//   - clustered join (--use-cs)      isomorphism.hpp:756-977, 1021-1178, BMS2.cpp:218-296
 //   - embeddings of one pair         (no reference counterpart; the join's DFS
 //                                     in EXACT semantics, writing each mapping)
 //

@@ -460,10 +460,11 @@ __device__ __forceinline__ void step_inrow(Lane<T, W>& L, const JoinArgs& a, Sta
 //     of query 0 over its own candidate rows (each lane a share of the roots)
 //     and write one entry per (match, run of up to kCsMembers members) into
 //     the array of the graph's size class;
-//   cs_extend_kernel<K>: the class's entries by work stealing; a lane builds
-//     the match's prefix state once and starts the entry's members one after
-//     the other with the steps, refills and splits of the plain join (a
-//     member of the prototype's size counts one, a smaller one nothing).
+//   cs_extend_kernel<K>: the class's entries by work stealing; the members of
+//     a warp's current entry go to its idle lanes as consecutive items, each
+//     lane builds the match's prefix state and starts its member with the
+//     steps, refills and splits of the plain join (a member of the prototype's
+//     size counts one, a smaller one nothing).
 // Later rounds run the subtrees that long searches handed over, as for the
 // plain join.
 
@@ -622,14 +623,9 @@ __global__ void __launch_bounds__(256) cs_enum_kernel(JoinArgs a) {
   }
 }
 
-// A lane's clustered work: members [j, jend) of the graph's GMCR row against
-// one match.  The prefix state (S.f, S.row, planes and mapped at depth `end`)
-// is built once per entry and survives every search that ends at depth `end`.
-struct CsWork {
-  uint32_t j, jend;
-  bool ready;  // the lane's prefix state is the entry's
-};
-
+// The prefix state of a match at depth `end` (S.f, S.row, counting planes,
+// mapped).  Built by every lane that starts a member of the entry; lanes of a
+// warp take consecutive members of the same entry, so they load the same rows.
 template <typename T, int W, bool kCounted>
 __device__ __forceinline__ void cs_prefix(Lane<T, W>& L, Stack<T, W>& S, uint32_t end, const uint8_t* pre,
                                           const uint64_t* arow) {
@@ -648,74 +644,75 @@ __device__ __forceinline__ void cs_prefix(Lane<T, W>& L, Stack<T, W>& S, uint32_
   }
 }
 
-// Start the lane on the next member of its work whose search needs a lane;
-// members of the prototype's size are counted, members with no candidate at
-// depth `end` (or whose depth `end` is the leaf level) are settled on the way.
+// Member j of the graph's GMCR row against the entry's match: a query of the
+// prototype's size counts one; otherwise depth `end` is computed with the
+// lane's test and, when it holds candidates, the lane starts the search there
+// (a leaf-level depth `end` is counted at once).  `held` is the entry whose
+// prefix state the lane holds (kNoRecord: none).
 template <typename T, int W, bool kCounted, int kMode>
-__device__ void cs_next_member(Lane<T, W>& L, Stack<T, W>& S, CsWork& w, const JoinArgs& a, const uint8_t* pre,
-                               uint32_t g0, uint32_t d_start) {
+__device__ __forceinline__ void cs_start_member(Lane<T, W>& L, Stack<T, W>& S, uint32_t& held, const JoinArgs& a,
+                                                uint32_t entry, const uint8_t* pre, uint32_t g0, uint32_t j,
+                                                uint32_t d_start) {
   constexpr bool kFindFirst = kMode == kModeFind, kLogVertices = kMode == kModeLog;
   const uint32_t end = a.cs_end;
-  const uint64_t* arow = a.ds.adj + 2 * uint64_t(d_start);
-  if (L.t != L.base) w.ready = false;  // the last search stopped below the prefix: rebuild
-  while (w.j < w.jend) {
-    const uint32_t j = w.j++;
-    if (uint64_t(g0) + j >= a.rec_cap) continue;
-    const uint4 pd = a.pos_desc[g0 + j];  // {record, first row, query nodes, query}
-    const uint32_t rec = pd.x, n = pd.z;
-    if (rec == kNoRecord) continue;
-    if (n < end) continue;
-    if (kFindFirst && (*(volatile const uint32_t*)&a.pair_flag[rec] & 1u)) continue;
-    if (n == end) {
-      atomicAdd(&a.pair_count[rec], 1ull);
-      if (kFindFirst) atomicOr(&a.pair_flag[rec], 1u);
-      continue;
-    }
-    if (!w.ready) {
-      cs_prefix<T, W, kCounted>(L, S, end, pre, arow);
-      L.t = L.base = int(end);
-      w.ready = true;
-    }
-    L.crow = a.arena + 2 * uint64_t(pd.y);
-    L.perm = a.o.perm + uint64_t(pd.w) * kMaxQueryNodes;
-    L.dadj = a.o.dadj + uint64_t(pd.w) * kMaxQueryNodes;
-    Bits<T, W> c;
-    if constexpr (kCounted) {
-      const uint64_t dm = __ldg(reinterpret_cast<const unsigned long long*>(L.dadj) + end);
-      c = bandn(bload<T, W>(L.crow + 2 * uint64_t(__ldg(L.perm + end))), L.mapped);
-      for (uint64_t pm = dm; pm && bany(c); pm &= pm - 1) c = band(c, S.row[__ffsll((long long)pm) - 1]);
-      const uint32_t k = uint32_t(__popcll(dm));
-      if (bany(c)) c = k < (1u << kPlanes) ? band(c, peq_added(L.P, z<T, W>(), k)) : z<T, W>();
-    } else {
-      c = cs_level<T, W>(L.crow, L.dadj, arow, a.ds.adjin + 2 * uint64_t(d_start), end, S.f, L.mapped);
-    }
-    if (!bany(c)) continue;  // no branch root: nothing to count, no expansion
-    if (end + 1 == n) {      // depth `end` is the leaf level
-      const uint32_t pc = bpop(c);
-      atomicAdd(&a.pair_count[rec], (unsigned long long)pc);
-      atomicAdd(&a.pair_exp[rec], (unsigned long long)pc);
-      if (kFindFirst) atomicOr(&a.pair_flag[rec], 1u);
-      continue;
-    }
-    L.rec = rec;
-    L.qoff = a.q.goff[pd.w];
-    L.n = n;
-    L.arow = arow;
-    L.irow = a.ds.adjin + 2 * uint64_t(d_start);
-    L.cnt = 0;
-    L.exps = 0;
-    L.since_check = 0;
-    L.no_split = false;
-    L.vis = z<T, W>();
-    L.mpset = 0;
-    if (kLogVertices)
-      for (uint32_t t = 0; t < n; ++t) S.expd[t] = 0;
-    L.cur = c;
-    L.active = true;
+  if (uint64_t(g0) + j >= a.rec_cap) return;
+  const uint4 pd = a.pos_desc[g0 + j];  // {record, first row, query nodes, query}
+  const uint32_t rec = pd.x, n = pd.z;
+  if (rec == kNoRecord || n < end) return;
+  if (kFindFirst && (*(volatile const uint32_t*)&a.pair_flag[rec] & 1u)) return;
+  if (n == end) {
+    atomicAdd(&a.pair_count[rec], 1ull);
+    if (kFindFirst) atomicOr(&a.pair_flag[rec], 1u);
     return;
   }
+  const uint64_t* arow = a.ds.adj + 2 * uint64_t(d_start);
+  if (held != entry || L.t != L.base) {  // another match, or a search that stopped below the prefix
+    cs_prefix<T, W, kCounted>(L, S, end, pre, arow);
+    L.t = L.base = int(end);
+    held = entry;
+  }
+  L.crow = a.arena + 2 * uint64_t(pd.y);
+  L.perm = a.o.perm + uint64_t(pd.w) * kMaxQueryNodes;
+  L.dadj = a.o.dadj + uint64_t(pd.w) * kMaxQueryNodes;
+  Bits<T, W> c;
+  if constexpr (kCounted) {
+    const uint64_t dm = __ldg(reinterpret_cast<const unsigned long long*>(L.dadj) + end);
+    c = bandn(bload<T, W>(L.crow + 2 * uint64_t(__ldg(L.perm + end))), L.mapped);
+    for (uint64_t pm = dm; pm; pm &= pm - 1) c = band(c, S.row[__ffsll((long long)pm) - 1]);
+    const uint32_t k = uint32_t(__popcll(dm));
+    c = k < (1u << kPlanes) ? band(c, peq_added(L.P, z<T, W>(), k)) : z<T, W>();
+  } else {
+    c = cs_level<T, W>(L.crow, L.dadj, arow, a.ds.adjin + 2 * uint64_t(d_start), end, S.f, L.mapped);
+  }
+  if (!bany(c)) return;  // no branch root: nothing to count, no expansion
+  if (end + 1 == n) {    // depth `end` is the leaf level
+    const uint32_t pc = bpop(c);
+    atomicAdd(&a.pair_count[rec], (unsigned long long)pc);
+    atomicAdd(&a.pair_exp[rec], (unsigned long long)pc);
+    if (kFindFirst) atomicOr(&a.pair_flag[rec], 1u);
+    return;
+  }
+  L.rec = rec;
+  L.qoff = a.q.goff[pd.w];
+  L.n = n;
+  L.arow = arow;
+  L.irow = a.ds.adjin + 2 * uint64_t(d_start);
+  L.cnt = 0;
+  L.exps = 0;
+  L.since_check = 0;
+  L.no_split = false;
+  L.vis = z<T, W>();
+  L.mpset = 0;
+  if (kLogVertices)
+    for (uint32_t t = 0; t < n; ++t) S.expd[t] = 0;
+  L.cur = c;
+  L.active = true;
 }
 
+// The class's entries by chunked work stealing.  The warp walks its entries
+// one at a time; the members of the current entry go to the lanes that need
+// work as consecutive items, so those lanes build the same prefix and test
+// their members side by side.
 template <int K, bool kCounted, int kMode>
 __global__ void __launch_bounds__(256) cs_extend_kernel(JoinArgs a) {
   using T = typename std::conditional<K == 0, uint32_t, uint64_t>::type;
@@ -734,60 +731,64 @@ __global__ void __launch_bounds__(256) cs_extend_kernel(JoinArgs a) {
   L.done_fetching = false;
   L.t = L.base = 0;
   Stack<T, W> S;
-  CsWork w{0, 0, false};
-  const uint8_t* pre = nullptr;
-  uint32_t g0 = 0, d_start = 0;
-  unsigned long long qbase = 0, qend = 0;  // this warp's chunk of the queue (warp-uniform)
+  uint32_t held = kNoRecord;
+  // warp-uniform: this warp's chunk of the queue and the entry being handed out
+  unsigned long long qbase = 0, qend = 0;
   bool queue_empty = false;
+  uint32_t e_id = 0, e_g0 = 0, e_j0 = 0, e_dstart = 0, nmem = 0, m = 0;
+  const uint8_t* e_pre = nullptr;
   for (;;) {
-    uint32_t need = __ballot_sync(0xffffffffu, !L.active && w.j >= w.jend && !L.done_fetching);
+    uint32_t need = __ballot_sync(0xffffffffu, !L.active && !L.done_fetching);
     while (need) {
-      if (qbase >= qend) {
-        if (queue_empty) break;
-        unsigned long long base = 0, chunk = 0;
-        if (lane == 0) {
-          const unsigned long long h = *(volatile const unsigned long long*)head;
-          const unsigned long long left = h < ntasks ? ntasks - h : 0;
-          chunk = left / (8 * nwarps);  // entries carry up to 32 members: small chunks
-          chunk = chunk < 4 ? 4 : (chunk > 32 ? 32 : chunk);
-          base = atomicAdd(head, chunk);
-        }
-        base = __shfl_sync(0xffffffffu, base, 0);
-        chunk = __shfl_sync(0xffffffffu, chunk, 0);
-        qbase = base < ntasks ? base : ntasks;
-        qend = base + chunk < ntasks ? base + chunk : ntasks;
+      if (m >= nmem) {  // the next entry
         if (qbase >= qend) {
-          queue_empty = true;
-          break;
+          if (queue_empty) break;
+          unsigned long long base = 0, chunk = 0;
+          if (lane == 0) {
+            const unsigned long long h = *(volatile const unsigned long long*)head;
+            const unsigned long long left = h < ntasks ? ntasks - h : 0;
+            chunk = left / (8 * nwarps);
+            chunk = chunk < 1 ? 1 : (chunk > 16 ? 16 : chunk);
+            base = atomicAdd(head, chunk);
+          }
+          base = __shfl_sync(0xffffffffu, base, 0);
+          chunk = __shfl_sync(0xffffffffu, chunk, 0);
+          qbase = base < ntasks ? base : ntasks;
+          qend = base + chunk < ntasks ? base + chunk : ntasks;
+          if (qbase >= qend) {
+            queue_empty = true;
+            break;
+          }
         }
-      }
-      const unsigned long long avail = qend - qbase;
-      const uint32_t rank = __popc(need & lt_mask);
-      const uint32_t took = uint64_t(__popc(need)) < avail ? uint32_t(__popc(need)) : uint32_t(avail);
-      if (((need >> lane) & 1u) && rank < avail) {
-        const uint8_t* e = ent + (qbase + rank) * a.cs_stride;
+        const uint8_t* e = ent + qbase * a.cs_stride;
         const CsEntry h = *reinterpret_cast<const CsEntry*>(e);
-        pre = e + sizeof(CsEntry);
-        d_start = a.d.goff[h.d];
-        g0 = a.gmcr_off[h.d];
-        w.j = h.j0;
-        w.jend = min(a.gmcr_off[h.d + 1] - g0, h.j0 + kCsMembers);
-        w.ready = false;
-        cs_next_member<T, W, kCounted, kMode>(L, S, w, a, pre, g0, d_start);
+        e_id = uint32_t(qbase);
+        e_pre = e + sizeof(CsEntry);
+        e_dstart = a.d.goff[h.d];
+        e_g0 = a.gmcr_off[h.d];
+        e_j0 = h.j0;
+        nmem = min(a.gmcr_off[h.d + 1] - e_g0 - h.j0, kCsMembers);
+        m = 0;
+        ++qbase;
+        continue;
       }
-      qbase += took;
-      need = __ballot_sync(0xffffffffu, !L.active && w.j >= w.jend && !L.done_fetching);
+      const uint32_t left = nmem - m;
+      const uint32_t rank = __popc(need & lt_mask);
+      const uint32_t took = uint32_t(__popc(need)) < left ? uint32_t(__popc(need)) : left;
+      if (((need >> lane) & 1u) && rank < left)
+        cs_start_member<T, W, kCounted, kMode>(L, S, held, a, e_id, e_pre, e_g0, e_j0 + m + rank, e_dstart);
+      m += took;
+      need = __ballot_sync(0xffffffffu, !L.active && !L.done_fetching);
     }
-    if (queue_empty && !L.active && w.j >= w.jend) L.done_fetching = true;
-    if (__all_sync(0xffffffffu, !L.active && w.j >= w.jend && L.done_fetching)) break;
+    if (queue_empty && m >= nmem && !L.active) L.done_fetching = true;
+    if (__all_sync(0xffffffffu, !L.active && L.done_fetching)) break;
     for (int s = 0; s < a.steps; ++s) {
       if (L.active) {
         if constexpr (kCounted) step_counted<T, W, kMode>(L, a, S);
         else step_inrow<T, W, kMode>(L, a, S);
       }
-      if (!L.active && w.j < w.jend) cs_next_member<T, W, kCounted, kMode>(L, S, w, a, pre, g0, d_start);
-      const uint32_t idle = __ballot_sync(0xffffffffu, !L.active && w.j >= w.jend && !L.done_fetching);
-      if (__popc(idle) >= a.refill || (idle && !__any_sync(0xffffffffu, L.active || w.j < w.jend))) break;
+      const uint32_t idle = __ballot_sync(0xffffffffu, !L.active && !L.done_fetching);
+      if (__popc(idle) >= a.refill || (idle && !__any_sync(0xffffffffu, L.active))) break;
     }
   }
 }

@@ -138,7 +138,8 @@ def _find_ring(lab, rows, label: int = 8, sizes=(6, 5)):
 
 
 def make_cluster(data: Graphs, n_members: int, seed: int, proto_nodes: tuple[int, int] = (5, 8),
-                 extra_nodes: tuple[int, int] = (1, 12), n_sources: int = 24, proto: str = "grow") -> Graphs:
+                 extra_nodes: tuple[int, int] = (1, 12), n_sources: int = 24, proto: str = "grow",
+                 source_graphs: int = 100_000) -> Graphs:
     """A query cluster in the layout of the reference's cluster files
     (generate_cs.py:338-362, 555-577): graph 0 is the prototype P; each member
     is P plus 1..12 further atoms grown around an induced occurrence of P in one
@@ -148,14 +149,16 @@ def make_cluster(data: Graphs, n_members: int, seed: int, proto_nodes: tuple[int
     chordless carbon ring of 6 (else 5) atoms in ring order, the reference's
     pure-ring clusters (generate_cs.py:259, 323: listed first).  (The reference
     clusters real molecules by maximum common substructure with rdkit, which is
-    absent here; this keeps its file convention.)"""
+    absent here; this keeps its file convention.)  The prototype and its
+    occurrences come from the first `source_graphs` data graphs, so any prefix of
+    the same data set at least that long yields the same cluster."""
     import numpy as np
 
     rng = np.random.default_rng(seed)
     v = data.view()
-    G = v.n_graphs
-    go = np.ctypeslib.as_array(v.graph_offsets, shape=(G + 1,))
-    sizes = go[1:].astype(np.int64) - go[:-1]
+    go = np.ctypeslib.as_array(v.graph_offsets, shape=(v.n_graphs + 1,))
+    G = min(v.n_graphs, source_graphs)
+    sizes = go[1:G + 1].astype(np.int64) - go[:G]
     want = proto_nodes[1] + extra_nodes[1]
     big = np.nonzero(sizes >= want)[0]
     pool = big if len(big) else np.array([int(np.argmax(sizes))])

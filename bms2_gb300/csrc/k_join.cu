@@ -239,7 +239,6 @@ struct Stack {
   uint8_t f[kMaxQueryNodes];         // node mapped at each depth
   uint8_t mp[kMaxQueryNodes];        // REFERENCE_DFS: mapping[] as the reference writes it
   Bits<T, W> F[kMaxQueryNodes];      // candidates left in each frame
-  Bits<T, W> row[kMaxQueryNodes];    // counted test: row of f[depth]
   uint32_t expd[kMaxQueryNodes];     // per-depth expansions (logging)
 };
 
@@ -328,7 +327,7 @@ __device__ __forceinline__ void step_counted(Lane<T, W>& L, const JoinArgs& a, S
     --t;
     L.cur = S.F[t];
     L.mapped = bandn(L.mapped, bbit<T, W>(S.f[t]));  // back in frame t: its node leaves the path
-    psub(L.P, S.row[t]);
+    psub(L.P, bload<T, W>(L.arow + 2 * uint64_t(S.f[t])));
   }
   L.t = t;
   const uint32_t v = blow(L.cur);
@@ -340,7 +339,8 @@ __device__ __forceinline__ void step_counted(Lane<T, W>& L, const JoinArgs& a, S
   const Bits<T, W> mapped = bor(L.mapped, bbit<T, W>(v));
   c = bandn(c, mapped);
   if ((dm >> t) & 1ull) c = band(c, row);
-  for (uint64_t pm = dm & ~(uint64_t(1) << t); pm; pm &= pm - 1) c = band(c, S.row[__ffsll((long long)pm) - 1]);
+  for (uint64_t pm = dm & ~(uint64_t(1) << t); pm; pm &= pm - 1)
+    c = band(c, bload<T, W>(L.arow + 2 * uint64_t(S.f[__ffsll((long long)pm) - 1])));
   const uint32_t k = uint32_t(__popcll(dm));
   c = k < (1u << kPlanes) ? band(c, peq_added(L.P, row, k)) : z<T, W>();
   L.exps += 1;
@@ -357,7 +357,6 @@ __device__ __forceinline__ void step_counted(Lane<T, W>& L, const JoinArgs& a, S
   } else if (bany(c)) {
     S.F[t] = L.cur;
     S.f[t] = uint8_t(v);
-    S.row[t] = row;
     padd(L.P, row);
     L.mapped = mapped;
     L.t = int(j);
@@ -623,7 +622,7 @@ __global__ void __launch_bounds__(256) cs_enum_kernel(JoinArgs a) {
   }
 }
 
-// The prefix state of a match at depth `end` (S.f, S.row, counting planes,
+// The prefix state of a match at depth `end` (S.f, counting planes,
 // mapped).  Built by every lane that starts a member of the entry; lanes of a
 // warp take consecutive members of the same entry, so they load the same rows.
 template <typename T, int W, bool kCounted>
@@ -638,7 +637,6 @@ __device__ __forceinline__ void cs_prefix(Lane<T, W>& L, Stack<T, W>& S, uint32_
     L.mapped = bor(L.mapped, bbit<T, W>(x));
     if constexpr (kCounted) {
       const Bits<T, W> row = bload<T, W>(arow + 2 * uint64_t(x));
-      S.row[j] = row;
       padd(L.P, row);
     }
   }
@@ -678,7 +676,7 @@ __device__ __forceinline__ void cs_start_member(Lane<T, W>& L, Stack<T, W>& S, u
   if constexpr (kCounted) {
     const uint64_t dm = __ldg(reinterpret_cast<const unsigned long long*>(L.dadj) + end);
     c = bandn(bload<T, W>(L.crow + 2 * uint64_t(__ldg(L.perm + end))), L.mapped);
-    for (uint64_t pm = dm; pm; pm &= pm - 1) c = band(c, S.row[__ffsll((long long)pm) - 1]);
+    for (uint64_t pm = dm; pm; pm &= pm - 1) c = band(c, bload<T, W>(arow + 2 * uint64_t(S.f[__ffsll((long long)pm) - 1])));
     const uint32_t k = uint32_t(__popcll(dm));
     c = k < (1u << kPlanes) ? band(c, peq_added(L.P, z<T, W>(), k)) : z<T, W>();
   } else {
@@ -913,7 +911,6 @@ __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
               L.mapped = bor(L.mapped, bbit<T, W>(x));
               if constexpr (kCounted) {
                 const Bits<T, W> row = bload<T, W>(L.arow + 2 * uint64_t(x));
-                S.row[j] = row;
                 padd(L.P, row);
               }
             }

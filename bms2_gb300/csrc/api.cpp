@@ -286,6 +286,25 @@ JoinArgs join_args(bms_ctx* c, int mode, int sem, bool log_vertices) {
   return ja;
 }
 
+// Side streams and fork/join events of the join (created once per context; a
+// creation failure leaves the classes on the main stream).
+const JoinStreams* join_streams(bms_ctx* c) {
+  JoinStreams& js = c->join_streams;
+  if (c->join_streams_failed) return nullptr;
+  if (!js.fork) {
+    bool ok = true;
+    for (auto& s : js.side) ok = ok && cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess;
+    for (auto& e : js.done) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+    ok = ok && cudaEventCreateWithFlags(&js.fork, cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+      cudaGetLastError();
+      c->join_streams_failed = true;  // the objects created so far are released by bms_destroy
+      return nullptr;
+    }
+  }
+  return &js;
+}
+
 // The clustered join applies when it is switched on and query 0 has nodes
 // (the reference driver keeps the plain join for a depth of 0, BMS2.cpp:233).
 bool cs_active(const bms_ctx* c) {
@@ -322,7 +341,7 @@ int cs_join(bms_ctx* c, int mode, int sem, const uint32_t* dense) {
     ja.err = c->errflag.as<uint32_t>() + 2;
     ClassLaunch cl[3];
     class_launches(c->sched, sem, cl);
-    CK(launch_join(ja, cl, c->st));
+    CK(launch_join(ja, cl, c->st, nullptr, join_streams(c)));
     return BMS_OK;
   }
   CsArgs a{};
@@ -388,7 +407,7 @@ int join_records(bms_ctx* c, int mode, int order, int sem, bool log_vertices, co
   const JoinArgs ja = join_args(c, mode, sem, log_vertices);
   ClassLaunch cl[3];
   class_launches(c->sched, sem, cl);
-  CK(launch_join(ja, cl, c->st));
+  CK(launch_join(ja, cl, c->st, nullptr, join_streams(c)));
   CK(record_event(c, EV_JOIN));
   CK(launch_totals(ctr, c->rec_cap, ja.pair_count, ja.pair_exp, ja.pair_flag, ja.find_first, ctr, c->st));
   c->last_mode = mode;
@@ -601,6 +620,11 @@ void bms_destroy(bms_ctx* c) {
         if (e) cudaEventDestroy(e);
   for (int i = 0; i < EV_COUNT; ++i)
     if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+  for (cudaStream_t s : c->join_streams.side)
+    if (s) cudaStreamDestroy(s);
+  if (c->join_streams.fork) cudaEventDestroy(c->join_streams.fork);
+  for (cudaEvent_t e : c->join_streams.done)
+    if (e) cudaEventDestroy(e);
   if (c->h_err) cudaFreeHost(c->h_err);
   if (c->h_ctr) cudaFreeHost(c->h_ctr);
   if (c->h_T) cudaFreeHost(c->h_T);

@@ -144,6 +144,8 @@ struct bms_ctx {
   uint64_t budget = 0;
   bms_schedule sched{};
   cudaEvent_t class_ev[bms::kJoinRounds][3][2] = {};  // per-class join timers of the autotuner
+  bms::JoinStreams join_streams{};  // side streams of the join's class kernels (created on first use)
+  bool join_streams_failed = false;
   // CUDA graph of the fused pipeline (BMS_OPT_CUDA_GRAPH)
   bool use_graph = true;
   unsigned long long load_gen = 0;  // bumped by every upload

@@ -326,8 +326,15 @@ struct ClassLaunch {
 };
 // All rounds of the join; the per-class fields of `a` come from cl[class].
 // With timers, events [round][class][0/1] bracket each class's launches.
+// Streams on which a round's three class kernels run side by side (the tail
+// of one class fills with the blocks of the others); without them, or with
+// timers, the classes run one after the other on `st`.
+struct JoinStreams {
+  cudaStream_t side[2];
+  cudaEvent_t fork, done[2];
+};
 cudaError_t launch_join(const JoinArgs& a, const ClassLaunch cl[3], cudaStream_t st,
-                        cudaEvent_t (*timers)[3][2] = nullptr);
+                        cudaEvent_t (*timers)[3][2] = nullptr, const JoinStreams* js = nullptr);
 
 // Embeddings of one record (EXACT semantics): every mapping by query vertex.
 struct EmbedArgs {

@@ -966,7 +966,8 @@ cudaError_t launch_class(const JoinArgs& a, int blocks, int threads, cudaStream_
 
 }  // namespace
 
-cudaError_t launch_join(const JoinArgs& args, const ClassLaunch cl[3], cudaStream_t st, cudaEvent_t (*timers)[3][2]) {
+cudaError_t launch_join(const JoinArgs& args, const ClassLaunch cl[3], cudaStream_t st, cudaEvent_t (*timers)[3][2],
+                        const JoinStreams* js) {
   // the reference DFS's visited state does not survive a split
   bool splits = false;
   for (int k = 0; k < 3; ++k) splits = splits || (cl[k].split_budget != 0 && !args.literal);
@@ -977,7 +978,13 @@ cudaError_t launch_join(const JoinArgs& args, const ClassLaunch cl[3], cudaStrea
       cs_enum_kernel<<<sm_count() * 8, 256, 0, st>>>(args); note_launch();
       e = cudaGetLastError();
     }
+    const bool fork = js && !timers;
+    if (fork && e == cudaSuccess) {  // classes 1 and 0 on the side streams, after everything before
+      e = cudaEventRecord(js->fork, st);
+      for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaStreamWaitEvent(js->side[i], js->fork, 0);
+    }
     for (int k = 2; k >= 0 && e == cudaSuccess; --k) {
+      const cudaStream_t ks = fork && k < 2 ? js->side[1 - k] : st;
       JoinArgs a = args;
       a.round = r;
       a.per_pair = args.literal ? 0 : cl[k].per_pair;
@@ -986,11 +993,16 @@ cudaError_t launch_join(const JoinArgs& args, const ClassLaunch cl[3], cudaStrea
       a.split_budget = !args.literal && r + 1 < kJoinRounds ? cl[k].split_budget : 0u;
       if (timers) e = cudaEventRecord(timers[r][k][0], st);
       if (e != cudaSuccess) break;
-      e = k == 2 ? launch_class<2>(a, cl[k].blocks, cl[k].threads, st)
-                 : (k == 1 ? launch_class<1>(a, cl[k].blocks, cl[k].threads, st)
-                           : launch_class<0>(a, cl[k].blocks, cl[k].threads, st));
+      e = k == 2 ? launch_class<2>(a, cl[k].blocks, cl[k].threads, ks)
+                 : (k == 1 ? launch_class<1>(a, cl[k].blocks, cl[k].threads, ks)
+                           : launch_class<0>(a, cl[k].blocks, cl[k].threads, ks));
       if (timers && e == cudaSuccess) e = cudaEventRecord(timers[r][k][1], st);
     }
+    if (fork)  // the next round (and everything after) waits for all three classes
+      for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+        e = cudaEventRecord(js->done[i], js->side[i]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, js->done[i], 0);
+      }
   }
   return e;
 }

@@ -80,7 +80,7 @@ int check_side_errors(bms_ctx* c, const char* side, uint32_t e) {
 // the window's first node and entry, and the ids are rebased on the device.
 // Drop the buffers of a side that are views of the resident batch.
 void release_views(Side& s) {
-  for (DevBuf* b : {&s.goff, &s.rowp, &s.col, &s.lab, &s.elab, &s.frec, &s.adj, &s.adjin, &s.ghist, &s.glabset,
+  for (DevBuf* b : {&s.goff, &s.rowp, &s.col, &s.lab, &s.frec, &s.adj, &s.adjin, &s.ghist, &s.glabset,
                     &s.maxin, &s.size_order})
     if (!b->owned) b->release();
 }
@@ -124,7 +124,6 @@ int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const 
   CK(s.rowp.ensure(sizeof(uint32_t) * (N + 1)));
   CK(s.col.ensure(sizeof(uint32_t) * (E ? E : 1)));
   CK(s.lab.ensure(N ? N : 1));
-  CK(s.elab.ensure(E ? E : 1));
   CK(cudaMemcpyAsync(s.goff.p, s.h_goff.data(), sizeof(uint32_t) * (G + 1), cudaMemcpyHostToDevice, c->st));
   if (&s == &c->q) {  // the fused filter screens queries longest first
     s.h_size_order.resize(G);
@@ -144,8 +143,8 @@ int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const 
   }
   if (E) {
     CK(cudaMemcpyAsync(s.col.p, v.column_indices, sizeof(uint32_t) * E, cudaMemcpyHostToDevice, c->st));
-    if (v.edge_labels) CK(cudaMemcpyAsync(s.elab.p, v.edge_labels, E, cudaMemcpyHostToDevice, c->st));
-    else CK(cudaMemsetAsync(s.elab.p, 0, E, c->st));
+    // edge labels are never read by matching (the reference ignores them too,
+    // isomorphism.hpp:30-472): they are accepted but not copied to the device
   }
   if (N) CK(launch_rebase(s.rowp.as<uint32_t>(), N + 1, entry_base, s.col.as<uint32_t>(), E, node_base, c->st));
   CK(s.frec.ensure(sizeof(uint64_t) * kRecWords * (N ? N : 1)));
@@ -949,7 +948,6 @@ void view_window(bms_ctx* c, uint32_t g0, uint32_t g1) {
   d.rowp.alias(r.rowp.p, r.rowp.bytes);
   d.col.alias(r.col.p, r.col.bytes);
   d.lab.alias(r.lab.p, r.lab.bytes);
-  d.elab.alias(r.elab.p, r.elab.bytes);
   d.frec.alias(r.frec.p, r.frec.bytes);
   d.adj.alias(r.adj.p, r.adj.bytes);
   d.adjin.alias(r.adjin.p, r.adjin.bytes);
@@ -1050,8 +1048,7 @@ int bms_graphs_pin(bms_graphs* g) {
   cudaError_t e = reg(g->goff.data(), g->goff.size() * sizeof(uint32_t));
   if (e == cudaSuccess) e = reg(g->rowp.data(), g->rowp.size() * sizeof(uint32_t));
   if (e == cudaSuccess) e = reg(g->col.data(), g->col.size() * sizeof(uint32_t));
-  if (e == cudaSuccess) e = reg(g->lab.data(), g->lab.size());
-  if (e == cudaSuccess) e = reg(g->elab.data(), g->elab.size());
+  if (e == cudaSuccess) e = reg(g->lab.data(), g->lab.size());  // edge labels are never copied
   if (e != cudaSuccess) {
     cudaGetLastError();
     release_graph_pins(g);

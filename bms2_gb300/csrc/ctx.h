@@ -62,7 +62,7 @@ struct Side {
   uint32_t max_nodes = 0;
   std::vector<uint32_t> h_goff;
   std::vector<uint32_t> h_size_order;  // query side: graph ids by decreasing node count
-  DevBuf goff, rowp, col, lab, elab, size_order;
+  DevBuf goff, rowp, col, lab, size_order;  // edge labels stay on the host: matching never reads them
   DevBuf frec, adj, adjin, ghist, glabset, maxin;
   int sig_steps = -1;
   bool asymmetric = false;

@@ -315,6 +315,7 @@ __global__ void query_totals_kernel(const PairRec* recs, const Counters* ctr, ui
   }
 }
 
+
 }  // namespace
 
 cudaError_t launch_label_count(const DGraphs& d, unsigned long long* counts, cudaStream_t st) {

@@ -540,3 +540,25 @@ def test_sliced_filter_slow_clauses(ctx):
         assert ctx.run(R, COUNT_ALL, ORDER_GMCR, SEM_EXACT) == want.total
         assert np.array_equal(ctx.pair_counts(), want.counts)
     assert want.total == 20 + 20 * 19 + 40320 + 1 + 1  # the [C,30] edge also sits once in kd
+
+
+def test_results_into_page_locked_memory(ctx, wl):
+    # results read into page-locked memory (aligned and at an 8-byte offset)
+    # equal those read into ordinary memory
+    import ctypes
+
+    torch = pytest.importorskip("torch")
+    from bms2_gb300 import native
+
+    q, d = wl
+    load(ctx, q, d)
+    ctx.run(2, COUNT_ALL, ORDER_GMCR, SEM_EXACT)
+    want = ctx.pair_counts()
+    T = len(want)
+    buf = torch.zeros(8 * T + 24, dtype=torch.uint8).pin_memory()
+    for off in (0, 8):
+        buf.zero_()
+        ptr = ctypes.cast(buf.data_ptr() + off, native._u64p)
+        native._check(native.lib().bms_get_pair_counts(ctx.handle, ptr, T), ctx.handle)
+        got = buf.numpy()[off:off + 8 * T].view(np.uint64)
+        assert np.array_equal(got, want)

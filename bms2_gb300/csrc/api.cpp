@@ -107,6 +107,7 @@ int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const 
   if (E && !v.column_indices) return fail(c, BMS_EINVAL, "column_indices is null");
   s.loaded = false;
   s.sig_steps = -1;
+  if (&s == &c->d) c->d_sig_cached = false;  // an upload replaces a resident window
   ++c->load_gen;
   s.G = G;
   s.N = N;
@@ -198,6 +199,10 @@ int run_signatures(bms_ctx* c, int R) {
   for (int i = 0; i < 2; ++i) {
     Side& s = *sides[i];
     s.sig_steps = R;
+    if (i == 0 && c->d_sig_cached && c->dres_sig_R == R) {  // computed once for the resident batch
+      CK(cudaMemcpyAsync(c->errflag.p, c->dres_err.p, sizeof(uint32_t), cudaMemcpyDeviceToDevice, c->st));
+      continue;
+    }
     CK(cudaMemsetAsync(s.maxin.p, 0, sizeof(uint32_t), c->st));
     CK(launch_signatures(s.dg(), s.ds(), i == 0 ? kMaxDataNodes : kMaxQueryNodes, c->errflag.as<uint32_t>() + i, c->st));
   }
@@ -673,6 +678,10 @@ int bms_set_option(bms_ctx* c, int option, int64_t value) {
       if (value != 0 && value != 1) return fail(c, BMS_EINVAL, "clustered join is 0 (off) or 1 (on)");
       c->use_cs = value != 0;
       return BMS_OK;
+    case BMS_OPT_RESIDENT_SIGNATURES:
+      if (value != 0 && value != 1) return fail(c, BMS_EINVAL, "resident signatures is 0 (off) or 1 (on)");
+      c->resident_sigs = value != 0;
+      return BMS_OK;
     default:
       return fail(c, BMS_EINVAL, "unknown option");
   }
@@ -927,6 +936,8 @@ int bms_load_resident(bms_ctx* c, const bms_graphs* data) {
   invalidate_downstream(c);
   release_views(c->d);  // views of the previous resident batch
   c->d.loaded = false;
+  c->d_sig_cached = false;
+  c->dres_sig_R = -1;
   bms_graphs_view v;
   bms_graphs_view_of(data, &v);
   return upload(c, c->dres, v, kMaxDataNodes, "data");
@@ -974,14 +985,38 @@ int bms_run_resident(bms_ctx* c, uint32_t window_graphs, int R, int mode, int or
       CK(c->per_query.ensure(sizeof(unsigned long long) * (Q ? Q : 1)));
       CK(cudaMemsetAsync(c->per_query.p, 0, sizeof(unsigned long long) * (Q ? Q : 1), c->st));
     }
+    if (R < 0 || R > BMS_MAX_REFINE_STEPS) return fail(c, BMS_EINVAL, "refine_steps must be in [0, 8]");
+    float ms_resident_sigs = 0.f;
+    if (!c->resident_sigs) {
+      c->dres_sig_R = -1;  // windows write the shared arrays and their own in-degree bound
+    } else if (c->dres_sig_R != R) {
+      // every node of the resident batch once, with the batch's in-degree bound and error bits
+      Side& r = c->dres;
+      CK(c->dres_err.ensure(sizeof(uint32_t)));
+      CK(cudaMemsetAsync(c->errflag.p, 0, 4 * sizeof(uint32_t), c->st));
+      CK(cudaMemsetAsync(r.maxin.p, 0, sizeof(uint32_t), c->st));
+      r.sig_steps = R;
+      CK(record_event(c, EV_START));
+      CK(launch_signatures(r.dg(), r.ds(), kMaxDataNodes, c->errflag.as<uint32_t>(), c->st));
+      CK(record_event(c, EV_SIG));
+      CK(cudaMemcpyAsync(c->dres_err.p, c->errflag.p, sizeof(uint32_t), cudaMemcpyDeviceToDevice, c->st));
+      CK(cudaMemcpyAsync(c->h_err, c->errflag.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->st));
+      CK(cudaStreamSynchronize(c->st));
+      ms_resident_sigs = elapsed(c, EV_START, EV_SIG);
+      int r2 = check_side_errors(c, "data", c->h_err[0]);
+      if (r2) return r2;
+      c->dres_sig_R = R;
+    }
     uint64_t sum = 0;
     int incomplete = 0;
     bms_stats acc{};
+    acc.ms_signatures = ms_resident_sigs;
     uint32_t g0 = 0;
     do {
       const uint32_t g1 = std::min<uint64_t>(G, uint64_t(g0) + window_graphs);
       invalidate_downstream(c);
       view_window(c, g0, g1);
+      c->d_sig_cached = c->resident_sigs && c->dres_sig_R == R;
       int r = build_classes(c);
       if (r) return r;
       uint64_t t = 0;

@@ -146,6 +146,12 @@ struct bms_ctx {
   cudaEvent_t class_ev[bms::kJoinRounds][3][2] = {};  // per-class join timers of the autotuner
   bms::JoinStreams join_streams{};  // side streams of the join's class kernels (created on first use)
   bool join_streams_failed = false;
+  // BMS_OPT_RESIDENT_SIGNATURES: data-side signatures of the resident batch,
+  // computed once for dres_sig_R refine steps (-1: none), with their error bits
+  bool resident_sigs = false;
+  int dres_sig_R = -1;
+  DevBuf dres_err;
+  bool d_sig_cached = false;  // the data side is a window whose signatures are cached
   // CUDA graph of the fused pipeline (BMS_OPT_CUDA_GRAPH)
   bool use_graph = true;
   unsigned long long load_gen = 0;  // bumped by every upload

@@ -26,7 +26,8 @@ SIZE_UNIFORM, SIZE_NORMAL, SIZE_LOGNORMAL = 0, 1, 2
 NUM_FEATURES = 12
 MLP_PARAMS = 64 * 12 + 64 + 64 * 64 + 64 + 64 + 1
 SCHED_BUCKETS = 4
-OPT_FILTER_KERNEL, OPT_JOIN_STEPS, OPT_SPLIT_BUDGET, OPT_SUBTREE_CAP, OPT_CUDA_GRAPH, OPT_USE_CS = 1, 2, 3, 4, 5, 6
+(OPT_FILTER_KERNEL, OPT_JOIN_STEPS, OPT_SPLIT_BUDGET, OPT_SUBTREE_CAP, OPT_CUDA_GRAPH, OPT_USE_CS,
+ OPT_RESIDENT_SIGNATURES) = 1, 2, 3, 4, 5, 6, 7
 FILTER_SLICED, FILTER_BALLOT = 0, 1
 
 

@@ -162,9 +162,13 @@ typedef enum {
   BMS_OPT_CUDA_GRAPH = 5,    /* 1 (default): bms_run captures its device work as a CUDA graph on the
                                 second run with unchanged inputs and settings, and replays it after;
                                 0: every run launches its kernels one by one */
-  BMS_OPT_USE_CS = 6         /* 1: the clustered join of the reference driver's --use-cs
+  BMS_OPT_USE_CS = 6,        /* 1: the clustered join of the reference driver's --use-cs
                                 (BMS2.cpp:218-296) replaces the join of bms_join, bms_run and the batch
                                 drivers; 0 (default): the plain join.  See below. */
+  BMS_OPT_RESIDENT_SIGNATURES = 7 /* 1: bms_run_resident computes the data-side signatures of the whole
+                                resident batch once (for its refine_steps) and every later window and
+                                call reuses them; 0 (default): each window computes its own.  For
+                                serving many small query batches over the same resident data. */
 } bms_option;
 /* Clustered join.  The loaded queries are one cluster in the layout of the
  * reference's cluster files (generate_cs.py:338-362, 555-577): query 0 is the

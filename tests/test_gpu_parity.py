@@ -338,6 +338,37 @@ def test_resident_windows_equal_one_run(ctx, window):
     assert total == oracle.run_pipeline(q, d, 2).total
 
 
+@pytest.mark.parametrize("window", [37, 0])
+def test_resident_signatures_computed_once(ctx, window):
+    # BMS_OPT_RESIDENT_SIGNATURES: the data side's signatures are computed once
+    # for the whole resident batch; later windows and calls reuse them (no
+    # signature time), with the same results; R and a new batch recompute
+    from bms2_gb300 import OPT_RESIDENT_SIGNATURES
+
+    d = Graphs.synth_molecules(260, 81, 0, 0, 0, 6, 110, 1, 4)
+    q = Graphs.synth_queries(d, 12, 82, 3, 10)
+    ctx.load(QUERY, q)
+    ctx.load_resident(d)
+    ctx.set_option(OPT_RESIDENT_SIGNATURES, 1)
+    try:
+        for R in (2, 6, 2):
+            want = oracle.run_pipeline(q, d, R)
+            dense = want.pair_counts_dense(q.n_graphs).sum(axis=1).astype(np.uint64)
+            for call in range(2):
+                total, per_query = ctx.run_resident(window, R)
+                assert total == want.total and np.array_equal(per_query, dense)
+            # the second call reused every window's signatures
+            assert ctx.stats()["ms_signatures"] < 1.0
+        d2 = Graphs.synth_molecules(150, 83, 0, 0, 0, 6, 110, 1, 4)
+        ctx.load_resident(d2)
+        total, _ = ctx.run_resident(window, 2)
+        assert total == oracle.run_pipeline(q, d2, 2).total
+    finally:
+        ctx.set_option(OPT_RESIDENT_SIGNATURES, 0)
+    total, _ = ctx.run_resident(window, 2)
+    assert total == oracle.run_pipeline(q, d2, 2).total
+
+
 def test_embeddings_equal_the_oracle(ctx):
     # every embedding of a pair (not only the count), sorted, against the
     # oracle's enumeration (itself pinned against networkx); graphs of up to

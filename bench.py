@@ -175,7 +175,8 @@ def run_ours(args) -> None:
     import torch
     import torch.distributed as dist
 
-    from bms2_gb300 import COUNT_ALL, DATA, ORDER_GMCR, ORDER_LEARNED, QUERY, SEM_EXACT, Context, shards, workloads
+    from bms2_gb300 import (COUNT_ALL, DATA, FIND_FIRST, ORDER_GMCR, ORDER_LEARNED, QUERY, SEM_EXACT, Context, shards,
+                            workloads)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -213,17 +214,17 @@ def run_ours(args) -> None:
     ctx.load(DATA, d)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
 
-    def step(o=order):
-        return ctx.run(REFINE_STEPS, COUNT_ALL, o, SEM_EXACT)
+    def step(o=order, mode=COUNT_ALL):
+        return ctx.run(REFINE_STEPS, mode, o, SEM_EXACT)
 
-    def timed(o, k):
+    def timed(o, k, mode=COUNT_ALL):
         """k steps of order o, each bracketed by CUDA events on the library's stream."""
         ms, stages = [], []
         for _ in range(k):
             flush.fill_(1)  # L2 flush between steps (outside the timed events)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            tot = step(o)
+            tot = step(o, mode)
             e1.record(stream)
             e1.synchronize()
             ms.append(e0.elapsed_time(e1))
@@ -276,6 +277,21 @@ def run_ours(args) -> None:
     t_total = float(np.sum(ms_steps)) / 1e3
     st = stage[-1]
     all_total, all_valid = int(total), int(st["n_valid_pairs"])
+    # find-first (the reference driver's default mode) on the same inputs: one
+    # 0/1 per pair, equal to "count-all found something" on every pair
+    ca_counts = ctx.pair_counts()
+    for _ in range(args.warmup):
+        step(order, FIND_FIRST)
+    ff_ms, ff_stage, ff_total = timed(order, args.steps, FIND_FIRST)
+    find_first = {"find_first_value": world * Q * D / (float(np.mean(ff_ms)) / 1e3),
+                  "find_first_ms_per_step": float(np.mean(ff_ms)),
+                  "find_first_join_ms": float(np.mean([s["ms_join"] for s in ff_stage])),
+                  "find_first_pairs_matched": int(ff_total),
+                  "find_first_equals_count_all_nonzero": bool(np.array_equal(
+                      ctx.pair_counts(), (ca_counts > 0).astype(np.uint64)))}
+    del ca_counts
+    for _ in range(args.warmup):
+        step()
     if world > 1:  # shards: sum of counts, slowest rank's time
         all_total, all_valid, t_total = shards.reduce_totals(all_total, all_valid, t_total, device=dev)
     # e2e: host buffers in, counts out, through the C ABI
@@ -352,6 +368,7 @@ def run_ours(args) -> None:
         line["results"]["learned_over_plain"] = line["results"]["plain_value"] and value / line["results"]["plain_value"]
         line["results"]["expansion_ratio_plain_over_learned"] = float(plain["plain_expansions"]) / max(1, st["expansions"])
     line["results"].update(extra)
+    line["results"].update(find_first)
     if schedule is not None:
         line["schedule"] = {"tuned_on": f"{args.workload} seed A, "
                                         f"{args.tune_graphs if args.tune_graphs > 0 else 'all'} data graphs",

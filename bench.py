@@ -412,12 +412,17 @@ def run_streamed(args) -> None:
     extra["synth_seconds"] = time.perf_counter() - t0
     Q, D = q.n_graphs, d.n_graphs
     ctx.load(QUERY, q)
-    # e2e: the data side streamed from host memory through the batch driver
+    # e2e: the data side streamed from host memory through the batch driver,
+    # from a page-locked host batch (bms_graphs_pin), after one untimed pass
+    # that sizes the device buffers
+    d.pin()
+    ctx.run_batches(d, args.slice, REFINE_STEPS, COUNT_ALL, order, SEM_EXACT)
     torch.cuda.synchronize(dev)
     t = time.perf_counter()
     e2e_total, _ = ctx.run_batches(d, args.slice, REFINE_STEPS, COUNT_ALL, order, SEM_EXACT)
     torch.cuda.synchronize(dev)
     e2e_s = time.perf_counter() - t
+    d.unpin()
     # value: the data side resident in HBM, processed in windows of --slice graphs
     ctx.load_resident(d)
     for _ in range(max(1, args.warmup)):
@@ -493,7 +498,8 @@ def run_streamed(args) -> None:
                    "l2": "inputs far larger than L2 (every window is processed once per pass)",
                    "parallelism": f"data-graph shards x{world}"},
         "e2e": {"value": world * pairs / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 8 * Q,
-                "note": "one pass through bms_run_batches: every slice uploaded from host memory inside it"},
+                "note": "one pass through bms_run_batches: every slice uploaded from page-locked host memory "
+                        "inside it (after one untimed pass)"},
         "roofline": {"kernel": "sliced_filter (fused filter + refine + GMCR validity), all slices", "bound": "hbm",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
                      "peak_kind": f"{peak_kind} hbm_gbs", "algorithmic_bytes": fbytes, "ms": st["ms_filter"],

@@ -25,7 +25,7 @@ struct WarpSmem {
   uint16_t row[kMaxDataNodes + 1];
   uint8_t col[kMaxEntries];
   B128 labmask[16];
-  uint32_t cyc[kMaxDataNodes][4];  // cycle closures per node (canonical enumeration)
+  alignas(16) uint32_t cyc[kMaxDataNodes][4];  // cycle closures per node (canonical enumeration)
   uint16_t first[kMaxDataNodes + 1];  // canonical enumeration: offsets of the (s0, a) work items
 };
 
@@ -52,6 +52,45 @@ __device__ __forceinline__ uint64_t label_hist(const WarpSmem& s, uint32_t prese
     h |= uint64_t(c < 15u ? c : 15u) << (4 * l);
   }
   return h;
+}
+
+// Exact-distance shells 1..R (signature.hpp:335-389 refines with BFS levels),
+// level-synchronous over the warp: reach_k(v) = reach_{k-1}(v) | reach_{k-1}(u)
+// for every u in the row of v, and shell k of v (the nodes first reached after
+// k steps) is reach_k(v) minus reach_{k-1}(v).  Every lane runs one union per
+// neighbour of its nodes per level, so lanes stay in step whatever the BFS
+// frontiers look like.  The reach sets live in s.same and s.cyc, which are
+// filled only after this; once no set grows, the remaining shells are empty.
+// Writes record words 6..13 (shells 1..8; steps >= R stay zero).
+__device__ void shells_levels(WarpSmem& s, const DSigs& out, uint32_t start, uint32_t m, uint32_t lane,
+                              uint32_t present) {
+  B128* cur = s.same;
+  B128* nxt = reinterpret_cast<B128*>(s.cyc);
+  for (uint32_t v = lane; v < m; v += 32) cur[v] = b_bit(v);
+  __syncwarp();
+  bool grows = out.R > 0;
+  for (int k = 0; k < kMaxSteps; ++k) {
+    bool grew = false;
+    for (uint32_t v = lane; v < m; v += 32) {
+      uint64_t h = 0;
+      if (grows && k < out.R) {
+        const B128 prev = cur[v];
+        B128 r = prev;
+        for (B128 a = s.adj[v]; b_any(a); a = b_clear_low(a)) r = b_or(r, cur[b_low(a)]);
+        nxt[v] = r;
+        const B128 shell = b_andn(r, prev);
+        grew = grew || b_any(shell);
+        h = label_hist(s, present, shell);
+      }
+      out.frec[uint64_t(kRecWords) * (uint64_t(start) + v) + 6 + k] = h;
+    }
+    grows = __any_sync(0xffffffffu, grew);
+    __syncwarp();
+    B128* t = cur;
+    cur = nxt;
+    nxt = t;
+  }
+  __syncwarp();
 }
 
 __device__ uint32_t mult(const Rows& r, uint32_t a, uint32_t target) {
@@ -275,6 +314,9 @@ __global__ void __launch_bounds__(kWarps * 32) signatures_kernel(DGraphs g, DSig
       }
     }
     __syncwarp();
+    // labels < 16 present in the graph: label histograms are popcounts of their masks
+    const uint32_t present = __ballot_sync(0xffffffffu, lane < 16 && b_any(s.labmask[lane]));
+    shells_levels(s, out, start, m, lane, present);
     uint32_t max_in = 0;
     for (uint32_t v = lane; v < m; v += 32) {
       B128 eq{0, 0};
@@ -296,8 +338,6 @@ __global__ void __launch_bounds__(kWarps * 32) signatures_kernel(DGraphs g, DSig
     // symmetric graphs without repeated entries: every cycle found once
     const bool canonical = !multi && !(bad & kErrAsym);
     if (canonical) cycles_canonical(s, m, lane);
-    // labels < 16 present in the graph: label histograms are popcounts of their masks
-    const uint32_t present = __ballot_sync(0xffffffffu, lane < 16 && b_any(s.labmask[lane]));
     for (uint32_t v = lane; v < m; v += 32) {
       const uint64_t u = uint64_t(start) + v;
       const uint32_t lu = s.lab[v];
@@ -308,19 +348,33 @@ __global__ void __launch_bounds__(kWarps * 32) signatures_kernel(DGraphs g, DSig
       } else {  // every entry distinct: the row as a set
         lg = label_hist(s, present, s.adj[v]);
       }
-      // path signature: walks v-a-w (w != v) and v-a-w-x (x != a, x != v)
+      // path signature: walks v-a-w (w != v) and v-a-w-x (x != a, x != v), as
+      // one flat loop with one Bloom insert per iteration, so lanes whose nodes
+      // have different neighbourhoods still hash in step (inserts commute)
       uint64_t p0 = 0, p1 = 0, p2 = 0, p3 = 0;
-      for (B128 ra = s.adj[v]; b_any(ra); ra = b_clear_low(ra)) {
-        const uint32_t a = b_low(ra);
-        const uint32_t la = s.lab[a];
-        for (B128 rw = b_andn(s.adj[a], b_bit(v)); b_any(rw); rw = b_clear_low(rw)) {
-          const uint32_t w = b_low(rw);
-          const uint32_t h2 = hcombine(lu, hcombine(la, s.lab[w]));
-          bloom_insert(p0, p1, p2, p3, fmix32(h2));
-          for (B128 rx = b_andn(s.adj[w], b_or(b_bit(a), b_bit(v))); b_any(rx); rx = b_clear_low(rx)) {
-            const uint32_t x = b_low(rx);
-            bloom_insert(p0, p1, p2, p3, fmix32(hcombine(h2, s.lab[x])));
+      {
+        const B128 bv = b_bit(v);
+        B128 ra = s.adj[v], rw{0, 0}, rx{0, 0};
+        uint32_t a = 0, h2 = 0;
+        while (true) {
+          uint32_t h;
+          if (b_any(rx)) {  // next x of the current v-a-w
+            h = hcombine(h2, s.lab[b_low(rx)]);
+            rx = b_clear_low(rx);
+          } else {  // next w, moving on to the next a with a continuation
+            while (!b_any(rw) && b_any(ra)) {
+              a = b_low(ra);
+              ra = b_clear_low(ra);
+              rw = b_andn(s.adj[a], bv);
+            }
+            if (!b_any(rw)) break;
+            const uint32_t w = b_low(rw);
+            rw = b_clear_low(rw);
+            h2 = hcombine(lu, hcombine(s.lab[a], s.lab[w]));
+            h = h2;
+            rx = b_andn(s.adj[w], b_or(b_bit(a), bv));
           }
+          bloom_insert(p0, p1, p2, p3, fmix32(h));
         }
       }
       // cycle signature
@@ -334,30 +388,12 @@ __global__ void __launch_bounds__(kWarps * 32) signatures_kernel(DGraphs g, DSig
       }
       const uint64_t cyc = uint64_t((c[0] & 0xFFFFu) >> 1) | (uint64_t((c[1] & 0xFFFFu) >> 1) << 16) |
                            (uint64_t((c[2] & 0xFFFFu) >> 1) << 32) | (uint64_t((c[3] & 0xFFFFu) >> 1) << 48);
-      // distance shells 1..R (exact BFS levels); unused steps stay zero
-      uint64_t sh[kMaxSteps];
-      B128 reached = b_bit(v), frontier = reached;
-#pragma unroll
-      for (int k = 0; k < kMaxSteps; ++k) {
-        sh[k] = 0;
-        if (k < out.R) {
-          B128 next{0, 0};
-          for (B128 f = frontier; b_any(f); f = b_clear_low(f)) next = b_or(next, s.adj[b_low(f)]);
-          next = b_andn(next, reached);
-          reached = b_or(reached, next);
-          sh[k] = label_hist(s, present, next);
-          frontier = next;
-        }
-      }
+      // record words 6..13 (distance shells) were written by shells_levels
       const uint32_t deg = rows.end(v) - rows.begin(v);
       ulonglong2* rec = reinterpret_cast<ulonglong2*>(out.frec + uint64_t(kRecWords) * u);
       rec[0] = make_ulonglong2(uint64_t(lu) | (uint64_t(deg) << 32), cyc);
       rec[1] = make_ulonglong2(p0, p1);
       rec[2] = make_ulonglong2(p2, p3);
-      rec[3] = make_ulonglong2(sh[0], sh[1]);
-      rec[4] = make_ulonglong2(sh[2], sh[3]);
-      rec[5] = make_ulonglong2(sh[4], sh[5]);
-      rec[6] = make_ulonglong2(sh[6], sh[7]);
       rec[7] = make_ulonglong2(lg, 0ull);
       st_b128(out.adj + 2 * u, s.adj[v]);
       st_b128(out.adjin + 2 * u, s.in[v]);

@@ -145,15 +145,24 @@ __device__ void cycles_entries(const WarpSmem& s, const Rows& r, uint32_t v, uin
 __device__ void cycles_canonical(WarpSmem& s, uint32_t m, uint32_t lane) {
   const B128 all = b_lowmask(m);
   // work items: (s0, a) with a an upper neighbour of s0, spread over the lanes
-  for (uint32_t v = lane; v < m; v += 32) {
-    for (int t = 0; t < 4; ++t) s.cyc[v][t] = 0;
-    s.first[v + 1] = uint16_t(b_pop(b_and(s.adj[v], b_andn(all, b_lowmask(v + 1)))));
+  // first[v] = items of the nodes before v: a warp scan per 32 nodes
+  uint32_t carry = 0;
+  for (uint32_t v0 = 0; v0 < m; v0 += 32) {
+    const uint32_t v = v0 + lane;
+    uint32_t n = 0;
+    if (v < m) {
+      for (int t = 0; t < 4; ++t) s.cyc[v][t] = 0;
+      n = b_pop(b_and(s.adj[v], b_andn(all, b_lowmask(v + 1))));
+    }
+    uint32_t incl = n;
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= uint32_t(d)) incl += y;
+    }
+    if (v < m) s.first[v + 1] = uint16_t(carry + incl);
+    carry += __shfl_sync(0xffffffffu, incl, 31);
   }
-  __syncwarp();
-  if (lane == 0) {
-    s.first[0] = 0;
-    for (uint32_t v = 1; v <= m; ++v) s.first[v] = uint16_t(s.first[v] + s.first[v - 1]);
-  }
+  if (lane == 0) s.first[0] = 0;
   __syncwarp();
   const uint32_t items = s.first[m];
   for (uint32_t k = lane; k < items; k += 32) {
@@ -319,10 +328,14 @@ __global__ void __launch_bounds__(kWarps * 32) signatures_kernel(DGraphs g, DSig
     shells_levels(s, out, start, m, lane, present);
     uint32_t max_in = 0;
     for (uint32_t v = lane; v < m; v += 32) {
-      B128 eq{0, 0};
       const uint8_t l = s.lab[v];
-      for (uint32_t y = 0; y < m; ++y)
-        if (s.lab[y] == l) eq = b_or(eq, b_bit(y));
+      B128 eq{0, 0};
+      if (l < 16) {
+        eq = s.labmask[l];
+      } else {
+        for (uint32_t y = 0; y < m; ++y)
+          if (s.lab[y] == l) eq = b_or(eq, b_bit(y));
+      }
       s.same[v] = eq;
       // symmetry as sets: out-set equals in-set
       const B128 o = s.adj[v], i = s.in[v];

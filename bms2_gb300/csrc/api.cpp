@@ -91,11 +91,13 @@ int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const 
   const uint32_t G = v.n_graphs;
   const uint32_t node_base = slice && G ? v.graph_offsets[0] : 0;
   if (G && v.graph_offsets[0] != node_base) return fail(c, BMS_EINVAL, "graph_offsets[0] must be 0");
-  uint32_t mx = 0;
+  uint32_t mx = 0, dec = 0;  // one branch-free pass
   for (uint32_t i = 0; i < G; ++i) {
-    if (v.graph_offsets[i + 1] < v.graph_offsets[i]) return fail(c, BMS_EINVAL, "graph_offsets must be non-decreasing");
-    mx = std::max(mx, v.graph_offsets[i + 1] - v.graph_offsets[i]);
+    const uint32_t a = v.graph_offsets[i], b = v.graph_offsets[i + 1];
+    dec |= uint32_t(b < a);
+    mx = std::max(mx, b - a);
   }
+  if (dec) return fail(c, BMS_EINVAL, "graph_offsets must be non-decreasing");
   if (mx > limit)
     return fail(c, BMS_EUNSUPPORTED,
                 std::string(name) + " graph with " + std::to_string(mx) + " nodes exceeds the limit of " + std::to_string(limit));
@@ -125,7 +127,10 @@ int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const 
   CK(s.rowp.ensure(sizeof(uint32_t) * (N + 1)));
   CK(s.col.ensure(sizeof(uint32_t) * (E ? E : 1)));
   CK(s.lab.ensure(N ? N : 1));
-  CK(cudaMemcpyAsync(s.goff.p, s.h_goff.data(), sizeof(uint32_t) * (G + 1), cudaMemcpyHostToDevice, c->st));
+  // offsets that need no rebasing go straight from the caller's array (no
+  // staging pass when it is page-locked, like the other arrays)
+  CK(cudaMemcpyAsync(s.goff.p, G && !node_base ? v.graph_offsets : s.h_goff.data(), sizeof(uint32_t) * (G + 1),
+                     cudaMemcpyHostToDevice, c->st));
   if (&s == &c->q) {  // the fused filter screens queries longest first
     s.h_size_order.resize(G);
     for (uint32_t i = 0; i < G; ++i) s.h_size_order[i] = i;
@@ -167,29 +172,27 @@ void invalidate_downstream(bms_ctx* c) {
 }
 
 // Data graphs grouped by size class, largest class first (it carries the most
-// work): 65..128 nodes, 33..64, then <= 32 (empty graphs included).  One
-// counting pass and one placement pass.
+// work): 65..128 nodes, 33..64, then <= 32 (empty graphs included), each class
+// in batch order.  The host counts the classes (the launches need their
+// bounds); the permutation itself is built on the device.
 int build_classes(bms_ctx* c) {
   const uint32_t G = c->d.G;
   const uint32_t* go = c->d.h_goff.data();
-  auto cls = [&](uint32_t g) -> int {
+  uint32_t gt32 = 0, gt64 = 0;
+  for (uint32_t g = 0; g < G; ++g) {
     const uint32_t m = go[g + 1] - go[g];
-    return m > 64 ? 2 : (m > 32 ? 1 : 0);
-  };
-  uint32_t count[3] = {0, 0, 0};
-  for (uint32_t g = 0; g < G; ++g) ++count[cls(g)];
-  uint32_t at[3];
-  at[2] = 0;
-  at[1] = count[2];
-  at[0] = count[2] + count[1];
-  for (int k = 0; k < 3; ++k) {
-    c->class_begin[k] = at[k];
-    c->class_end[k] = at[k] + count[k];
+    gt32 += uint32_t(m > 32);
+    gt64 += uint32_t(m > 64);
   }
-  c->h_dperm.resize(G);
-  for (uint32_t g = 0; g < G; ++g) c->h_dperm[at[cls(g)]++] = g;
+  const uint32_t count[3] = {G - gt32, gt32 - gt64, gt64};
+  c->class_begin[2] = 0;
+  c->class_begin[1] = count[2];
+  c->class_begin[0] = count[2] + count[1];
+  for (int k = 0; k < 3; ++k) c->class_end[k] = c->class_begin[k] + count[k];
   CK(c->dperm.ensure(sizeof(uint32_t) * (G ? G : 1)));
-  if (G) CK(cudaMemcpyAsync(c->dperm.p, c->h_dperm.data(), sizeof(uint32_t) * G, cudaMemcpyHostToDevice, c->st));
+  if (!G) return BMS_OK;
+  CK(c->class_scratch.ensure(sizeof(uint32_t) * class_scratch_words(G)));
+  CK(launch_size_classes(c->d.dg().goff, G, c->class_scratch.as<uint32_t>(), c->dperm.as<uint32_t>(), c->st));
   return BMS_OK;
 }
 

@@ -130,7 +130,7 @@ struct bms_ctx {
   uint64_t sub_cap_opt = 0;  // BMS_OPT_SUBTREE_CAP (0: automatic)
   uint64_t rec_cap = 0, row_cap = 0, task_cap = 0;
   DevBuf dperm;
-  std::vector<uint32_t> h_dperm;  // host copy of dperm (kept alive for the asynchronous upload)
+  DevBuf class_scratch;  // tile counts and scans of the size-class partition
   uint32_t class_begin[3] = {0, 0, 0}, class_end[3] = {0, 0, 0};
   DevBuf filter_order, filter_dup, qpack, prog_len, prog_off, prog, prog_slow, prog_used, prog_remap, prog_ids, prog_nused, label_count, perm, dadj, vertex_exp, cand_sum, recs_per_query, features, cost;
   bool have_results = false, have_vexp = false;

@@ -253,6 +253,11 @@ cudaError_t launch_sliced_filter(const SlicedArgs& a, int words, size_t smem, cu
 // must hold scan_scratch_words(n) words.
 size_t scan_scratch_words(uint64_t n);
 cudaError_t launch_scan_u32(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* scratch, cudaStream_t st);
+// Data graphs grouped by size class into dperm: 65..128 nodes first, then
+// 33..64, then <= 32, each class in batch order.  scratch holds
+// class_scratch_words(G) words.
+uint64_t class_scratch_words(uint32_t G);
+cudaError_t launch_size_classes(const uint32_t* goff, uint32_t G, uint32_t* scratch, uint32_t* dperm, cudaStream_t st);
 
 // GMCR query indices from the valid bits and offsets.
 cudaError_t launch_gmcr_indices(const uint32_t* valid, uint32_t QW, uint32_t Q, uint32_t D, const uint32_t* offsets,

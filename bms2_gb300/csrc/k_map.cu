@@ -316,6 +316,92 @@ __global__ void query_totals_kernel(const PairRec* recs, const Counters* ctr, ui
 }
 
 
+// Data graphs grouped by size class (65..128 nodes, then 33..64, then <= 32),
+// each class in batch order: per tile of kClassTile graphs the class counts,
+// then (after scans of those counts) each tile places its graphs.
+constexpr uint32_t kClassTile = 2048;
+constexpr uint32_t kClassThreads = 256;
+
+__device__ __forceinline__ uint32_t size_class(const uint32_t* goff, uint32_t g) {
+  const uint32_t m = goff[g + 1] - goff[g];
+  return uint32_t(m > 32u) + uint32_t(m > 64u);
+}
+
+__global__ void __launch_bounds__(kClassThreads) class_count_kernel(const uint32_t* goff, uint32_t G, uint32_t* n2,
+                                                                    uint32_t* n1) {
+  __shared__ uint32_t s2[kClassThreads / 32], s1[kClassThreads / 32];
+  const uint32_t t0 = blockIdx.x * kClassTile, lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t c2 = 0, c1 = 0;
+  for (uint32_t i = threadIdx.x; i < kClassTile; i += kClassThreads) {
+    const uint32_t g = t0 + i;
+    if (g < G) {
+      const uint32_t k = size_class(goff, g);
+      c2 += k == 2u;
+      c1 += k == 1u;
+    }
+  }
+  c2 = __reduce_add_sync(0xffffffffu, c2);
+  c1 = __reduce_add_sync(0xffffffffu, c1);
+  if (lane == 0) {
+    s2[warp] = c2;
+    s1[warp] = c1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t a = 0, b = 0;
+    for (uint32_t w = 0; w < kClassThreads / 32; ++w) {
+      a += s2[w];
+      b += s1[w];
+    }
+    n2[blockIdx.x] = a;
+    n1[blockIdx.x] = b;
+  }
+}
+
+// p2, p1: exclusive scans of the tiles' class-2 and class-1 counts (p[tiles] =
+// the class's total).  A graph's place: its class's start, the class's graphs
+// in earlier tiles, then those before it in its tile.
+__global__ void __launch_bounds__(kClassThreads) class_place_kernel(const uint32_t* goff, uint32_t G,
+                                                                    const uint32_t* p2, const uint32_t* p1,
+                                                                    uint32_t tiles, uint32_t* dperm) {
+  __shared__ uint32_t w2[kClassThreads / 32], w1[kClassThreads / 32];
+  const uint32_t t0 = blockIdx.x * kClassTile, lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t total2 = p2[tiles], total1 = p1[tiles];
+  const uint32_t b2 = p2[blockIdx.x], b1 = p1[blockIdx.x];
+  const uint32_t b0 = t0 - b2 - b1;  // class-0 graphs in earlier tiles
+  const uint32_t lt = (1u << lane) - 1u;
+  uint32_t run2 = 0, run1 = 0;  // the tile's class-2 / class-1 graphs in earlier rounds
+  for (uint32_t i0 = 0; i0 < kClassTile; i0 += kClassThreads) {
+    const uint32_t i = i0 + threadIdx.x, g = t0 + i;
+    const bool in = g < G;
+    const uint32_t k = in ? size_class(goff, g) : 3u;
+    const uint32_t m2 = __ballot_sync(0xffffffffu, k == 2u), m1 = __ballot_sync(0xffffffffu, k == 1u);
+    if (lane == 0) {
+      w2[warp] = uint32_t(__popc(m2));
+      w1[warp] = uint32_t(__popc(m1));
+    }
+    __syncthreads();
+    uint32_t r2 = run2 + uint32_t(__popc(m2 & lt)), r1 = run1 + uint32_t(__popc(m1 & lt));
+    for (uint32_t w = 0; w < kClassThreads / 32; ++w) {
+      const uint32_t a = w2[w], b = w1[w];
+      if (w < warp) {
+        r2 += a;
+        r1 += b;
+      }
+      run2 += a;
+      run1 += b;
+    }
+    if (in) {
+      uint32_t pos;
+      if (k == 2u) pos = b2 + r2;
+      else if (k == 1u) pos = total2 + b1 + r1;
+      else pos = total2 + total1 + b0 + (i - r2 - r1);
+      dperm[pos] = g;
+    }
+    __syncthreads();
+  }
+}
+
 }  // namespace
 
 cudaError_t launch_label_count(const DGraphs& d, unsigned long long* counts, cudaStream_t st) {
@@ -429,6 +515,28 @@ cudaError_t launch_query_totals(const PairRec* recs, const Counters* ctr, uint64
   const int use_smem = smem <= (48u << 10);
   query_totals_kernel<<<grid_for(rec_cap, 256, 4), 256, use_smem ? smem : 0, st>>>(recs, ctr, rec_cap, pair_count,
                                                                                   find_first, Q, per_query, use_smem); note_launch();
+  return cudaGetLastError();
+}
+
+uint64_t class_scratch_words(uint32_t G) {
+  const uint64_t tiles = (uint64_t(G) + kClassTile - 1) / kClassTile;
+  return 4 * (tiles + 1) + scan_scratch_words(tiles);
+}
+
+cudaError_t launch_size_classes(const uint32_t* goff, uint32_t G, uint32_t* scratch, uint32_t* dperm, cudaStream_t st) {
+  if (G == 0) return cudaSuccess;
+  const uint32_t tiles = uint32_t((uint64_t(G) + kClassTile - 1) / kClassTile);
+  uint32_t* n2 = scratch;
+  uint32_t* n1 = n2 + (tiles + 1);
+  uint32_t* p2 = n1 + (tiles + 1);
+  uint32_t* p1 = p2 + (tiles + 1);
+  uint32_t* ss = p1 + (tiles + 1);
+  class_count_kernel<<<tiles, kClassThreads, 0, st>>>(goff, G, n2, n1); note_launch();
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  if ((e = launch_scan_u32(n2, p2, tiles, ss, st)) != cudaSuccess) return e;
+  if ((e = launch_scan_u32(n1, p1, tiles, ss, st)) != cudaSuccess) return e;
+  class_place_kernel<<<tiles, kClassThreads, 0, st>>>(goff, G, p2, p1, tiles, dperm); note_launch();
   return cudaGetLastError();
 }
 

@@ -191,7 +191,9 @@ int bms_set_option(bms_ctx* ctx, int option, int64_t value);
 /* createDeviceCSRGraph (graph.hpp:251-310): upload a batch as the query or the
  * data side.  The CSR must be symmetric with column ids inside each graph; the
  * check runs on the device and is reported by the next stage call.  Edge labels
- * are accepted but not copied: matching never reads them (as in the reference). */
+ * are accepted but not copied: matching never reads them (as in the reference).
+ * Arrays in page-locked memory are copied asynchronously: keep them unchanged
+ * until the next stage call, run or read-back on the context returns. */
 int bms_load_graphs(bms_ctx* ctx, int kind, const bms_graphs* g);
 int bms_load_csr(bms_ctx* ctx, int kind, uint32_t n_graphs, const uint32_t* graph_offsets,
                  const uint32_t* row_offsets, const uint32_t* column_indices, const uint8_t* node_labels,

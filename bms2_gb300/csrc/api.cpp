@@ -91,16 +91,7 @@ int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const 
   const uint32_t G = v.n_graphs;
   const uint32_t node_base = slice && G ? v.graph_offsets[0] : 0;
   if (G && v.graph_offsets[0] != node_base) return fail(c, BMS_EINVAL, "graph_offsets[0] must be 0");
-  uint32_t mx = 0, dec = 0;  // one branch-free pass
-  for (uint32_t i = 0; i < G; ++i) {
-    const uint32_t a = v.graph_offsets[i], b = v.graph_offsets[i + 1];
-    dec |= uint32_t(b < a);
-    mx = std::max(mx, b - a);
-  }
-  if (dec) return fail(c, BMS_EINVAL, "graph_offsets must be non-decreasing");
-  if (mx > limit)
-    return fail(c, BMS_EUNSUPPORTED,
-                std::string(name) + " graph with " + std::to_string(mx) + " nodes exceeds the limit of " + std::to_string(limit));
+  if (G && v.graph_offsets[G] < node_base) return fail(c, BMS_EINVAL, "graph_offsets must be non-decreasing");
   const uint64_t N = G ? v.graph_offsets[G] - node_base : 0;
   if (N && (!v.row_offsets || !v.node_labels)) return fail(c, BMS_EINVAL, "row_offsets or node_labels is null");
   const uint32_t entry_base = slice && N ? v.row_offsets[0] : 0;
@@ -111,6 +102,35 @@ int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const 
   s.sig_steps = -1;
   if (&s == &c->d) c->d_sig_cached = false;  // an upload replaces a resident window
   ++c->load_gen;
+  // the large arrays first: their copies run while the host checks the offsets
+  // (a batch that fails the checks leaves the side unloaded)
+  CK(s.goff.ensure(sizeof(uint32_t) * (G + 1)));
+  CK(s.rowp.ensure(sizeof(uint32_t) * (N + 1)));
+  CK(s.col.ensure(sizeof(uint32_t) * (E ? E : 1)));
+  CK(s.lab.ensure(N ? N : 1));
+  if (E) {
+    CK(cudaMemcpyAsync(s.col.p, v.column_indices, sizeof(uint32_t) * E, cudaMemcpyHostToDevice, c->st));
+    // edge labels are never read by matching (the reference ignores them too,
+    // isomorphism.hpp:30-472): they are accepted but not copied to the device
+  }
+  if (N) {
+    CK(cudaMemcpyAsync(s.rowp.p, v.row_offsets, sizeof(uint32_t) * (N + 1), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(s.lab.p, v.node_labels, N, cudaMemcpyHostToDevice, c->st));
+  } else {
+    CK(cudaMemsetAsync(s.rowp.p, 0, sizeof(uint32_t), c->st));
+  }
+  uint32_t mx = 0, dec = 0;  // one branch-free pass
+  for (uint32_t i = 0; i < G; ++i) {
+    const uint32_t a = v.graph_offsets[i], b = v.graph_offsets[i + 1];
+    dec |= uint32_t(b < a);
+    mx = std::max(mx, b - a);
+  }
+  if (dec || mx > limit) {
+    cudaStreamSynchronize(c->st);  // the caller's arrays are free again once this returns
+    if (dec) return fail(c, BMS_EINVAL, "graph_offsets must be non-decreasing");
+    return fail(c, BMS_EUNSUPPORTED,
+                std::string(name) + " graph with " + std::to_string(mx) + " nodes exceeds the limit of " + std::to_string(limit));
+  }
   s.G = G;
   s.N = N;
   s.E = E;
@@ -123,10 +143,6 @@ int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const 
     for (uint64_t i = 0; i < N; ++i)
       if (v.node_labels[i] < 16) s.labels_lt16 |= 1u << v.node_labels[i];
   if (!G) s.h_goff.assign(1, 0);
-  CK(s.goff.ensure(sizeof(uint32_t) * (G + 1)));
-  CK(s.rowp.ensure(sizeof(uint32_t) * (N + 1)));
-  CK(s.col.ensure(sizeof(uint32_t) * (E ? E : 1)));
-  CK(s.lab.ensure(N ? N : 1));
   // offsets that need no rebasing go straight from the caller's array (no
   // staging pass when it is page-locked, like the other arrays)
   CK(cudaMemcpyAsync(s.goff.p, G && !node_base ? v.graph_offsets : s.h_goff.data(), sizeof(uint32_t) * (G + 1),
@@ -140,17 +156,6 @@ int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const 
     CK(s.size_order.ensure(sizeof(uint32_t) * (G ? G : 1)));
     if (G)
       CK(cudaMemcpyAsync(s.size_order.p, s.h_size_order.data(), sizeof(uint32_t) * G, cudaMemcpyHostToDevice, c->st));
-  }
-  if (N) {
-    CK(cudaMemcpyAsync(s.rowp.p, v.row_offsets, sizeof(uint32_t) * (N + 1), cudaMemcpyHostToDevice, c->st));
-    CK(cudaMemcpyAsync(s.lab.p, v.node_labels, N, cudaMemcpyHostToDevice, c->st));
-  } else {
-    CK(cudaMemsetAsync(s.rowp.p, 0, sizeof(uint32_t), c->st));
-  }
-  if (E) {
-    CK(cudaMemcpyAsync(s.col.p, v.column_indices, sizeof(uint32_t) * E, cudaMemcpyHostToDevice, c->st));
-    // edge labels are never read by matching (the reference ignores them too,
-    // isomorphism.hpp:30-472): they are accepted but not copied to the device
   }
   if (N) CK(launch_rebase(s.rowp.as<uint32_t>(), N + 1, entry_base, s.col.as<uint32_t>(), E, node_base, c->st));
   CK(s.frec.ensure(sizeof(uint64_t) * kRecWords * (N ? N : 1)));

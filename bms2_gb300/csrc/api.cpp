@@ -561,13 +561,12 @@ int run_sliced_filter(bms_ctx* c, const ShellPack& sp, int R, int sem) {
   if (smem > (220u << 10)) return fail(c, BMS_EUNSUPPORTED, "too many queries for the sliced filter's shared memory");
   CK(launch_sliced_filter(a, 2, smem, c->st));
   CK(cudaMemcpyAsync(&a.ctr->recs_wide, &a.ctr->recs, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, c->st));
-  // one-word graphs
-  smem = sliced_smem_bytes(a, 1);
+  // one-word graphs: 33..64 nodes in 64-bit masks, <= 32 nodes in 32-bit masks
   for (int k = 1; k >= 0; --k) {
     a.class_begin = c->class_begin[k];
     a.class_end = c->class_end[k];
     a.class_id = k;
-    CK(launch_sliced_filter(a, 1, smem, c->st));
+    CK(launch_sliced_filter(a, k, sliced_smem_bytes(a, k), c->st));
     if (k == 1)
       CK(cudaMemcpyAsync(&a.ctr->recs_mid, &a.ctr->recs, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, c->st));
   }

@@ -247,6 +247,8 @@ cudaError_t launch_screen(const DGraphs& q, const DSigs& qs, const uint32_t* qor
 // Per (query, level) descriptors of the sliced filter (after query_prep and the programs).
 cudaError_t launch_level_desc(const DGraphs& q, const uint8_t* filter_order, const uint8_t* dup,
                               const uint32_t* prog_off, const uint8_t* slow, uint2* desc, cudaStream_t st);
+// words: 64-bit words per node mask (1: graphs of 33..64 nodes, 2: 65..128),
+// or 0 for 32-bit masks (graphs of <= 32 nodes).
 cudaError_t launch_sliced_filter(const SlicedArgs& a, int words, size_t smem, cudaStream_t st);
 
 // exclusive scan of n uint32 values into out[0..n] (out[n] = total); scratch

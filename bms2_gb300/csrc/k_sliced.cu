@@ -30,36 +30,63 @@ constexpr uint32_t kMaxMaskIds = kClauseIds;  // 2240
 constexpr uint8_t kSlowLabel = 1, kSlowDeg = 2, kSlowCyc = 4;
 constexpr uint32_t kNoRow = 0xFFFFFFFFu;
 
+// Node masks of one data graph: W 64-bit words (graphs of up to 64 W nodes),
+// or for W = 0 one 32-bit word (graphs of up to 32 nodes: half the mask table
+// and one 32-bit operation per mask AND).
+template <int W>
+struct MaskWord {
+  using T = uint64_t;
+  static constexpr int n = W;
+  static constexpr uint32_t bits = 64;
+};
+template <>
+struct MaskWord<0> {
+  using T = uint32_t;
+  static constexpr int n = 1;
+  static constexpr uint32_t bits = 32;
+};
 template <int W>
 struct Mask {
-  uint64_t w[W];
+  typename MaskWord<W>::T w[MaskWord<W>::n];
 };
+template <int W>
+constexpr uint32_t kMaxNodesOf = W == 0 ? 32u : 64u * W;
+template <int W>
+constexpr uint32_t kHalvesOf = W == 0 ? 1u : 2u * W;  // 32-bit chunks per mask
 template <int W>
 __device__ __forceinline__ Mask<W> mand(Mask<W> a, Mask<W> b) {
 #pragma unroll
-  for (int i = 0; i < W; ++i) a.w[i] &= b.w[i];
+  for (int i = 0; i < MaskWord<W>::n; ++i) a.w[i] &= b.w[i];
   return a;
 }
 template <int W>
 __device__ __forceinline__ bool many(Mask<W> a) {
-  uint64_t x = 0;
+  typename MaskWord<W>::T x = 0;
 #pragma unroll
-  for (int i = 0; i < W; ++i) x |= a.w[i];
+  for (int i = 0; i < MaskWord<W>::n; ++i) x |= a.w[i];
   return x != 0;
 }
 template <int W>
 __device__ __forceinline__ Mask<W> mlow(uint32_t m) {
+  using T = typename MaskWord<W>::T;
+  constexpr uint32_t B = MaskWord<W>::bits;
   Mask<W> r;
 #pragma unroll
-  for (int i = 0; i < W; ++i) {
-    const uint32_t lo = 64u * i;
-    r.w[i] = m <= lo ? 0ull : (m >= lo + 64 ? ~0ull : ((uint64_t(1) << (m - lo)) - 1));
+  for (int i = 0; i < MaskWord<W>::n; ++i) {
+    const uint32_t lo = B * i;
+    r.w[i] = m <= lo ? T(0) : (m >= lo + B ? ~T(0) : T((T(1) << (m - lo)) - 1));
   }
   return r;
 }
 template <int W>
+__device__ __forceinline__ void mclear(Mask<W>& a, uint32_t v) {
+  using T = typename MaskWord<W>::T;
+  constexpr uint32_t B = MaskWord<W>::bits;
+  a.w[v / B] &= ~(T(1) << (v % B));
+}
+template <int W>
 __device__ __forceinline__ B128 to128(Mask<W> a) {
-  return W == 1 ? B128{a.w[0], 0ull} : B128{a.w[0], a.w[W - 1]};
+  return W <= 1 ? B128{uint64_t(a.w[0]), 0ull} : B128{a.w[0], a.w[MaskWord<W>::n - 1]};
 }
 
 // ------------------------------------------------------------- query side
@@ -211,8 +238,8 @@ __device__ __forceinline__ bool eval_node(const SlicedArgs& a, const GraphCtx<W>
   if (src != 0xFFu) {  // same record as an earlier, non-empty row
     if (row0 != kNoRow) {
       const B128 c = ld_b128(a.arena + 2 * (uint64_t(row0) + src));
-      row.w[0] = c.lo;
-      if (W > 1) row.w[W - 1] = c.hi;
+      row.w[0] = typename MaskWord<W>::T(c.lo);
+      if (W > 1) row.w[MaskWord<W>::n - 1] = c.hi;
     }
     return true;
   }
@@ -238,7 +265,7 @@ __device__ __forceinline__ bool eval_node(const SlicedArgs& a, const GraphCtx<W>
         ok = ok && uint32_t(dr[0] >> 32) >= qd;
       }
       if (slow & kSlowCyc) ok = ok && cyc_ge(g.cyc[v], rec1);
-      if (!ok) row.w[v >> 6] &= ~(uint64_t(1) << (v & 63u));
+      if (!ok) mclear(row, v);
     }
   }
   return many(row);
@@ -264,16 +291,16 @@ template <int W>
 __device__ __forceinline__ void put_chunk(uint32_t* tab32, const uint32_t* used, const uint16_t* remap, uint32_t id,
                                           uint32_t ch, uint32_t bits, uint32_t zero_from) {
   if ((used[id >> 5] >> (id & 31u)) & 1u) {
-    uint32_t* p = tab32 + uint32_t(remap[id]) * (2 * W);
+    uint32_t* p = tab32 + uint32_t(remap[id]) * kHalvesOf<W>;
     p[ch] = bits;
-    for (uint32_t z = zero_from; z < 2 * W; ++z) p[z] = 0;
+    for (uint32_t z = zero_from; z < kHalvesOf<W>; ++z) p[z] = 0;
   }
 }
 
 template <int W>
 __global__ void __launch_bounds__(256) sliced_filter_kernel(SlicedArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  constexpr uint32_t MAXN = 64 * W;
+  constexpr uint32_t MAXN = kMaxNodesOf<W>;
   const int R = a.ds.R;
   // shared layout
   uint64_t* s_path = reinterpret_cast<uint64_t*>(smem);            // [MAXN*4]
@@ -298,7 +325,7 @@ __global__ void __launch_bounds__(256) sliced_filter_kernel(SlicedArgs a) {
   if (tid == 0) {  // the all-ones mask that pads programs; used masks never overwrite it
     Mask<W> ones;
 #pragma unroll
-    for (int x = 0; x < W; ++x) ones.w[x] = ~0ull;
+    for (int x = 0; x < MaskWord<W>::n; ++x) ones.w[x] = ~typename MaskWord<W>::T(0);
     s_tab[min(*a.n_used, a.n_used_cap - 1)] = ones;
   }
   for (;;) {
@@ -344,7 +371,7 @@ __global__ void __launch_bounds__(256) sliced_filter_kernel(SlicedArgs a) {
         const uint32_t item = it / chunks, ch = it - item * chunks;
         const uint32_t v = ch * 32 + lane;
         const bool in = v < m;
-        const uint32_t zero_from = ch + 1 == chunks ? chunks : 2 * W;  // halves past the graph
+        const uint32_t zero_from = ch + 1 == chunks ? chunks : kHalvesOf<W>;  // halves past the graph
         uint32_t row = 0, id = 0;
         bool used = false;
         if (item < 10) {
@@ -522,10 +549,10 @@ __global__ void __launch_bounds__(256) sliced_filter_kernel(SlicedArgs a) {
 
 template <int W>
 size_t sliced_smem(const SlicedArgs& a) {
-  constexpr size_t MAXN = 64 * W;
+  constexpr size_t MAXN = kMaxNodesOf<W>;
   const size_t R = size_t(a.ds.R > 0 ? a.ds.R : 1);
   size_t b = 8 * (4 * MAXN + MAXN + MAXN * R);
-  b += sizeof(uint64_t) * W * (a.n_used_cap ? a.n_used_cap : 1);
+  b += sizeof(Mask<W>) * (a.n_used_cap ? a.n_used_cap : 1);
   b += 4 * (4 * size_t(a.q.G) + a.QW);
   b += 2 * MAXN;
   return (b + 15) & ~size_t(15);
@@ -533,7 +560,9 @@ size_t sliced_smem(const SlicedArgs& a) {
 
 }  // namespace
 
-size_t sliced_smem_bytes(const SlicedArgs& a, int words) { return words == 1 ? sliced_smem<1>(a) : sliced_smem<2>(a); }
+size_t sliced_smem_bytes(const SlicedArgs& a, int words) {
+  return words == 0 ? sliced_smem<0>(a) : (words == 1 ? sliced_smem<1>(a) : sliced_smem<2>(a));
+}
 
 cudaError_t launch_query_programs(const DGraphs& q, const DSigs& qs, ShellPack sp, uint32_t* len, uint32_t* prog_off,
                                   uint32_t* scan_scratch, uint32_t* used, uint16_t* remap, uint16_t* used_ids,
@@ -573,7 +602,10 @@ cudaError_t launch_sliced_filter(const SlicedArgs& a, int words, size_t smem, cu
   const uint32_t graphs = a.class_end - a.class_begin;
   const uint64_t per_sm = smem ? std::max<uint64_t>(1, std::min<uint64_t>(8, (200u << 10) / smem)) : 8;
   const unsigned blocks = unsigned(std::min<uint64_t>(graphs, uint64_t(sm_count()) * per_sm));
-  if (words == 1) {
+  if (words == 0) {
+    cudaFuncSetAttribute(sliced_filter_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    sliced_filter_kernel<0><<<blocks, 256, smem, st>>>(a); note_launch();
+  } else if (words == 1) {
     cudaFuncSetAttribute(sliced_filter_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     sliced_filter_kernel<1><<<blocks, 256, smem, st>>>(a); note_launch();
   } else {

@@ -14,8 +14,8 @@
 namespace bms {
 namespace {
 
-constexpr int kWarps = 4;  // ~9.8 KB of shared memory per warp
-constexpr int kMaxEntries = 1024;  // CSR entries staged per graph; larger rows read global memory
+constexpr int kWarps = 4;  // ~10.4 KB of shared memory per warp: five blocks fit an SM
+constexpr int kMaxEntries = 512;  // CSR entries staged per graph; larger rows read global memory
 
 struct WarpSmem {
   B128 adj[kMaxDataNodes];      // out-neighbour set of every node (row as a set)
@@ -27,6 +27,7 @@ struct WarpSmem {
   B128 labmask[16];
   alignas(16) uint32_t cyc[kMaxDataNodes][4];  // cycle closures per node (canonical enumeration)
   uint16_t first[kMaxDataNodes + 1];  // canonical enumeration: offsets of the (s0, a) work items
+  alignas(16) uint32_t bloom[32][8];  // per lane: the path filter of its current node, 32-bit words
 };
 
 // CSR row access of the current graph with local ids, from shared memory when
@@ -364,7 +365,11 @@ __global__ void __launch_bounds__(kWarps * 32) signatures_kernel(DGraphs g, DSig
       // path signature: walks v-a-w (w != v) and v-a-w-x (x != a, x != v), as
       // one flat loop with one Bloom insert per iteration, so lanes whose nodes
       // have different neighbourhoods still hash in step (inserts commute)
-      uint64_t p0 = 0, p1 = 0, p2 = 0, p3 = 0;
+      // the filter's bits accumulate in the lane's own shared words (one OR per
+      // position, PathSignatureDevice::insert, signature.hpp:418-430)
+      uint32_t* bl = s.bloom[lane];
+      reinterpret_cast<uint4*>(bl)[0] = make_uint4(0, 0, 0, 0);
+      reinterpret_cast<uint4*>(bl)[1] = make_uint4(0, 0, 0, 0);
       {
         const B128 bv = b_bit(v);
         B128 ra = s.adj[v], rw{0, 0}, rx{0, 0};
@@ -387,9 +392,18 @@ __global__ void __launch_bounds__(kWarps * 32) signatures_kernel(DGraphs g, DSig
             h = h2;
             rx = b_andn(s.adj[w], b_or(b_bit(a), bv));
           }
-          bloom_insert(p0, p1, p2, p3, fmix32(h));
+          uint32_t x = fmix32(h);
+#pragma unroll
+          for (int r = 0; r < 3; ++r) {
+            const uint32_t idx = x & 255u;
+            atomicOr(&bl[idx >> 5], 1u << (idx & 31u));
+            x = fmix32(x);
+          }
         }
       }
+      const uint4 bq0 = reinterpret_cast<const uint4*>(bl)[0], bq1 = reinterpret_cast<const uint4*>(bl)[1];
+      const uint64_t p0 = uint64_t(bq0.x) | (uint64_t(bq0.y) << 32), p1 = uint64_t(bq0.z) | (uint64_t(bq0.w) << 32);
+      const uint64_t p2 = uint64_t(bq1.x) | (uint64_t(bq1.y) << 32), p3 = uint64_t(bq1.z) | (uint64_t(bq1.w) << 32);
       // cycle signature
       uint32_t c[4] = {0, 0, 0, 0};
       if (canonical) {

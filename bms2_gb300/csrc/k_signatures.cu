@@ -376,9 +376,11 @@ __global__ void __launch_bounds__(kWarps * 32) signatures_kernel(DGraphs g, DSig
         uint32_t a = 0, h2 = 0;
         while (true) {
           uint32_t h;
-          if (b_any(rx)) {  // next x of the current v-a-w
-            h = hcombine(h2, s.lab[b_low(rx)]);
-            rx = b_clear_low(rx);
+          if (b_any(rx)) {  // next x of the current v-a-w; the hash depends on x's
+            // label only, so every other x of that label is dropped with it
+            const uint32_t lx = s.lab[b_low(rx)];
+            h = hcombine(h2, lx);
+            rx = lx < 16 ? b_andn(rx, s.labmask[lx]) : b_clear_low(rx);
           } else {  // next w, moving on to the next a with a continuation
             while (!b_any(rw) && b_any(ra)) {
               a = b_low(ra);

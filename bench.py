@@ -121,6 +121,28 @@ def algorithmic_filter_bytes(qn: int, dn: int, R: int) -> float:
     return qn * dn / 8.0 + (dn + qn) * (45.0 + 8.0 * R)
 
 
+def graph_offsets(g) -> np.ndarray:
+    """graph_offsets of a Graphs batch as a numpy view (no copy of the batch)."""
+    v = g.view()
+    if v.n_graphs == 0:
+        return np.zeros(1, dtype=np.uint32)
+    return np.ctypeslib.as_array(v.graph_offsets, shape=(v.n_graphs + 1,))
+
+
+def outside_reference_domain(q_offsets, d_offsets) -> dict:
+    """Share of a workload outside the reference's sizes: its bitsets and
+    join arrays hold data graphs of <= 64 nodes and queries of <= 30 nodes
+    (utils.hpp:90-120, isomorphism.hpp:248).  Pairs are the full cross
+    product, so the pairs with either side beyond those sizes are
+    1 - (data share inside) x (query share inside)."""
+    dsz = np.diff(np.asarray(d_offsets, dtype=np.int64))
+    qsz = np.diff(np.asarray(q_offsets, dtype=np.int64))
+    d_in = float(np.mean(dsz <= 64)) if len(dsz) else 1.0
+    q_in = float(np.mean(qsz <= 30)) if len(qsz) else 1.0
+    return {"data_graphs_over_64_nodes": 1.0 - d_in, "queries_over_30_nodes": 1.0 - q_in,
+            "pairs": 1.0 - d_in * q_in}
+
+
 def algorithmic_signature_bytes(nodes: int, entries: int, R: int) -> float:
     """Compulsory bytes of the data and query signatures: row offsets and labels
     (4 + 1 per node) and the CSR column ids (4 per entry) read once, and per
@@ -359,7 +381,8 @@ def run_ours(args) -> None:
                                f"count-all, EXACT semantics, order {args.order}",
                    "data_graphs_per_gpu": D, "queries": Q, "refine_steps": REFINE_STEPS, "order": args.order,
                    "l2": "flushed between steps (512 MiB write outside the timed events)",
-                   "parallelism": f"data-graph shards x{world}"},
+                   "parallelism": f"data-graph shards x{world}",
+                   "outside_reference_domain": outside_reference_domain(qa["graph_offsets"], da["graph_offsets"])},
         "e2e": {"value": world * pairs / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": int(T * 8)},
         "roofline": {"kernel": "sliced_filter (fused filter + refine + GMCR validity)", "bound": "hbm",
@@ -512,7 +535,8 @@ def run_streamed(args) -> None:
                                f"of {args.slice}, refine steps {REFINE_STEPS}, count-all, EXACT, order {args.order}",
                    "data_graphs_per_gpu": D, "queries": Q, "slice_graphs": args.slice, "order": args.order,
                    "l2": "inputs far larger than L2 (every window is processed once per pass)",
-                   "parallelism": f"data-graph shards x{world}"},
+                   "parallelism": f"data-graph shards x{world}",
+                   "outside_reference_domain": outside_reference_domain(graph_offsets(q), graph_offsets(d))},
         "e2e": {"value": world * pairs / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 8 * Q,
                 "note": "one pass through bms_run_batches: every slice uploaded from page-locked host memory "
                         "inside it (after one untimed pass)"},
@@ -666,7 +690,8 @@ def run_clustered(args) -> None:
                                f"refine steps {REFINE_STEPS}, count-all, EXACT, clustered join (--use-cs)",
                    "data_graphs_per_gpu": D, "queries": Q, "refine_steps": REFINE_STEPS, "order": "plain",
                    "l2": "flushed between steps (512 MiB write outside the timed events)",
-                   "parallelism": f"data-graph shards x{world}"},
+                   "parallelism": f"data-graph shards x{world}",
+                   "outside_reference_domain": outside_reference_domain(qa["graph_offsets"], da["graph_offsets"])},
         "e2e": {"value": world * pairs / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": int(T * 8)},
         "roofline": {"kernel": "sliced_filter (fused filter + refine + GMCR validity)", "bound": "hbm",

@@ -176,3 +176,18 @@ def test_status_names():
     assert L.bms_status_name(-5) == b"BMS_ESTATE"
     assert L.bms_feature_name(0) == b"log2_mean_candidates"
     assert len(native.feature_names()) == 12
+
+
+def test_outside_reference_domain_shares():
+    import bench
+
+    q = [0, 3, 33, 40]  # query sizes 3, 30, 7: none above 30
+    d = [0, 64, 129, 139, 139]  # data sizes 64, 65, 10, 0: one of four above 64
+    got = bench.outside_reference_domain(q, d)
+    assert got == {"data_graphs_over_64_nodes": 0.25, "queries_over_30_nodes": 0.0, "pairs": 0.25}
+    got = bench.outside_reference_domain([0, 31, 32], d)  # one of two queries above 30
+    assert got["queries_over_30_nodes"] == 0.5 and got["pairs"] == 1.0 - 0.75 * 0.5
+    g = Graphs.synth_molecules(50, 3, 0, 0, 0, 60, 70, 1, 4)
+    off = bench.graph_offsets(g)
+    assert np.array_equal(off, g.arrays()["graph_offsets"])
+    assert bench.outside_reference_domain([0, 5], off)["data_graphs_over_64_nodes"] > 0

@@ -83,7 +83,7 @@ def build_oracle(force: bool = False) -> Path:
     src = ORACLE_DIR / "oracle.cpp"
     if force or _stale(ORACLE_LIB, [src]):
         cxx = shutil.which("g++") or "g++"
-        _run([cxx, "-std=c++17", "-O2", "-fopenmp", "-fPIC", "-shared", str(src), "-o", str(ORACLE_LIB)])
+        _run([cxx, "-std=c++17", "-O3", "-fopenmp", "-fPIC", "-shared", str(src), "-o", str(ORACLE_LIB)])
     return ORACLE_LIB
 
 

@@ -12,11 +12,13 @@
 //   shell k nibble of label l >= c                  -> SHELL[k][l][c]
 // So for one data graph, the candidate row of a query node is the AND of the
 // node masks of the clauses its own signature selects.  A block owns one data
-// graph at a time: it builds, in shared memory, the masks any query uses (one
-// thread per mask, a loop over the graph's nodes), then evaluates the queries
-// level by level in their selectivity order with one thread per still-alive
-// query: each evaluation is a walk over the query node's precomputed clause
-// list ("program"), ANDing 64- or 128-bit masks.  A query dies at its first
+// graph at a time: it builds, in shared memory, the masks any query uses (a
+// warp per clause family and 32-node chunk, bit-transposed across the warp),
+// then evaluates the queries level by level in their selectivity order with
+// one thread per still-alive query: each evaluation is a walk over the query
+// node's precomputed clause list ("program"), ANDing node masks of 32 bits
+// (graphs of <= 32 nodes), 64 bits (<= 64) or 128 bits, one launch per size
+// class.  A query dies at its first
 // empty row; its output rows are allocated once its first row is non-empty.
 // Queries whose label multiset cannot embed (EXACT semantics) keep being tested
 // for GMCR validity but write no rows and reach no join.

@@ -1,7 +1,8 @@
 // Mapping and bookkeeping kernels: GMCR offsets and query indices (gmcr.hpp:
 // 92-127, with a parallel scan in place of the reference's single-work-item
-// prefix sum), query preparation, search orders, task emission, totals and the
-// scatter of per-pair results into GMCR order.
+// prefix sum), query preparation, search orders, task emission, totals, the
+// scatter of per-pair results into GMCR order, and the grouping of a data
+// batch's graphs by size class at upload.
 #include "device_common.cuh"
 
 namespace bms {

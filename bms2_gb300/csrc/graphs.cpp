@@ -23,30 +23,35 @@ void append_graph(bms_graphs& g, const std::vector<uint8_t>& labels, const std::
   const uint32_t n = uint32_t(labels.size());
   const uint32_t node_base = uint32_t(g.lab.size());
   const uint32_t entry_base = uint32_t(g.col.size());
-  std::vector<uint32_t> rows(n + 1, 0);
+  // rows[i]: start of node i's row (local), then its fill cursor
+  thread_local std::vector<uint32_t> rows;
+  rows.assign(size_t(n) + 1, 0);
   for (const Edge& e : edges) {
     rows[std::get<0>(e) + 1]++;
     rows[std::get<1>(e) + 1]++;
   }
   for (uint32_t i = 1; i <= n; ++i) rows[i] += rows[i - 1];
   const uint32_t entries = rows[n];
-  std::vector<uint32_t> col(entries, 0);
-  std::vector<uint8_t> el(entries, 0);
-  std::vector<uint32_t> pos(n + 1, 0);
+  const size_t r0 = g.rowp.size();
+  g.rowp.resize(r0 + n);
+  for (uint32_t i = 0; i < n; ++i) g.rowp[r0 + i] = entry_base + rows[i + 1];
+  // an entry never written (the second slot of a self-loop) holds local id 0
+  g.col.resize(size_t(entry_base) + entries, node_base);
+  g.elab.resize(size_t(entry_base) + entries, 0);
+  uint32_t* col = g.col.data() + entry_base;
+  uint8_t* el = g.elab.data() + entry_base;
   for (const Edge& e : edges) {
+    // both ends are written before either cursor moves (graph.hpp:229-240): a
+    // self-loop writes one slot twice and skips the next
     const uint32_t a = std::get<0>(e), b = std::get<1>(e);
     const uint8_t l = std::get<2>(e);
-    col[rows[a] + pos[a]] = b;
-    el[rows[a] + pos[a]] = l;
-    col[rows[b] + pos[b]] = a;
-    el[rows[b] + pos[b]] = l;
-    pos[a]++;
-    pos[b]++;
-  }
-  for (uint32_t i = 0; i < n; ++i) g.rowp.push_back(entry_base + rows[i + 1]);
-  for (uint32_t i = 0; i < entries; ++i) {
-    g.col.push_back(node_base + col[i]);
-    g.elab.push_back(el[i]);
+    const uint32_t ia = rows[a], ib = rows[b];
+    col[ia] = node_base + b;
+    el[ia] = l;
+    col[ib] = node_base + a;
+    el[ib] = l;
+    rows[a]++;
+    rows[b]++;
   }
   g.lab.insert(g.lab.end(), labels.begin(), labels.end());
   g.goff.push_back(node_base + n);
@@ -138,7 +143,8 @@ bool parse_line(const char* s, size_t len, std::vector<uint8_t>& labels, std::ve
     err = "expected e#<edges>";
     return false;
   }
-  std::vector<std::pair<const char*, size_t>> toks;
+  thread_local std::vector<std::pair<const char*, size_t>> toks;
+  toks.clear();
   const char* b;
   size_t k;
   while (t.next(b, k)) toks.emplace_back(b, k);
@@ -176,9 +182,10 @@ using bms::set_thread_error;
 namespace {
 
 // Serial parse of one buffer; a malformed line is reported with its number
-// counted from first_line.
+// counted from first_line, or (bad_line given) that number is stored there and
+// the message carries only ": <reason>".
 int parse_serial(const char* text, size_t len, uint32_t max_graphs, int skip_invalid, size_t first_line,
-                 bms_graphs** out) {
+                 bms_graphs** out, size_t* bad_line = nullptr) {
   if (!out) return BMS_EINVAL;
   *out = nullptr;
   bms_graphs* g = new (std::nothrow) bms_graphs();
@@ -211,7 +218,12 @@ int parse_serial(const char* text, size_t len, uint32_t max_graphs, int skip_inv
           bms::append_graph(*g, labels, edges);
         } else if (!skip_invalid) {
           delete g;
-          set_thread_error("line " + std::to_string(line_no) + ": " + err);
+          if (bad_line) {  // the caller numbers the line
+            *bad_line = line_no;
+            set_thread_error(": " + err);
+          } else {
+            set_thread_error("line " + std::to_string(line_no) + ": " + err);
+          }
           return BMS_EINVAL;
         }
       }
@@ -226,19 +238,38 @@ int parse_serial(const char* text, size_t len, uint32_t max_graphs, int skip_inv
   return BMS_OK;
 }
 
-// Append batch b to a (ids rebased); false if the 32-bit id space overflows.
-bool append_batch(bms_graphs& a, const bms_graphs& b) {
-  const uint64_t n0 = a.lab.size(), e0 = a.col.size();
-  if (n0 + b.lab.size() > 0xFFFFFFF0ull || e0 + b.col.size() > 0xFFFFFFF0ull) return false;
-  a.goff.reserve(a.goff.size() + b.n_graphs());
-  for (size_t i = 1; i < b.goff.size(); ++i) a.goff.push_back(uint32_t(n0 + b.goff[i]));
-  a.rowp.reserve(a.rowp.size() + b.lab.size());
-  for (size_t i = 1; i < b.rowp.size(); ++i) a.rowp.push_back(uint32_t(e0 + b.rowp[i]));
-  a.col.reserve(e0 + b.col.size());
-  for (uint32_t c : b.col) a.col.push_back(uint32_t(n0 + c));
-  a.lab.insert(a.lab.end(), b.lab.begin(), b.lab.end());
-  a.elab.insert(a.elab.end(), b.elab.begin(), b.elab.end());
-  a.max_nodes = std::max(a.max_nodes, b.max_nodes);
+// Concatenate the pieces of a parallel parse into one batch (ids rebased):
+// the result is sized once and every piece copies its part in its own
+// thread.  False if the 32-bit id space overflows.
+bool merge_batches(const std::vector<bms_graphs*>& part, bms_graphs& g) {
+  const size_t n = part.size();
+  std::vector<uint64_t> g0(n + 1, 0), n0(n + 1, 0), e0(n + 1, 0);
+  for (size_t k = 0; k < n; ++k) {
+    g0[k + 1] = g0[k] + part[k]->n_graphs();
+    n0[k + 1] = n0[k] + part[k]->lab.size();
+    e0[k + 1] = e0[k] + part[k]->col.size();
+  }
+  if (n0[n] > 0xFFFFFFF0ull || e0[n] > 0xFFFFFFF0ull) return false;
+  g.goff.assign(g0[n] + 1, 0);
+  g.rowp.assign(n0[n] + 1, 0);
+  g.col.resize(e0[n]);
+  g.lab.resize(n0[n]);
+  g.elab.resize(e0[n]);
+  g.max_nodes = 0;
+  for (const bms_graphs* b : part) g.max_nodes = std::max(g.max_nodes, b->max_nodes);
+  auto copy = [&](size_t k) {
+    const bms_graphs& b = *part[k];
+    const uint32_t nb = uint32_t(n0[k]), eb = uint32_t(e0[k]);
+    for (size_t i = 1; i < b.goff.size(); ++i) g.goff[g0[k] + i] = nb + b.goff[i];
+    for (size_t i = 1; i < b.rowp.size(); ++i) g.rowp[n0[k] + i] = eb + b.rowp[i];
+    for (size_t i = 0; i < b.col.size(); ++i) g.col[e0[k] + i] = nb + b.col[i];
+    std::copy(b.lab.begin(), b.lab.end(), g.lab.begin() + ptrdiff_t(n0[k]));
+    std::copy(b.elab.begin(), b.elab.end(), g.elab.begin() + ptrdiff_t(e0[k]));
+  };
+  std::vector<std::thread> pool;
+  for (size_t k = 1; k < n; ++k) pool.emplace_back(copy, k);
+  copy(0);
+  for (auto& t : pool) t.join();
   return true;
 }
 
@@ -261,41 +292,52 @@ int parse_buffer(const char* text, size_t len, uint32_t max_graphs, int skip_inv
   }
   cut.push_back(len);
   const size_t n = cut.size() - 1;
-  std::vector<size_t> lines(n + 1, 0);  // lines before each piece
-  for (size_t k = 0; k < n; ++k) {
-    size_t c = 0;
-    for (const char* q = text + cut[k]; q < text + cut[k + 1]; ++q) c += *q == '\n';
-    lines[k + 1] = lines[k] + c;
-  }
   std::vector<bms_graphs*> part(n, nullptr);
   std::vector<int> status(n, BMS_OK);
+  std::vector<size_t> lines(n, 0), bad_line(n, 0);  // lines of each piece; a malformed line's number in it
   std::vector<std::string> msg(n);
   std::vector<std::thread> pool;
   for (size_t k = 0; k < n; ++k)
     pool.emplace_back([&, k] {
-      status[k] = parse_serial(text + cut[k], cut[k + 1] - cut[k], 0, skip_invalid, lines[k], &part[k]);
+      const char* b = text + cut[k];
+      const size_t m = cut[k + 1] - cut[k];
+      status[k] = parse_serial(b, m, 0, skip_invalid, 0, &part[k], &bad_line[k]);
       if (status[k] != BMS_OK) msg[k] = bms::thread_error();
+      lines[k] = size_t(std::count(b, b + m, '\n'));
     });
   for (auto& t : pool) t.join();
   int r = BMS_OK;
-  for (size_t k = 0; k < n && r == BMS_OK; ++k)
+  size_t before = 0;  // lines before piece k
+  for (size_t k = 0; k < n && r == BMS_OK; ++k) {
     if (status[k] != BMS_OK) {
       r = status[k];
-      set_thread_error(msg[k]);
+      // a malformed line: its number counted from the start of the buffer
+      set_thread_error(bad_line[k] ? "line " + std::to_string(before + bad_line[k]) + msg[k] : msg[k]);
     }
-  bms_graphs* g = r == BMS_OK ? part[0] : nullptr;
+    before += lines[k];
+  }
+  bms_graphs* g = nullptr;
+  if (r == BMS_OK) {
+    g = new (std::nothrow) bms_graphs();
+    if (!g) {
+      set_thread_error("out of host memory while parsing");
+      r = BMS_ENOMEM;
+    }
+  }
   try {
-    for (size_t k = 1; k < n && r == BMS_OK; ++k)
-      if (!append_batch(*g, *part[k])) {
-        set_thread_error("batch exceeds 32-bit node or entry ids");
-        r = BMS_EUNSUPPORTED;
-      }
+    if (r == BMS_OK && !merge_batches(part, *g)) {
+      set_thread_error("batch exceeds 32-bit node or entry ids");
+      r = BMS_EUNSUPPORTED;
+    }
   } catch (const std::bad_alloc&) {
     set_thread_error("out of host memory while parsing");
     r = BMS_ENOMEM;
   }
-  for (size_t k = (r == BMS_OK ? 1 : 0); k < n; ++k) delete part[k];
-  if (r != BMS_OK) return r;
+  for (bms_graphs* b : part) delete b;
+  if (r != BMS_OK) {
+    delete g;
+    return r;
+  }
   *out = g;
   return BMS_OK;
 }
@@ -334,17 +376,38 @@ int bms_graphs_parse_file(const char* path, uint32_t max_graphs, int skip_invali
     set_thread_error(std::string("cannot open ") + path + ": " + std::strerror(errno));
     return BMS_EIO;
   }
-  std::string buf;
-  char chunk[1 << 16];
-  size_t k;
-  while ((k = std::fread(chunk, 1, sizeof chunk, f)) > 0) buf.append(chunk, k);
+  // one read of the file's size where it has one, then any remainder in chunks
+  std::vector<char> buf;
+  size_t len = 0;
+  if (std::fseek(f, 0, SEEK_END) == 0) {
+    const long sz = std::ftell(f);
+    if (sz > 0) buf.reserve(size_t(sz));
+    std::rewind(f);
+  }
+  try {
+    if (buf.capacity()) {
+      buf.resize(buf.capacity());
+      len = std::fread(buf.data(), 1, buf.size(), f);
+    }
+    char chunk[1 << 16];
+    size_t k;
+    while ((k = std::fread(chunk, 1, sizeof chunk, f)) > 0) {
+      if (len + k > buf.size()) buf.resize(std::max(buf.size() * 2, len + k));
+      std::memcpy(buf.data() + len, chunk, k);
+      len += k;
+    }
+  } catch (const std::bad_alloc&) {
+    std::fclose(f);
+    set_thread_error("out of host memory while reading");
+    return BMS_ENOMEM;
+  }
   bool bad = std::ferror(f) != 0;
   std::fclose(f);
   if (bad) {
     set_thread_error(std::string("read error on ") + path);
     return BMS_EIO;
   }
-  return parse_buffer(buf.data(), buf.size(), max_graphs, skip_invalid, out);
+  return parse_buffer(buf.data(), len, max_graphs, skip_invalid, out);
 }
 
 int bms_graphs_from_csr(uint32_t G, const uint32_t* goff, const uint32_t* rowp, const uint32_t* col,

@@ -110,6 +110,14 @@ def test_parallel_parse_equals_serial_parse(tmp_path):
     assert msgs[0] == msgs[1] and f"line {bad + 1}:" in msgs[0]
     skipped = Graphs.parse_file(path, skip_invalid=True)
     assert skipped.n_graphs == d.n_graphs - 1
+    # a malformed line in the first and in a middle piece keeps its number too
+    for bad2 in (4, len(lines) // 2):
+        lines2 = list(lines)
+        lines2[bad2] = b"n#3 l#3 0 8 1 8"
+        path.write_bytes(b"\n".join(lines2))
+        with pytest.raises(BmsError) as e:
+            Graphs.parse_file(path)
+        assert f"line {bad2 + 1}:" in str(e.value)
 
 
 def test_parse_file_missing_is_eio(tmp_path):

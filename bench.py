@@ -357,6 +357,7 @@ def run_ours(args) -> None:
     peak, peak_kind = peaks()
     fbytes = algorithmic_filter_bytes(st["n_query_nodes"], st["n_data_nodes"], REFINE_STEPS)
     f_ms = float(np.mean([s["ms_filter"] for s in stage]))
+    j_ms = float(np.mean([s["ms_join"] for s in stage]))
     achieved = fbytes / (f_ms / 1e3) / 1e9
     sig_bytes = algorithmic_signature_bytes(int(st["n_data_nodes"] + st["n_query_nodes"]),
                                             int(len(da["column_indices"]) + len(qa["column_indices"])), REFINE_STEPS)
@@ -394,6 +395,11 @@ def run_ours(args) -> None:
                                 "achieved": sig_gbs, "peak": peak, "unit": "GB/s", "frac": sig_gbs / peak,
                                 "algorithmic_bytes": sig_bytes, "ms": sig_ms,
                                 "note": "instruction-bound: profiles/signatures_mol1m_100k.md"},
+        "join": {"kernel": "join_kernel (three size classes side by side)", "bound": "latency",
+                 "ms": j_ms, "expansions_per_step": int(st["expansions"]),
+                 "expansions_per_s": float(st["expansions"]) / max(j_ms / 1e3, 1e-9),
+                 "note": "no HBM or tensor roofline: a DFS bound by latency and integer issue, "
+                         "10-14 of 32 lanes active (profiles/join_mol1m_100k.md)"},
         "stage_ms": {k: float(np.mean([s[k] for s in stage])) for k in
                      ("ms_signatures", "ms_filter", "ms_map", "ms_order", "ms_join", "ms_total")},
         "clocks": clk,

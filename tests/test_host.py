@@ -199,3 +199,21 @@ def test_outside_reference_domain_shares():
     off = bench.graph_offsets(g)
     assert np.array_equal(off, g.arrays()["graph_offsets"])
     assert bench.outside_reference_domain([0, 5], off)["data_graphs_over_64_nodes"] > 0
+
+
+def test_parallel_parse_with_empty_pieces():
+    # 40 MiB of blank lines between two halves: the middle pieces of the
+    # parallel parse hold no graph and must merge to the serial result
+    d = Graphs.synth_molecules(2000, 19, 0, 0, 0, 10, 40, 1, 4)
+    import tempfile, os
+    with tempfile.TemporaryDirectory() as t:
+        p = os.path.join(t, "g.txt")
+        d.write_file(p)
+        text = open(p, "rb").read()
+    lines = text.split(b"\n")
+    half = len(lines) // 2
+    buf = b"\n".join(lines[:half]) + b"\n" + b"\n" * (40 << 20) + b"\n".join(lines[half:])
+    par = Graphs.parse_text(buf).arrays()
+    ref = d.arrays()
+    for k in ref:
+        assert np.array_equal(par[k], ref[k]), k

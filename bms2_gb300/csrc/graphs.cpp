@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <system_error>
 #include <thread>
 #include <fstream>
 #include <new>
@@ -267,7 +268,13 @@ bool merge_batches(const std::vector<bms_graphs*>& part, bms_graphs& g) {
     std::copy(b.elab.begin(), b.elab.end(), g.elab.begin() + ptrdiff_t(e0[k]));
   };
   std::vector<std::thread> pool;
-  for (size_t k = 1; k < n; ++k) pool.emplace_back(copy, k);
+  for (size_t k = 1; k < n; ++k) {
+    try {
+      pool.emplace_back(copy, k);
+    } catch (const std::system_error&) {
+      copy(k);  // no thread to spare: this piece on the calling thread
+    }
+  }
   copy(0);
   for (auto& t : pool) t.join();
   return true;
@@ -296,15 +303,21 @@ int parse_buffer(const char* text, size_t len, uint32_t max_graphs, int skip_inv
   std::vector<int> status(n, BMS_OK);
   std::vector<size_t> lines(n, 0), bad_line(n, 0);  // lines of each piece; a malformed line's number in it
   std::vector<std::string> msg(n);
+  auto piece = [&](size_t k) {
+    const char* b = text + cut[k];
+    const size_t m = cut[k + 1] - cut[k];
+    status[k] = parse_serial(b, m, 0, skip_invalid, 0, &part[k], &bad_line[k]);
+    if (status[k] != BMS_OK) msg[k] = bms::thread_error();
+    lines[k] = size_t(std::count(b, b + m, '\n'));
+  };
   std::vector<std::thread> pool;
-  for (size_t k = 0; k < n; ++k)
-    pool.emplace_back([&, k] {
-      const char* b = text + cut[k];
-      const size_t m = cut[k + 1] - cut[k];
-      status[k] = parse_serial(b, m, 0, skip_invalid, 0, &part[k], &bad_line[k]);
-      if (status[k] != BMS_OK) msg[k] = bms::thread_error();
-      lines[k] = size_t(std::count(b, b + m, '\n'));
-    });
+  for (size_t k = 0; k < n; ++k) {
+    try {
+      pool.emplace_back(piece, k);
+    } catch (const std::system_error&) {
+      piece(k);  // no thread to spare: this piece on the calling thread
+    }
+  }
   for (auto& t : pool) t.join();
   int r = BMS_OK;
   size_t before = 0;  // lines before piece k

@@ -9,6 +9,9 @@ these.  Inputs are a seeded synthetic molecular workload plus hand-built
 graphs, stored as text in the reference format (graph.hpp:150-202).
 
 Run from the repository root:  python tests/golden/make_golden.py
+`python tests/golden/make_golden.py large` writes tests/golden/nx_large.json
+instead: the same answer key for data graphs of 65-128 nodes, beyond the
+reference's 64-node bitsets, where the engine's generalized reading applies.
 """
 from __future__ import annotations
 
@@ -94,5 +97,36 @@ def main() -> None:
     print(f"{path}: {len(counts)} non-zero pairs, total {sum(c[2] for c in counts)}")
 
 
+def main_large() -> None:
+    build()
+    d = Graphs.synth_molecules(30, 29, 0, 0, 0, 65, 128, 1, 4)
+    q = Graphs.synth_queries(d, 12, 31, 3, 8, 0.25, 0.0)
+    tmp = ROOT / "_work" / "golden_tmp.txt"
+    tmp.parent.mkdir(exist_ok=True)
+    q_text, d_text = text_of(q, tmp), text_of(d, tmp)
+    q_text += "".join(line(*g) + "\n" for g in [ring(6), chain(5), star(3)])
+    qg = Graphs.parse_text(q_text)
+    dg = Graphs.parse_text(d_text)
+    Q, D = to_nx(qg.arrays()), to_nx(dg.arrays())
+    counts = [[qi, di, c] for qi, qq in enumerate(Q) for di, dd in enumerate(D) if (c := count(dd, qq))]
+    out = {
+        "about": "networkx VF2 induced, label-preserving embedding counts for data graphs of 65-128 nodes "
+                 "(answer key for EXACT semantics, R <= 2)",
+        "generator": "tests/golden/make_golden.py large",
+        "networkx": nx.__version__,
+        "query_text": q_text,
+        "data_text": d_text,
+        "n_queries": len(Q),
+        "n_data": len(D),
+        "counts": counts,
+    }
+    path = Path(__file__).with_name("nx_large.json")
+    path.write_text(json.dumps(out, separators=(",", ":")))
+    print(f"{path}: {len(counts)} non-zero pairs, total {sum(c[2] for c in counts)}")
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["large"]:
+        main_large()
+    else:
+        main()

@@ -101,3 +101,36 @@ def test_oracle_embeddings_match_networkx():
             assert [tuple(int(x) for x in row) for row in got] == want, (qi, di)
             checked += 1
     assert checked > 20
+
+
+GOLDEN_LARGE = Path(__file__).with_name("golden") / "nx_large.json"
+
+
+def golden_large():
+    g = json.loads(GOLDEN_LARGE.read_text())
+    q = Graphs.parse_text(g["query_text"])
+    d = Graphs.parse_text(g["data_text"])
+    dense = np.zeros((g["n_queries"], g["n_data"]), np.uint64)
+    for qi, di, c in g["counts"]:
+        dense[qi, di] = c
+    return q, d, dense
+
+
+@pytest.mark.parametrize("R", [0, 2])
+def test_oracle_counts_match_networkx_beyond_64_nodes(R):
+    # data graphs of 65-128 nodes: the generalized reading (bitsets as wide as
+    # the graph, cycle signatures for every size) keeps every filter sound, so
+    # EXACT counts equal the independent answer key
+    q, d, want = golden_large()
+    assert int(np.diff(d.arrays()["graph_offsets"]).min()) > 64
+    r = oracle.run_pipeline(q, d, R)
+    assert np.array_equal(r.pair_counts_dense(q.n_graphs), want)
+
+
+def test_x86_reading_loses_matches_beyond_64_nodes():
+    # the reference's own reading zeroes the data side's cycle signatures above
+    # 64 nodes (signature.hpp:614), so queries with cycles lose their matches
+    q, d, want = golden_large()
+    r = oracle.run_pipeline(q, d, 0, x86=True)
+    got = r.pair_counts_dense(q.n_graphs)
+    assert (got <= want).all() and got.sum() < want.sum()

@@ -10,8 +10,9 @@ graphs, stored as text in the reference format (graph.hpp:150-202).
 
 Run from the repository root:  python tests/golden/make_golden.py
 `python tests/golden/make_golden.py large` writes tests/golden/nx_large.json
-instead: the same answer key for data graphs of 65-128 nodes, beyond the
-reference's 64-node bitsets, where the engine's generalized reading applies.
+instead: the same answer key for data graphs of 65-128 nodes and queries of up
+to 40 nodes, beyond the reference's 64-node bitsets and 30-node join arrays,
+where the engine's generalized reading applies.
 """
 from __future__ import annotations
 
@@ -101,9 +102,10 @@ def main_large() -> None:
     build()
     d = Graphs.synth_molecules(30, 29, 0, 0, 0, 65, 128, 1, 4)
     q = Graphs.synth_queries(d, 12, 31, 3, 8, 0.25, 0.0)
+    q_big = Graphs.synth_queries(d, 8, 37, 31, 40, 0.0, 0.0)  # beyond the reference's 30-node join arrays
     tmp = ROOT / "_work" / "golden_tmp.txt"
     tmp.parent.mkdir(exist_ok=True)
-    q_text, d_text = text_of(q, tmp), text_of(d, tmp)
+    q_text, d_text = text_of(q, tmp) + text_of(q_big, tmp), text_of(d, tmp)
     q_text += "".join(line(*g) + "\n" for g in [ring(6), chain(5), star(3)])
     qg = Graphs.parse_text(q_text)
     dg = Graphs.parse_text(d_text)
@@ -111,7 +113,7 @@ def main_large() -> None:
     counts = [[qi, di, c] for qi, qq in enumerate(Q) for di, dd in enumerate(D) if (c := count(dd, qq))]
     out = {
         "about": "networkx VF2 induced, label-preserving embedding counts for data graphs of 65-128 nodes "
-                 "(answer key for EXACT semantics, R <= 2)",
+                 "and queries of up to 40 nodes (answer key for EXACT semantics, R <= 2)",
         "generator": "tests/golden/make_golden.py large",
         "networkx": nx.__version__,
         "query_text": q_text,

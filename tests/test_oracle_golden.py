@@ -118,11 +118,13 @@ def golden_large():
 
 @pytest.mark.parametrize("R", [0, 2])
 def test_oracle_counts_match_networkx_beyond_64_nodes(R):
-    # data graphs of 65-128 nodes: the generalized reading (bitsets as wide as
-    # the graph, cycle signatures for every size) keeps every filter sound, so
-    # EXACT counts equal the independent answer key
+    # data graphs of 65-128 nodes and queries of up to 40: the generalized
+    # reading (bitsets as wide as the graph, cycle signatures for every size,
+    # no 30-node join arrays) keeps every filter sound, so EXACT counts equal
+    # the independent answer key
     q, d, want = golden_large()
     assert int(np.diff(d.arrays()["graph_offsets"]).min()) > 64
+    assert int(np.diff(q.arrays()["graph_offsets"]).max()) > 30
     r = oracle.run_pipeline(q, d, R)
     assert np.array_equal(r.pair_counts_dense(q.n_graphs), want)
 

@@ -217,3 +217,15 @@ def test_parallel_parse_with_empty_pieces():
     ref = d.arrays()
     for k in ref:
         assert np.array_equal(par[k], ref[k]), k
+
+
+def test_bench_algorithmic_bytes_follow_their_definitions():
+    import bench
+
+    # filter + refine: Qn*Dn/8 candidate bits once, (45 + 8R) bytes per node on both sides
+    assert bench.algorithmic_filter_bytes(16, 1000, 6) == 16 * 1000 / 8 + (1000 + 16) * (45 + 48)
+    assert bench.algorithmic_filter_bytes(0, 0, 6) == 0
+    # signatures: CSR read once (5 per node + 4 per entry), 48 + 8R bytes written per node
+    assert bench.algorithmic_signature_bytes(10, 22, 6) == 10 * 5 + 22 * 4 + 10 * (48 + 48)
+    empty = bench.graph_offsets(Graphs.parse_text(""))
+    assert empty.tolist() == [0]

@@ -61,15 +61,25 @@ void append_graph(bms_graphs& g, const std::vector<uint8_t>& labels, const std::
 
 namespace {
 
+// whitespace (the characters isspace accepts in the C locale), as a table
+struct SpaceTable {
+  bool ws[256] = {};
+  constexpr SpaceTable() {
+    ws[uint8_t(' ')] = ws[uint8_t('\t')] = ws[uint8_t('\r')] = ws[uint8_t('\n')] = true;
+    ws[uint8_t('\f')] = ws[uint8_t('\v')] = true;
+  }
+};
+constexpr SpaceTable kSpace{};
+
 // whitespace tokenizer over one line
 struct Tok {
   const char* p;
   const char* e;
   bool next(const char*& b, size_t& n) {
-    while (p < e && (*p == ' ' || *p == '\t' || *p == '\r' || *p == '\n' || *p == '\f' || *p == '\v')) ++p;
+    while (p < e && kSpace.ws[uint8_t(*p)]) ++p;
     if (p >= e) return false;
     b = p;
-    while (p < e && !(*p == ' ' || *p == '\t' || *p == '\r' || *p == '\n' || *p == '\f' || *p == '\v')) ++p;
+    while (p < e && !kSpace.ws[uint8_t(*p)]) ++p;
     n = size_t(p - b);
     return true;
   }

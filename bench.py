@@ -151,30 +151,41 @@ def algorithmic_signature_bytes(nodes: int, entries: int, R: int) -> float:
     return nodes * (4.0 + 1.0) + entries * 4.0 + nodes * (8.0 + 32.0 + 8.0 + 8.0 * R)
 
 
-def cpu_baseline(q, d, threads: int, budget_s: float = 15.0, cs: bool = False) -> dict:
+def cpu_baseline(qa: dict, da: dict, threads: int, budget_s: float = 15.0, cs: bool = False) -> tuple[dict, object, int]:
     """The CPU restatement of the reference pipeline (OpenMP over nodes, words,
     pairs) on a bounded sample: all queries x the first k data graphs (cs: the
-    clustered join of the driver's --use-cs)."""
+    clustered join of the driver's --use-cs).  Returns the baseline record, the
+    oracle's result on the sample (its per-pair counts are the parity check of
+    the GPU run) and k."""
     import oracle
-    from bms2_gb300 import Graphs
 
-    a = d.arrays()
-    Q = q.n_graphs
-    k = 256
-    t_one = None
+    Q = len(qa["graph_offsets"]) - 1
+    D = len(da["graph_offsets"]) - 1
+    k = min(256, D)
     while True:
-        sub = _head(a, k)
+        sub = _head(da, k)
         t0 = time.perf_counter()
-        res = oracle.run_pipeline(q, sub, REFINE_STEPS, threads=threads, keep_steps=False, cs=cs)
-        t = time.perf_counter() - t0
-        if t > budget_s / 4 or k >= len(a["graph_offsets"]) - 1:
-            t_one = t
+        res = oracle.run_pipeline(qa, sub, REFINE_STEPS, threads=threads, keep_steps=False, cs=cs)
+        t_one = time.perf_counter() - t0
+        if t_one > budget_s / 4 or k >= D:
             break
-        k = min(k * 4, len(a["graph_offsets"]) - 1)
-    del Graphs
-    return {"value": Q * k / t_one, "unit": "pairs/s", "cores": threads, "kind": "port",
-            "sample": f"{Q} queries x first {k} of {len(a['graph_offsets']) - 1} data graphs, R={REFINE_STEPS}, "
+        k = min(k * 4, D)
+    info = {"value": Q * k / t_one, "unit": "pairs/s", "cores": threads, "kind": "port",
+            "sample": f"{Q} queries x first {k} of {D} data graphs, R={REFINE_STEPS}, "
                       f"count-all{', clustered join' if cs else ''}, {t_one:.2f} s", "matches": int(res.total)}
+    return info, res, k
+
+
+def sample_parity(gpu_offsets: np.ndarray, gpu_qidx: np.ndarray, gpu_counts: np.ndarray, res, k: int) -> dict:
+    """The GPU run's GMCR rows and per-pair counts of the first k data graphs
+    against the oracle's run on exactly those graphs (all queries)."""
+    n = int(res.offsets[-1])
+    ok_off = bool(len(gpu_offsets) > k and np.array_equal(gpu_offsets[:k + 1].astype(np.int64),
+                                                           res.offsets.astype(np.int64)))
+    ok_q = ok_off and bool(np.array_equal(gpu_qidx[:n], res.qidx))
+    ok_c = ok_q and bool(np.array_equal(gpu_counts[:n], res.counts))
+    return {"data_graphs": int(k), "pairs_compared": n, "gmcr_equal": ok_q, "counts_equal": ok_c,
+            "matches": int(res.total)}
 
 
 def _head(a: dict, k: int) -> dict:
@@ -205,8 +216,8 @@ def run_ours(args) -> None:
     import torch
     import torch.distributed as dist
 
-    from bms2_gb300 import (COUNT_ALL, DATA, FIND_FIRST, ORDER_GMCR, ORDER_LEARNED, QUERY, SEM_EXACT, Context, shards,
-                            workloads)
+    from bms2_gb300 import (COUNT_ALL, DATA, FIND_FIRST, ORDER_GMCR, ORDER_LEARNED, QUERY, SEM_EXACT,
+                            SEM_REFERENCE_DFS, Context, shards, workloads)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -244,17 +255,17 @@ def run_ours(args) -> None:
     ctx.load(DATA, d)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
 
-    def step(o=order, mode=COUNT_ALL):
-        return ctx.run(REFINE_STEPS, mode, o, SEM_EXACT)
+    def step(o=order, mode=COUNT_ALL, sem=SEM_EXACT):
+        return ctx.run(REFINE_STEPS, mode, o, sem)
 
-    def timed(o, k, mode=COUNT_ALL):
+    def timed(o, k, mode=COUNT_ALL, sem=SEM_EXACT):
         """k steps of order o, each bracketed by CUDA events on the library's stream."""
         ms, stages = [], []
         for _ in range(k):
             flush.fill_(1)  # L2 flush between steps (outside the timed events)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            tot = step(o, mode)
+            tot = step(o, mode, sem)
             e1.record(stream)
             e1.synchronize()
             ms.append(e0.elapsed_time(e1))
@@ -307,9 +318,11 @@ def run_ours(args) -> None:
     t_total = float(np.sum(ms_steps)) / 1e3
     st = stage[-1]
     all_total, all_valid = int(total), int(st["n_valid_pairs"])
+    # the timed run's GMCR and per-pair counts, for the oracle comparison below
+    ca_counts = ctx.pair_counts()
+    ca_off, ca_qidx = ctx.gmcr()
     # find-first (the reference driver's default mode) on the same inputs: one
     # 0/1 per pair, equal to "count-all found something" on every pair
-    ca_counts = ctx.pair_counts()
     for _ in range(args.warmup):
         step(order, FIND_FIRST)
     ff_ms, ff_stage, ff_total = timed(order, args.steps, FIND_FIRST)
@@ -319,7 +332,18 @@ def run_ours(args) -> None:
                   "find_first_pairs_matched": int(ff_total),
                   "find_first_equals_count_all_nonzero": bool(np.array_equal(
                       ctx.pair_counts(), (ca_counts > 0).astype(np.uint64)))}
-    del ca_counts
+    # the reference's own DFS (REFERENCE_DFS: its literal frame bookkeeping,
+    # isomorphism.hpp:401-448, in plain GMCR order) timed on the same inputs
+    rd_steps = max(1, min(args.steps, 5))
+    for _ in range(args.warmup):
+        step(ORDER_GMCR, COUNT_ALL, SEM_REFERENCE_DFS)
+    rd_ms, rd_stage, rd_total = timed(ORDER_GMCR, rd_steps, COUNT_ALL, SEM_REFERENCE_DFS)
+    rd_counts = ctx.pair_counts()
+    rd_off, rd_qidx = ctx.gmcr()
+    reference_dfs = {"reference_dfs_value": world * Q * D / (float(np.mean(rd_ms)) / 1e3),
+                     "reference_dfs_ms_per_step": float(np.mean(rd_ms)),
+                     "reference_dfs_join_ms": float(np.mean([s_["ms_join"] for s_ in rd_stage])),
+                     "reference_dfs_total_matches": int(rd_total), "reference_dfs_steps": rd_steps}
     for _ in range(args.warmup):
         step()
     if world > 1:  # shards: sum of counts, slowest rank's time
@@ -394,12 +418,12 @@ def run_ours(args) -> None:
         "roofline_signatures": {"kernel": "signatures_kernel (data and query side)", "bound": "hbm",
                                 "achieved": sig_gbs, "peak": peak, "unit": "GB/s", "frac": sig_gbs / peak,
                                 "algorithmic_bytes": sig_bytes, "ms": sig_ms,
-                                "note": "instruction-bound: profiles/signatures_mol1m_100k.md"},
+                                "note": "instruction-bound (ncu: lanes active per instruction, issue stalls)"},
         "join": {"kernel": "join_kernel (three size classes side by side)", "bound": "latency",
                  "ms": j_ms, "expansions_per_step": int(st["expansions"]),
                  "expansions_per_s": float(st["expansions"]) / max(j_ms / 1e3, 1e-9),
                  "note": "no HBM or tensor roofline: a DFS bound by latency and integer issue, "
-                         "10-14 of 32 lanes active (profiles/join_mol1m_100k.md)"},
+                         "lanes active per instruction and stall reasons from ncu"},
         "stage_ms": {k: float(np.mean([s[k] for s in stage])) for k in
                      ("ms_signatures", "ms_filter", "ms_map", "ms_order", "ms_join", "ms_total")},
         "clocks": clk,
@@ -414,17 +438,41 @@ def run_ours(args) -> None:
         line["results"]["expansion_ratio_plain_over_learned"] = float(plain["plain_expansions"]) / max(1, st["expansions"])
     line["results"].update(extra)
     line["results"].update(find_first)
+    line["results"].update(reference_dfs)
     if schedule is not None:
         line["schedule"] = {"tuned_on": f"{args.workload} seed A, "
                                         f"{args.tune_graphs if args.tune_graphs > 0 else 'all'} data graphs",
                             "buckets": schedule}
-    if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(q, d, os.cpu_count() or 1, args.cpu_budget)
+    parity_ok = True
+    if rank == 0:
+        import oracle
+
+        threads = os.cpu_count() or 1
+        if not args.no_cpu:
+            info, res, k = cpu_baseline(qa, da, threads, args.cpu_budget)
+            line["cpu_baseline"] = info
+        else:
+            k = min(1024, D)
+            res = oracle.run_pipeline(qa, _head(da, k), REFINE_STEPS, threads=threads, keep_steps=False)
+        # the oracle's counts on the sample, pair by pair: EXACT for the timed
+        # run, the literal restatement of the reference DFS for REFERENCE_DFS
+        exact = sample_parity(ca_off, ca_qidx, ca_counts, res, k)
+        k_lit = min(k, 4096)
+        lit = oracle.run_pipeline(qa, _head(da, k_lit), REFINE_STEPS, threads=threads, keep_steps=False,
+                                  dfs_literal=True)
+        literal = sample_parity(rd_off, rd_qidx, rd_counts, lit, k_lit)
+        line["results"]["oracle_sample"] = {"exact": exact, "reference_dfs": literal}
+        line["results"]["oracle_sample_counts_equal"] = exact["counts_equal"]
+        line["results"]["reference_dfs_oracle_counts_equal"] = literal["counts_equal"]
+        parity_ok = exact["counts_equal"] and literal["counts_equal"]
     if rank == 0:
         print(json.dumps(line), flush=True)
+    del ca_counts, rd_counts
     ctx.close()
     if world > 1:
         dist.destroy_process_group()
+    if not parity_ok:
+        sys.exit("per-pair counts differ from the oracle on the sample: the measurement is void")
 
 
 def run_streamed(args) -> None:
@@ -652,6 +700,7 @@ def run_clustered(args) -> None:
     launches = sum(s["kernel_launches"] for s in stage)
     st = stage[-1]
     c_counts = ctx.pair_counts()
+    c_off, c_qidx = ctx.gmcr()
     t_total = float(np.sum(ms_steps)) / 1e3
     all_total, all_valid = int(total), int(st["n_valid_pairs"])
     if world > 1:
@@ -718,44 +767,68 @@ def run_clustered(args) -> None:
                     "counts_equal_every_pair": bool(np.array_equal(c_counts, p_counts)),
                     "counts_equal_every_pair_at_2_refine_steps": r2_equal},
     }
-    if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(q, d, os.cpu_count() or 1, args.cpu_budget, cs=True)
+    parity_ok = True
+    if rank == 0:
+        import oracle
+
+        threads = os.cpu_count() or 1
+        if not args.no_cpu:
+            info, res, k = cpu_baseline(qa, da, threads, args.cpu_budget, cs=True)
+            line["cpu_baseline"] = info
+        else:
+            k = min(1024, D)
+            res = oracle.run_pipeline(qa, _head(da, k), REFINE_STEPS, threads=threads, keep_steps=False, cs=True)
+        par = sample_parity(c_off, c_qidx, c_counts, res, k)
+        line["results"]["oracle_sample"] = {"exact": par}
+        line["results"]["oracle_sample_counts_equal"] = par["counts_equal"]
+        parity_ok = par["counts_equal"]
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
     if world > 1:
         dist.destroy_process_group()
+    if not parity_ok:
+        sys.exit("per-pair counts differ from the oracle on the sample: the measurement is void")
 
 
 def run_reference(args) -> None:
-    """The reference's CPU path: its SYCL CPU build cannot be built here, so the
-    oracle (a C++ restatement of the reference kernels, OpenMP over all host
-    threads) runs on a bounded sample of the same workload."""
+    """The reference's CPU path.  Its SYCL CPU build cannot be built here (no
+    SYCL compiler or runtime), so the oracle — the C++ restatement of the
+    reference kernels, OpenMP over all host threads — runs on a bounded sample
+    of the same workload.  Nothing of the GPU engine is loaded in this arm: the
+    inputs come from the generator's own CPU-only build (oracle/synth.py),
+    byte-identical to the engine arm's."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    from bms2_gb300 import workloads
+    from oracle import synth
+
+    from bms2_gb300.workloads import make_cluster_arrays
 
     cs = args.workload == "mol1m-cs"
     if cs:
-        _, d = workloads.make("mol1m", 202)
-        q = workloads.make_cluster(d, args.cluster_members, 303, proto_nodes=(5, 8), proto=args.cluster_proto)
+        _, da = synth.make("mol1m", 202)
+        qa = make_cluster_arrays(da, args.cluster_members, 303, proto_nodes=(5, 8), proto=args.cluster_proto)
     else:
-        q, d = workloads.make(args.workload, 202)
+        qa, da = synth.make(args.workload, 202)
     threads = os.cpu_count() or 1
     cb = None
     vals = []
     for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(q, d, threads, budget_s=args.cpu_budget if i >= args.warmup else 4.0, cs=cs)
+        cb, _, _ = cpu_baseline(qa, da, threads, budget_s=args.cpu_budget if i >= args.warmup else 4.0, cs=cs)
         if i >= args.warmup:
             vals.append(cb["value"])
     v = float(np.mean(vals))
     cb["value"] = v
+    cb["implementation"] = "oracle restatement of the reference kernels (the reference's SYCL build is unavailable)"
+    Q, D = len(qa["graph_offsets"]) - 1, len(da["graph_offsets"]) - 1
     line = {"metric": METRIC, "value": v, "unit": "pairs/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": f"{args.workload}: {d.n_graphs} data graphs x {q.n_graphs} queries (bounded sample per "
-                                   f"step), refine steps {REFINE_STEPS}, count-all", "order": "plain"},
+            "config": {"workload": f"{args.workload}: {D} data graphs x {Q} queries (bounded sample per "
+                                   f"step), refine steps {REFINE_STEPS}, count-all", "order": "plain",
+                       "sample_scaling": "pairs/s of all queries x a prefix of the data graphs; the prefix grows "
+                                         "until one pass takes about a quarter of the CPU budget"},
             "cpu_baseline": cb, "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -783,10 +856,12 @@ def main() -> None:
     args = ap.parse_args()
     from bms2_gb300 import build
 
-    build.build()
     if args.impl == "reference":
+        build.build_cpu_side()  # the oracle and the generator only
         run_reference(args)
-    elif args.workload == "mol10m":
+        return
+    build.build()
+    if args.workload == "mol10m":
         run_streamed(args)
     elif args.workload == "mol1m-cs":
         run_clustered(args)

@@ -21,6 +21,8 @@ CLI = OUT / "bms2"
 ORACLE_DIR = ROOT / "oracle"
 ORACLE_OUT = ORACLE_DIR / "_build"
 ORACLE_LIB = ORACLE_OUT / "liboracle.so"
+# the workload generator alone, for the CPU side (no engine code mapped there)
+SYNTH_LIB = ORACLE_OUT / "libsynth.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
@@ -87,12 +89,31 @@ def build_oracle(force: bool = False) -> Path:
     return ORACLE_LIB
 
 
-def build(force: bool = False) -> None:
+def build_synth(force: bool = False) -> Path:
+    """The seeded generator (csrc/synth.cpp with its host graph container
+    csrc/graphs.cpp) compiled on its own, without CUDA, for the CPU baseline."""
+    ORACLE_OUT.mkdir(parents=True, exist_ok=True)
+    srcs = [CSRC / "synth.cpp", CSRC / "graphs.cpp"]
+    deps = srcs + [CSRC / "graphs.h", ROOT / "include" / "bms.h"]
+    if force or _stale(SYNTH_LIB, deps):
+        cxx = shutil.which("g++") or "g++"
+        _run([cxx, "-std=c++17", "-O2", "-fPIC", "-shared", "-I", str(ROOT / "include"), *map(str, srcs), "-o",
+              str(SYNTH_LIB), "-lpthread"])
+    return SYNTH_LIB
+
+
+def build_cpu_side(force: bool = False) -> None:
+    """What the CPU-baseline arm needs: the oracle and the generator."""
     with cf.ThreadPoolExecutor(max_workers=2) as ex:
-        f1 = ex.submit(build_library, force)
-        f2 = ex.submit(build_oracle, force)
-        f1.result()
-        f2.result()
+        for f in [ex.submit(build_oracle, force), ex.submit(build_synth, force)]:
+            f.result()
+
+
+def build(force: bool = False) -> None:
+    with cf.ThreadPoolExecutor(max_workers=3) as ex:
+        fs = [ex.submit(build_library, force), ex.submit(build_oracle, force), ex.submit(build_synth, force)]
+        for f in fs:
+            f.result()
 
 
 if __name__ == "__main__":

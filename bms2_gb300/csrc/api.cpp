@@ -95,7 +95,10 @@ int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const 
   const uint64_t N = G ? v.graph_offsets[G] - node_base : 0;
   if (N && (!v.row_offsets || !v.node_labels)) return fail(c, BMS_EINVAL, "row_offsets or node_labels is null");
   const uint32_t entry_base = slice && N ? v.row_offsets[0] : 0;
-  const uint64_t E = N ? v.row_offsets[N] - entry_base : 0;
+  // checked before anything is sized or copied: a last offset below the first
+  // would wrap the entry count and over-read the caller's column array
+  if (N && v.row_offsets[N] < entry_base) return fail(c, BMS_EINVAL, "row_offsets must be non-decreasing");
+  const uint64_t E = N ? uint64_t(v.row_offsets[N]) - entry_base : 0;
   if (N && v.row_offsets[0] != entry_base) return fail(c, BMS_EINVAL, "row_offsets[0] must be 0");
   if (E && !v.column_indices) return fail(c, BMS_EINVAL, "column_indices is null");
   s.loaded = false;

@@ -30,13 +30,36 @@ static __device__ __align__(256) uint32_t g_scan_scratch[kStaticScanWords];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
+// Per device: the context the address was looked up in, and the address.  A
+// module's globals live per context, so a caller that makes another context
+// current on the same device (driver API) gets its own lookup.
+void* g_scratch_ctx[kMaxDevices] = {};
 uint32_t* g_scratch_addr[kMaxDevices] = {};
 
-// Device address of g_scan_scratch on the current device, looked up once per
-// device (the host-side symbol is only a stand-in, never a device address).
+// cuCtxGetCurrent through the runtime's driver entry point (no libcuda link).
+using CtxGetCurrentFn = int (*)(void**);
+CtxGetCurrentFn ctx_get_current() {
+  static CtxGetCurrentFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+    }
+    return reinterpret_cast<CtxGetCurrentFn>(p);
+  }();
+  return fn;
+}
+
+// Device address of g_scan_scratch in the current context of `device`, looked
+// up once per (device, context): the host-side symbol is only a stand-in,
+// never a device address.
 int scratch_address(int device, uint32_t** out) {
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_addr[device]) {
+  void* cur = nullptr;
+  if (CtxGetCurrentFn f = ctx_get_current()) f(&cur);
+  if (!g_scratch_addr[device] || g_scratch_ctx[device] != cur) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_scan_scratch);
     if (e != cudaSuccess) {
@@ -46,6 +69,9 @@ int scratch_address(int device, uint32_t** out) {
       return BMS_ECUDA;
     }
     g_scratch_addr[device] = static_cast<uint32_t*>(p);
+    // the first runtime call above may have created the primary context
+    if (CtxGetCurrentFn f = ctx_get_current()) f(&cur);
+    g_scratch_ctx[device] = cur;
   }
   *out = g_scratch_addr[device];
   return BMS_OK;

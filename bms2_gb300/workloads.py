@@ -55,17 +55,12 @@ def make(name: str, seed: int = 1, n_data: int | None = None, n_queries: int | N
 
 
 # ------------------------------------------------------------------ clusters
-def _graph_at(v, g: int):
-    """(labels, rows, edge labels) of graph g of a GraphsView, local ids; rows[u]
-    lists u's neighbours in CSR order."""
-    import numpy as np
-
-    go = np.ctypeslib.as_array(v.graph_offsets, shape=(v.n_graphs + 1,))
+def _graph_at(a: dict, g: int):
+    """(labels, rows, edge labels) of graph g of a CSR batch (dict of arrays),
+    local ids; rows[u] lists u's neighbours in CSR order."""
+    go, ro, ci, el, nl = (a["graph_offsets"], a["row_offsets"], a["column_indices"], a["edge_labels"],
+                          a["node_labels"])
     s, e = int(go[g]), int(go[g + 1])
-    ro = np.ctypeslib.as_array(v.row_offsets, shape=(v.n_nodes + 1,))
-    ci = np.ctypeslib.as_array(v.column_indices, shape=(max(v.n_entries, 1),))
-    el = np.ctypeslib.as_array(v.edge_labels, shape=(max(v.n_entries, 1),))
-    nl = np.ctypeslib.as_array(v.node_labels, shape=(max(v.n_nodes, 1),))
     rows, elab = [], []
     for u in range(s, e):
         a, b = int(ro[u]), int(ro[u + 1])
@@ -140,6 +135,14 @@ def _find_ring(lab, rows, label: int = 8, sizes=(6, 5)):
 def make_cluster(data: Graphs, n_members: int, seed: int, proto_nodes: tuple[int, int] = (5, 8),
                  extra_nodes: tuple[int, int] = (1, 12), n_sources: int = 24, proto: str = "grow",
                  source_graphs: int = 100_000) -> Graphs:
+    """make_cluster_arrays on a Graphs batch, as a Graphs batch."""
+    return Graphs.from_csr(**make_cluster_arrays(data.arrays(), n_members, seed, proto_nodes, extra_nodes, n_sources,
+                                                 proto, source_graphs))
+
+
+def make_cluster_arrays(data: dict, n_members: int, seed: int, proto_nodes: tuple[int, int] = (5, 8),
+                        extra_nodes: tuple[int, int] = (1, 12), n_sources: int = 24, proto: str = "grow",
+                        source_graphs: int = 100_000) -> dict:
     """A query cluster in the layout of the reference's cluster files
     (generate_cs.py:338-362, 555-577): graph 0 is the prototype P; each member
     is P plus 1..12 further atoms grown around an induced occurrence of P in one
@@ -155,9 +158,9 @@ def make_cluster(data: Graphs, n_members: int, seed: int, proto_nodes: tuple[int
     import numpy as np
 
     rng = np.random.default_rng(seed)
-    v = data.view()
-    go = np.ctypeslib.as_array(v.graph_offsets, shape=(v.n_graphs + 1,))
-    G = min(v.n_graphs, source_graphs)
+    v = data
+    go = v["graph_offsets"]
+    G = min(len(go) - 1, source_graphs)
     sizes = go[1:G + 1].astype(np.int64) - go[:G]
     want = proto_nodes[1] + extra_nodes[1]
     big = np.nonzero(sizes >= want)[0]
@@ -216,5 +219,6 @@ def make_cluster(data: Graphs, n_members: int, seed: int, proto_nodes: tuple[int
             roff.append(len(cols))
             labs.append(lab[u])
         goff.append(base + len(nodes))
-    return Graphs.from_csr(np.array(goff, np.uint32), np.array(roff, np.uint32), np.array(cols, np.uint32),
-                           np.array(labs, np.uint8), np.array(elabs, np.uint8))
+    return {"graph_offsets": np.array(goff, np.uint32), "row_offsets": np.array(roff, np.uint32),
+            "column_indices": np.array(cols, np.uint32), "node_labels": np.array(labs, np.uint8),
+            "edge_labels": np.array(elabs, np.uint8)}

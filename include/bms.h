@@ -277,7 +277,11 @@ int bms_get_gmcr(bms_ctx* ctx, uint32_t* data_graph_offsets, uint32_t* query_gra
  * scan's scratch in a fixed 256 KiB array that every GPU loading libbms holds
  * until the process exits.  Limit: n <= 100,000,000 (BMS_EUNSUPPORTED above).
  * The first call on a device looks up that array's device address (a one-time
- * set-up); make that first call before any stream capture.  All calls share the
+ * set-up per device and current context: a caller that makes another context
+ * current on the device gets a fresh lookup); make that first call before any
+ * stream capture.  cudaDeviceReset ends the context the address belongs to, as
+ * it ends every other libbms device buffer: use no libbms state of that device
+ * afterwards in the same process.  All calls share the
  * one array, so calls that overlap on the GPU (other streams, other threads)
  * race: order them.  The work is queued on `stream` (a cudaStream_t, NULL for
  * the default stream); the call does not wait for it. */

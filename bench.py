@@ -243,7 +243,7 @@ def run_ours(args) -> None:
         schedule = [{"max_data_nodes": s["max_data_nodes"][k], "word_bits": s["word_bits"][k],
                      "split_depth": s["split_depth"][k], "blocks_per_sm": s["blocks_per_sm"][k],
                      "warps_per_block": s["warps_per_block"][k], "steps": s["steps"][k],
-                     "refill": s["refill"][k],
+                     "refill": s["refill"][k], "lanes_per_pair": s["lanes_per_pair"][k],
                      "split_budget": s["split_budget"][k], "tuned_join_ms": round(s["ms"][k], 3)}
                     for k in range(3)]
         del tq, td

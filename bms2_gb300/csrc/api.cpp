@@ -29,7 +29,8 @@ bms_schedule default_schedule() {
   const uint32_t nodes[3] = {32, 64, 128};
   for (int i = 0; i < 3; ++i) {
     s.max_data_nodes[i] = nodes[i];
-    s.word_bits[i] = nodes[i];
+    s.word_bits[i] = i == 0 ? 32 : 64;
+    s.lanes_per_pair[i] = 1;
     s.split_depth[i] = 0;
     s.blocks_per_sm[i] = 3;
     s.warps_per_block[i] = 8;
@@ -271,6 +272,10 @@ void class_launches(const bms_schedule& s, int sem, ClassLaunch cl[3]) {
     cl[k].steps = int(s.steps[k] ? s.steps[k] : 32);
     cl[k].refill = s.refill[k] ? (s.refill[k] > 32 ? 32u : s.refill[k]) : 4u;
     cl[k].split_budget = s.split_budget[k];
+    uint32_t lg = 0;
+    while (lg < 5 && (1u << (lg + 1)) <= s.lanes_per_pair[k]) ++lg;
+    cl[k].lanes_log2 = lg;
+    cl[k].word_bits = k == 0 || s.word_bits[k] == 32 ? 32 : 64;
   }
 }
 
@@ -1590,13 +1595,17 @@ int bms_set_schedule(bms_ctx* c, const bms_schedule* s) {
     if (s->blocks_per_sm[i] == 0 || s->blocks_per_sm[i] > 32 || s->warps_per_block[i] == 0 ||
         s->warps_per_block[i] > 8 || s->split_depth[i] > 1 || s->steps[i] == 0 || s->steps[i] > 4096 ||
         s->refill[i] == 0 || s->refill[i] > 32 ||
-        s->split_budget[i] > (1u << 31))
+        s->split_budget[i] > (1u << 31) || (s->word_bits[i] != 32 && s->word_bits[i] != 64) ||
+        (i == 0 && s->word_bits[i] != 32) || s->lanes_per_pair[i] == 0 || s->lanes_per_pair[i] > 32 ||
+        (s->lanes_per_pair[i] & (s->lanes_per_pair[i] - 1)) != 0)
       return fail(c, BMS_EINVAL, "schedule entry out of range");
   const bms_schedule fixed = default_schedule();
   c->sched = *s;
-  for (int i = 0; i < BMS_SCHED_BUCKETS; ++i) {  // the bucket bounds and word widths are not settable
+  for (int i = 0; i < BMS_SCHED_BUCKETS; ++i)  // the bucket bounds are not settable
     c->sched.max_data_nodes[i] = fixed.max_data_nodes[i];
+  for (int i = 3; i < BMS_SCHED_BUCKETS; ++i) {
     c->sched.word_bits[i] = fixed.word_bits[i];
+    c->sched.lanes_per_pair[i] = fixed.lanes_per_pair[i];
   }
   return BMS_OK;
 }

@@ -299,6 +299,7 @@ struct JoinArgs {
   SubTask* sub[2];                 // subtrees: round r reads sub[r & 1], writes sub[(r + 1) & 1]
   uint64_t sub_cap;                // entries of each subtree buffer
   uint32_t split_budget;           // expansions before a search splits (0: never)
+  uint32_t lanes_log2;             // per-record tasks: 2^lanes_log2 lanes per record (root ranks g mod 2^lanes_log2)
   int round;                       // set by launch_join
   // Clustered join (EXACT): with cs_end > 0, round 0 first writes every
   // prototype match as entries (match, first member, data graph) per size
@@ -326,10 +327,12 @@ constexpr uint32_t kCsMembers = 32;  // members of the graph's GMCR row per entr
 // Launch shape and task settings of one record class (size bucket) of the join.
 struct ClassLaunch {
   int blocks, threads;
-  int per_pair;           // 1: one task per record; 0: (pair, root) tasks
+  int per_pair;           // 1: one task per record (or per lane of its group); 0: (pair, root) tasks
   int steps;              // DFS steps between refills
   uint32_t refill;        // idle lanes that trigger a refill
   uint32_t split_budget;  // 0: never split
+  uint32_t lanes_log2;    // per-record tasks: 2^lanes_log2 lanes share a record's roots
+  int word_bits;          // machine word of the search sets: 32 or 64
 };
 // All rounds of the join; the per-class fields of `a` come from cl[class].
 // With timers, events [round][class][0/1] bracket each class's launches.

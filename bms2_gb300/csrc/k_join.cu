@@ -135,42 +135,98 @@ template <typename T, int W>
 __device__ __forceinline__ bool bhas(Bits<T, W> a, uint32_t v) {
   constexpr uint32_t kB = Bits<T, W>::kBits;
   T x = a.w[0];
-  if (W > 1 && v >= kB) x = a.w[W - 1];
+#pragma unroll
+  for (int i = 1; i < W; ++i)
+    if (v / kB == uint32_t(i)) x = a.w[i];
   return (x >> (v % kB)) & 1u;
 }
 template <typename T, int W>
 __device__ __forceinline__ uint32_t blow(Bits<T, W> a) {
-  if (W == 1 || a.w[0]) return wlow(a.w[0]);
-  return Bits<T, W>::kBits + wlow(a.w[W - 1]);
+  constexpr uint32_t kB = Bits<T, W>::kBits;
+  uint32_t r = wlow(a.w[W - 1]) + (W - 1) * kB;
+#pragma unroll
+  for (int i = W - 2; i >= 0; --i)
+    if (a.w[i]) r = uint32_t(i) * kB + wlow(a.w[i]);
+  return r;
 }
 template <typename T, int W>
 __device__ __forceinline__ uint32_t bhigh(Bits<T, W> a) {
-  if (W > 1 && a.w[W - 1]) return Bits<T, W>::kBits + whigh(a.w[W - 1]);
-  return whigh(a.w[0]);
+  constexpr uint32_t kB = Bits<T, W>::kBits;
+  uint32_t r = whigh(a.w[0]);
+#pragma unroll
+  for (int i = 1; i < W; ++i)
+    if (a.w[i]) r = uint32_t(i) * kB + whigh(a.w[i]);
+  return r;
 }
 template <typename T, int W>
 __device__ __forceinline__ Bits<T, W> bclear_low(Bits<T, W> a) {
-  if (W == 1 || a.w[0]) {
-    a.w[0] &= a.w[0] - 1;
-  } else {
-    a.w[W - 1] &= a.w[W - 1] - 1;
+  bool done = false;
+#pragma unroll
+  for (int i = 0; i < W; ++i) {
+    if (!done && a.w[i]) {
+      a.w[i] &= a.w[i] - 1;
+      done = true;
+    }
   }
   return a;
 }
-// Rows are stored as two 64-bit words (little-endian); narrower searches read
-// the low word, or its low half.  Rows are read-only during the join.
+// Rows are stored as two 64-bit words (little-endian); a search reads as many
+// of its words as its set holds: 32, 64 or 128 bits, in 32- or 64-bit words.
 template <typename T, int W>
 __device__ __forceinline__ Bits<T, W> bload(const uint64_t* p) {
+  static_assert(sizeof(T) * 8 * W <= 128, "rows hold 128 bits");
   Bits<T, W> r;
-  if constexpr (sizeof(T) == 4) {
-    r.w[0] = __ldg(reinterpret_cast<const unsigned int*>(p));
-  } else if constexpr (W == 1) {
-    r.w[0] = __ldg(reinterpret_cast<const unsigned long long*>(p));
+  if constexpr (sizeof(T) * 8 * W == 32) {
+    r.w[0] = T(__ldg(reinterpret_cast<const unsigned int*>(p)));
+  } else if constexpr (sizeof(T) * 8 * W == 64) {
+    const unsigned long long x = __ldg(reinterpret_cast<const unsigned long long*>(p));
+    if constexpr (W == 1) {
+      r.w[0] = T(x);
+    } else {
+      r.w[0] = T(uint32_t(x));
+      r.w[1] = T(uint32_t(x >> 32));
+    }
   } else {
     const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(p));
-    r.w[0] = v.x;
-    r.w[W - 1] = v.y;
+    if constexpr (W == 2) {
+      r.w[0] = T(v.x);
+      r.w[1] = T(v.y);
+    } else {
+      r.w[0] = T(uint32_t(v.x));
+      r.w[1] = T(uint32_t(v.x >> 32));
+      r.w[2] = T(uint32_t(v.y));
+      r.w[3] = T(uint32_t(v.y >> 32));
+    }
   }
+  return r;
+}
+// A set given as its low and high 64 bits (subtree records).
+template <typename T, int W>
+__device__ __forceinline__ Bits<T, W> bfrom64(uint64_t lo, uint64_t hi) {
+  Bits<T, W> r;
+  if constexpr (sizeof(T) == 8) {
+    r.w[0] = T(lo);
+    if constexpr (W == 2) r.w[1] = T(hi);
+  } else {
+    r.w[0] = T(uint32_t(lo));
+    if constexpr (W >= 2) r.w[1] = T(uint32_t(lo >> 32));
+    if constexpr (W == 4) {
+      r.w[2] = T(uint32_t(hi));
+      r.w[3] = T(uint32_t(hi >> 32));
+    }
+  }
+  return r;
+}
+// The members of `a` whose rank (0 = lowest) is g modulo 2^lg: lane g of a
+// group of 2^lg lanes searching one pair takes these roots.
+template <typename T, int W>
+__device__ __forceinline__ Bits<T, W> bstride(Bits<T, W> a, uint32_t g, uint32_t lg) {
+  if (lg == 0) return a;
+  const uint32_t mask = (1u << lg) - 1u;
+  Bits<T, W> r = z<T, W>();
+  uint32_t k = 0;
+  for (; bany(a); a = bclear_low(a), ++k)
+    if ((k & mask) == g) r = bor(r, bbit<T, W>(blow(a)));
   return r;
 }
 
@@ -791,14 +847,17 @@ __global__ void __launch_bounds__(256) cs_extend_kernel(JoinArgs a) {
   }
 }
 
-// Record class K: 2 = data graphs of 65..128 nodes (two 64-bit words), 1 =
-// 33..64 nodes (one 64-bit word), 0 = up to 32 nodes (one 32-bit word).
-// kCounted selects the counted test (EXACT, in-degrees <= 7) or the in-row test.
-template <int K, bool kCounted, int kMode>
+// Record class K: 2 = data graphs of 65..128 nodes (128-bit sets), 1 = 33..64
+// nodes (64 bits), 0 = up to 32 nodes (32 bits); kWordBits: the sets' machine
+// word (32 or 64 bits, at most the set's width).  kCounted selects the counted
+// test (EXACT, in-degrees <= 7) or the in-row test.
+template <int K, int kWordBits, bool kCounted, int kMode>
 __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
   constexpr bool kFindFirst = kMode == kModeFind, kLogVertices = kMode == kModeLog;
-  using T = typename std::conditional<K == 0, uint32_t, uint64_t>::type;
-  constexpr int W = K == 2 ? 2 : 1;
+  using T = typename std::conditional<kWordBits == 32, uint32_t, uint64_t>::type;
+  constexpr int kSetBits = 32 << K;
+  static_assert(kWordBits <= kSetBits, "a word wider than the set");
+  constexpr int W = kSetBits / kWordBits;
   const bool counted_applies = !a.literal && *a.ds.maxin < (1u << kPlanes);
   if (counted_applies != kCounted) return;  // the other variant runs this class
   const uint32_t lane = lane_id();
@@ -817,9 +876,9 @@ __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
   if (subtrees) {
     first = 0;
     ntasks = min((unsigned long long)a.sub_cap, a.ctr->sub_n[a.round]);
-  } else if (a.per_pair) {
+  } else if (a.per_pair) {  // 2^lanes_log2 lanes per record, each a share of its roots
     first = lo;
-    ntasks = hi - lo;
+    ntasks = (hi - lo) << a.lanes_log2;
   } else {
     first = 0;
     ntasks = min((unsigned long long)a.task_cap, a.ctr->tasks);
@@ -869,7 +928,7 @@ __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
           rec = sub->rec;
           take = (K == 2 || rec >= lo) && rec < hi;  // kNoRecord is never in range
         } else if (a.per_pair) {
-          rec = uint32_t(first + qbase + rank);
+          rec = uint32_t(first + ((qbase + rank) >> a.lanes_log2));
         } else {
           const Task tk = a.tasks[qbase + rank];
           rec = tk.pair;
@@ -887,7 +946,9 @@ __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
           L.irow = a.ds.adjin + 2 * uint64_t(a.d.goff[r.d]);
           L.perm = a.o.perm + uint64_t(r.q) * kMaxQueryNodes;
           L.dadj = a.o.dadj + uint64_t(r.q) * kMaxQueryNodes;
-          if (a.per_pair && !subtrees) roots = bload<T, W>(L.crow + 2 * uint64_t(L.perm[0]));
+          if (a.per_pair && !subtrees)
+            roots = bstride(bload<T, W>(L.crow + 2 * uint64_t(L.perm[0])),
+                            uint32_t(qbase + rank) & ((1u << a.lanes_log2) - 1u), a.lanes_log2);
           L.cnt = 0;
           L.exps = 0;
           L.since_check = 0;
@@ -903,8 +964,7 @@ __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
             const int dep = int(sub->depth);
             L.t = dep;
             L.base = dep;
-            roots.w[0] = T(sub->cand[0]);
-            if (W > 1) roots.w[W - 1] = T(sub->cand[1]);
+            roots = bfrom64<T, W>(sub->cand[0], sub->cand[1]);
             for (int j = 0; j < dep; ++j) {
               const uint32_t x = sub->f[j];
               S.f[j] = uint8_t(x);
@@ -937,7 +997,7 @@ __global__ void __launch_bounds__(256) join_kernel(JoinArgs a) {
   }
 }
 
-template <int K, int kMode>
+template <int K, int kWordBits, int kMode>
 cudaError_t launch_mode(const JoinArgs& a, int blocks, int threads, cudaStream_t st) {
   if constexpr (kMode != kModeLog) {
     if (a.cs_end && a.round == 0) {  // the clustered entries of this class
@@ -949,19 +1009,32 @@ cudaError_t launch_mode(const JoinArgs& a, int blocks, int threads, cudaStream_t
     }
   }
   if (!a.literal) {
-    join_kernel<K, true, kMode><<<blocks, threads, 0, st>>>(a); note_launch();
+    join_kernel<K, kWordBits, true, kMode><<<blocks, threads, 0, st>>>(a); note_launch();
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
-  join_kernel<K, false, kMode><<<blocks, threads, 0, st>>>(a); note_launch();
+  join_kernel<K, kWordBits, false, kMode><<<blocks, threads, 0, st>>>(a); note_launch();
   return cudaGetLastError();
 }
 
+template <int K, int kWordBits>
+cudaError_t launch_width(const JoinArgs& a, int blocks, int threads, cudaStream_t st) {
+  if (a.vertex_exp) return launch_mode<K, kWordBits, kModeLog>(a, blocks, threads, st);
+  if (a.find_first) return launch_mode<K, kWordBits, kModeFind>(a, blocks, threads, st);
+  return launch_mode<K, kWordBits, kModeCount>(a, blocks, threads, st);
+}
+
+// Class 0 sets hold 32 bits: one 32-bit word.  Classes 1 and 2 run with 32- or
+// 64-bit words (the schedule's word_bits).
 template <int K>
-cudaError_t launch_class(const JoinArgs& a, int blocks, int threads, cudaStream_t st) {
-  if (a.vertex_exp) return launch_mode<K, kModeLog>(a, blocks, threads, st);
-  if (a.find_first) return launch_mode<K, kModeFind>(a, blocks, threads, st);
-  return launch_mode<K, kModeCount>(a, blocks, threads, st);
+cudaError_t launch_class(const JoinArgs& a, int blocks, int threads, int word_bits, cudaStream_t st) {
+  if constexpr (K == 0) {
+    (void)word_bits;
+    return launch_width<0, 32>(a, blocks, threads, st);
+  } else {
+    if (word_bits == 32) return launch_width<K, 32>(a, blocks, threads, st);
+    return launch_width<K, 64>(a, blocks, threads, st);
+  }
 }
 
 }  // namespace
@@ -991,11 +1064,12 @@ cudaError_t launch_join(const JoinArgs& args, const ClassLaunch cl[3], cudaStrea
       a.steps = cl[k].steps;
       a.refill = cl[k].refill;
       a.split_budget = !args.literal && r + 1 < kJoinRounds ? cl[k].split_budget : 0u;
+      a.lanes_log2 = cl[k].lanes_log2;
       if (timers) e = cudaEventRecord(timers[r][k][0], st);
       if (e != cudaSuccess) break;
-      e = k == 2 ? launch_class<2>(a, cl[k].blocks, cl[k].threads, ks)
-                 : (k == 1 ? launch_class<1>(a, cl[k].blocks, cl[k].threads, ks)
-                           : launch_class<0>(a, cl[k].blocks, cl[k].threads, ks));
+      e = k == 2 ? launch_class<2>(a, cl[k].blocks, cl[k].threads, cl[k].word_bits, ks)
+                 : (k == 1 ? launch_class<1>(a, cl[k].blocks, cl[k].threads, cl[k].word_bits, ks)
+                           : launch_class<0>(a, cl[k].blocks, cl[k].threads, cl[k].word_bits, ks));
       if (timers && e == cudaSuccess) e = cudaEventRecord(timers[r][k][1], st);
     }
     if (fork)  // the next round (and everything after) waits for all three classes

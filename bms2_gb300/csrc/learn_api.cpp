@@ -286,8 +286,8 @@ int bms_model_train(bms_ctx* c, const float* x, const float* y, uint32_t n, uint
   return BMS_OK;
 }
 
-// Times the join of the loaded workload under candidate launch shapes and
-// keeps the fastest.  Tasks are emitted once; every trial re-runs the join over
+// Times the join of the loaded workload under candidate schedules and keeps
+// the fastest.  Tasks are emitted once; every trial re-runs the join over
 // them from a reset work head.  The schedule table records the shape per query
 // size bucket (one shape serves all buckets of the single persistent launch).
 // Coordinate search over the join schedule, all buckets at once: every
@@ -321,6 +321,8 @@ int bms_autotune(bms_ctx* c, int R, int mode, int order, bms_schedule* out) {
   const uint32_t steps[] = {16, 32, 64};
   const uint32_t refills[] = {1, 2, 4, 8};
   const uint32_t depths[] = {0, 1};
+  const uint32_t lanes[] = {1, 2, 4, 8, 32};
+  const uint32_t words[] = {32, 64};
   auto sweep = [&](int n, auto apply) -> int {
     for (int i = 0; i < n; ++i) {
       bms_schedule s = best;
@@ -339,6 +341,8 @@ int bms_autotune(bms_ctx* c, int R, int mode, int order, bms_schedule* out) {
           best.steps[k] = pick.steps[k];
           best.refill[k] = pick.refill[k];
           best.split_depth[k] = pick.split_depth[k];
+          best.lanes_per_pair[k] = pick.lanes_per_pair[k];
+          best.word_bits[k] = pick.word_bits[k];
         }
     }
     return BMS_OK;
@@ -355,6 +359,14 @@ int bms_autotune(bms_ctx* c, int R, int mode, int order, bms_schedule* out) {
   r = sweep(4, [&](bms_schedule& s, int k, int i) { s.refill[k] = refills[i]; });
   if (r) return r;
   r = sweep(2, [&](bms_schedule& s, int k, int i) { s.split_depth[k] = depths[i]; });
+  if (r) return r;
+  // lanes per pair (per-pair tasks only): 1 lane, a few lanes, one warp per
+  // pair as the reference's sub-group decomposition (isomorphism.hpp:401)
+  r = sweep(int(sizeof(lanes) / sizeof(lanes[0])), [&](bms_schedule& s, int k, int i) { s.lanes_per_pair[k] = lanes[i]; });
+  if (r) return r;
+  // machine word of the search sets: 32- or 64-bit words for the 64- and
+  // 128-bit buckets (the 32-bit bucket has one 32-bit word)
+  r = sweep(2, [&](bms_schedule& s, int k, int i) { s.word_bits[k] = k == 0 ? 32u : words[i]; });
   if (r) return r;
   for (int k = 0; k < 3; ++k) best.ms[k] = best_ms[k];
   best.ms[3] = 0.f;

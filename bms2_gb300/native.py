@@ -73,7 +73,7 @@ class Schedule(C.Structure):
                 ("split_depth", C.c_uint32 * SCHED_BUCKETS), ("blocks_per_sm", C.c_uint32 * SCHED_BUCKETS),
                 ("warps_per_block", C.c_uint32 * SCHED_BUCKETS), ("steps", C.c_uint32 * SCHED_BUCKETS),
                 ("refill", C.c_uint32 * SCHED_BUCKETS), ("split_budget", C.c_uint32 * SCHED_BUCKETS),
-                ("ms", C.c_float * SCHED_BUCKETS)]
+                ("lanes_per_pair", C.c_uint32 * SCHED_BUCKETS), ("ms", C.c_float * SCHED_BUCKETS)]
 
     def as_dict(self) -> dict:
         return {k: list(getattr(self, k)) for k, _ in self._fields_}

@@ -24,7 +24,7 @@
 extern "C" {
 #endif
 
-#define BMS_ABI_VERSION 1
+#define BMS_ABI_VERSION 2
 
 /* Limits of this implementation.  The reference itself is defined for data
  * graphs of at most 64 nodes and queries of at most 30 nodes (64-bit bitsets,
@@ -339,26 +339,30 @@ int bms_model_predict(bms_ctx* ctx, float* cost, uint8_t* order);
 /* ------------------------------------------------------------ scheduling */
 /* Schedule of the persistent join, one row per size bucket.  Bucket b holds
  * the (query, data graph) pairs whose data graph has at most max_data_nodes[b]
- * nodes (32, 64, 128; bucket 3 is unused) and searches with bitsets of
- * word_bits[b] bits (32, 64, 128; both fixed by the bucket).  Per bucket:
- * task granularity (split_depth 0 = one task per pair, 1 = one per (pair,
- * root)), launch shape, DFS steps a warp runs between refills, how many idle
- * lanes trigger a refill, and the
- * expansions after which a search hands its unexplored subtrees to the next
- * round (0 = never).  bms_autotune times candidate schedules of every bucket
- * on the loaded workload (each bucket's kernels timed on their own) and
- * installs the fastest; ms[b] is the bucket's join time under the chosen row.
+ * nodes (32, 64, 128; bucket 3 is unused); its search sets hold that many
+ * bits, in machine words of word_bits[b] bits (32 or 64; bucket 0 always 32).
+ * Per bucket: task granularity (split_depth 0 = one task per pair, 1 = one per
+ * (pair, root)), lanes_per_pair (per-pair tasks: 1, 2, 4, 8, 16 or 32 lanes
+ * share a pair, lane g of the group searching the roots of rank g modulo the
+ * group size — 32 is one warp per pair, the reference's sub-group per task,
+ * isomorphism.hpp:401), launch shape, DFS steps a warp runs between refills,
+ * how many idle lanes trigger a refill, and the expansions after which a
+ * search hands its unexplored subtrees to the next round (0 = never).
+ * bms_autotune times candidate schedules of every bucket on the loaded
+ * workload (each bucket's kernels timed on their own) and installs the
+ * fastest; ms[b] is the bucket's join time under the chosen row.
  * BMS_OPT_JOIN_STEPS and BMS_OPT_SPLIT_BUDGET set their column for every bucket. */
 #define BMS_SCHED_BUCKETS 4
 typedef struct {
   uint32_t max_data_nodes[BMS_SCHED_BUCKETS]; /* read-only */
-  uint32_t word_bits[BMS_SCHED_BUCKETS];      /* read-only */
+  uint32_t word_bits[BMS_SCHED_BUCKETS];      /* 32 or 64 (bucket 0: 32) */
   uint32_t split_depth[BMS_SCHED_BUCKETS];
   uint32_t blocks_per_sm[BMS_SCHED_BUCKETS];
   uint32_t warps_per_block[BMS_SCHED_BUCKETS]; /* 1..8 */
   uint32_t steps[BMS_SCHED_BUCKETS];
   uint32_t refill[BMS_SCHED_BUCKETS];          /* idle lanes of a warp that trigger a refill, 1..32 */
   uint32_t split_budget[BMS_SCHED_BUCKETS];
+  uint32_t lanes_per_pair[BMS_SCHED_BUCKETS];  /* 1, 2, 4, 8, 16, 32 */
   float ms[BMS_SCHED_BUCKETS];
 } bms_schedule;
 int bms_get_schedule(bms_ctx* ctx, bms_schedule* out);

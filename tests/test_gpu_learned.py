@@ -125,3 +125,31 @@ def test_learned_order_requires_exact_semantics(ctx, trained):
     ctx.load(DATA, d)
     with pytest.raises(BmsError):
         ctx.run(2, COUNT_ALL, ORDER_LEARNED, 1)
+
+
+def test_trained_order_expands_less_than_plain_on_held_out_data():
+    # The network is trained on plain-order expansion logs of seed-A graphs and
+    # queries and evaluated on fresh seed-B graphs and queries of the same
+    # shape (the 1M-graph workload's size distribution): the learned order must
+    # need fewer DFS expansions than the plain GMCR order, with the same count
+    # on every pair.
+    from bms2_gb300 import Context
+
+    with Context(0) as c:
+        qa, da = workloads.make("mol1m", 101, n_data=20000, n_queries=1000)
+        c.load(QUERY, qa)
+        c.load(DATA, da)
+        x, y = collect(c, 6)
+        train(c, x, y, seed=101)
+        qb, db = workloads.make("mol1m", 202, n_data=20000, n_queries=1000)
+        c.load(QUERY, qb)
+        c.load(DATA, db)
+        plain = c.run(6, COUNT_ALL, ORDER_GMCR, SEM_EXACT)
+        plain_counts, plain_exps = c.pair_counts().copy(), c.stats()["expansions"]
+        learned = c.run(6, COUNT_ALL, ORDER_LEARNED, SEM_EXACT)
+        learned_exps = c.stats()["expansions"]
+        assert learned == plain
+        assert np.array_equal(c.pair_counts(), plain_counts)
+        ratio = plain_exps / learned_exps
+        print(f"held-out expansions: plain {plain_exps}, learned {learned_exps}, ratio {ratio:.3f}")
+        assert ratio > 1.04

@@ -515,6 +515,32 @@ def test_task_granularity_does_not_change_counts(ctx, split):
         ctx.set_schedule(sched)
 
 
+@pytest.mark.parametrize("lanes,words", [(1, 32), (2, 64), (4, 32), (8, 64), (32, 64), (32, 32)])
+def test_lanes_per_pair_and_word_width_keep_counts(ctx, lanes, words):
+    # lanes per pair (lane g of a group takes the roots of rank g mod lanes)
+    # and the search sets' machine word change the schedule, never a count or
+    # an expansion; all three size classes, count-all and find-first
+    d = Graphs.synth_molecules(300, 43, 0, 0, 0, 5, 120, 1, 4)
+    q = Graphs.synth_queries(d, 14, 44, 3, 16)
+    load(ctx, q, d)
+    before = ctx.schedule()
+    try:
+        s = dict(before)
+        s["lanes_per_pair"] = [lanes] * 3 + [1]
+        s["word_bits"] = [32, words, words, 64]
+        s["split_depth"] = [0, 0, 0, 0]
+        ctx.set_schedule(s)
+        for mode in (COUNT_ALL, FIND_FIRST):
+            want = oracle.run_pipeline(q, d, 2, find_first=mode == FIND_FIRST)
+            total = ctx.run(2, mode, ORDER_GMCR, SEM_EXACT)
+            assert total == want.total
+            assert np.array_equal(ctx.pair_counts(), want.counts)
+            if mode == COUNT_ALL:
+                assert np.array_equal(ctx.pair_expansions(), want.expansions)
+    finally:
+        ctx.set_schedule(before)
+
+
 def test_autotune_picks_a_valid_schedule_and_keeps_counts(ctx):
     d = Graphs.synth_molecules(400, 41, 0, 0, 0, 8, 120, 1, 4)
     q = Graphs.synth_queries(d, 16, 42, 3, 14)
@@ -523,8 +549,10 @@ def test_autotune_picks_a_valid_schedule_and_keeps_counts(ctx):
     before = ctx.schedule()
     try:
         s = ctx.autotune(2)
-        assert s["max_data_nodes"][:3] == [32, 64, 128] and s["word_bits"][:3] == [32, 64, 128]
+        assert s["max_data_nodes"][:3] == [32, 64, 128] and s["word_bits"][0] == 32
         for k in range(3):
+            assert s["word_bits"][k] in (32, 64)
+            assert s["lanes_per_pair"][k] in (1, 2, 4, 8, 32)
             assert s["blocks_per_sm"][k] in (2, 3, 4, 6, 8, 12)
             assert s["warps_per_block"][k] in (2, 4, 8)
             assert s["steps"][k] in (16, 32, 64)

@@ -21,7 +21,7 @@ def test_library_exports_every_declared_symbol():
     assert not missing, missing
     bound = {name for name, _, _ in native.SIGNATURES}
     assert declared == bound, declared ^ bound
-    assert native.lib().bms_abi_version() == 1
+    assert native.lib().bms_abi_version() == 2
 
 
 def test_parse_csr_follows_toCSRGraph():

@@ -465,14 +465,214 @@ def run_ours(args) -> None:
         line["results"]["oracle_sample_counts_equal"] = exact["counts_equal"]
         line["results"]["reference_dfs_oracle_counts_equal"] = literal["counts_equal"]
         parity_ok = exact["counts_equal"] and literal["counts_equal"]
-    if rank == 0:
-        print(json.dumps(line), flush=True)
     del ca_counts, rd_counts
     ctx.close()
+    del flush
+    torch.cuda.empty_cache()
+    if rank == 0 and world == 1 and args.workload == "mol1m" and not args.no_configs:
+        # the other GPU configurations, measured in the same run
+        configs = {}
+        for name, fn in (("mol100k", lambda: leg_mol100k(local, min(args.steps, 10), args.warmup, args.train_graphs)),
+                         ("mol10m", lambda: leg_mol10m(local, 1, args.train_graphs))):
+            t0 = time.perf_counter()
+            try:
+                configs[name] = fn()
+            except Exception as e:  # recorded, not fatal: the headline stands on its own
+                configs[name] = {"error": f"{type(e).__name__}: {e}"}
+            configs[name]["wall_seconds"] = time.perf_counter() - t0
+        line["configs"] = configs
+        parity_ok = parity_ok and all(c.get("counts_equal", True) for c in configs.values())
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
     if not parity_ok:
         sys.exit("per-pair counts differ from the oracle on the sample: the measurement is void")
+
+
+def _ms_timed(ctx, stream, flush, k, fn):
+    """k calls of fn, each bracketed by CUDA events on the library's stream
+    (L2 flushed before each, outside the events); mean ms and the last stats."""
+    import torch
+
+    ms = []
+    out = None
+    for _ in range(k):
+        flush.fill_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = fn()
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return float(np.mean(ms)), ctx.stats(), out
+
+
+def leg_mol100k(local: int, steps: int, warmup: int, train_graphs: int) -> dict:
+    """The plain-method GPU configuration: 100,000 data graphs (N(28, 9) atoms,
+    10-60) x 600 queries of 5-30 nodes (30% pure carbon); count-all and
+    find-first in plain GMCR order, the reference's literal DFS, and the
+    learned order, each compared pair by pair with the oracle on a sample."""
+    import torch
+
+    import oracle
+    from bms2_gb300 import (COUNT_ALL, DATA, FIND_FIRST, ORDER_GMCR, ORDER_LEARNED, QUERY, SEM_EXACT,
+                            SEM_REFERENCE_DFS, Context, workloads)
+
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    out = {"workload": "mol100k: 100000 data graphs x 600 queries, refine steps 6"}
+    with Context(local) as ctx:
+        ctx.set_stream(stream.cuda_stream)
+        out.update(train_cost_model(ctx, "mol100k", seed=101, n_data=train_graphs))
+        tq, td = workloads.make("mol100k", 101)
+        ctx.load(QUERY, tq)
+        ctx.load(DATA, td)
+        ctx.autotune(REFINE_STEPS, COUNT_ALL, ORDER_GMCR)
+        q, d = workloads.make("mol100k", 202)
+        Q, D = q.n_graphs, d.n_graphs
+        ctx.load(QUERY, q)
+        ctx.load(DATA, d)
+        res = {}
+        for name, mode, order, sem in (("plain", COUNT_ALL, ORDER_GMCR, SEM_EXACT),
+                                       ("learned", COUNT_ALL, ORDER_LEARNED, SEM_EXACT),
+                                       ("find_first", FIND_FIRST, ORDER_GMCR, SEM_EXACT),
+                                       ("reference_dfs", COUNT_ALL, ORDER_GMCR, SEM_REFERENCE_DFS)):
+            def run(mode=mode, order=order, sem=sem):
+                return ctx.run(REFINE_STEPS, mode, order, sem)
+            for _ in range(warmup):
+                run()
+            ms, st, total = _ms_timed(ctx, stream, flush, steps, run)
+            off, qidx = ctx.gmcr()
+            res[name] = {"value": Q * D / (ms / 1e3), "ms_per_step": ms, "ms_join": st["ms_join"],
+                         "total": int(total), "expansions": int(st["expansions"]),
+                         "_counts": ctx.pair_counts(), "_gmcr": (off, qidx)}
+        qa, da = q.arrays(), d.arrays()
+        k = 2048
+        threads = os.cpu_count() or 1
+        checks = {}
+        for name, kw in (("plain", {}), ("find_first", {"find_first": True}), ("reference_dfs", {"dfs_literal": True})):
+            want = oracle.run_pipeline(qa, _head(da, k), REFINE_STEPS, threads=threads, keep_steps=False, **kw)
+            off, qidx = res[name]["_gmcr"]
+            checks[name] = sample_parity(off, qidx, res[name]["_counts"], want, k)
+        learned_equal = bool(np.array_equal(res["learned"]["_counts"], res["plain"]["_counts"]))
+        for r in res.values():
+            r.pop("_counts")
+            r.pop("_gmcr")
+        out.update({"data_graphs": D, "queries": Q, "runs": res, "oracle_sample": checks,
+                    "learned_counts_equal_plain_every_pair": learned_equal,
+                    "learned_over_plain": res["learned"]["value"] / res["plain"]["value"],
+                    "expansion_ratio_plain_over_learned": res["plain"]["expansions"] / max(1, res["learned"]["expansions"]),
+                    "counts_equal": all(c["counts_equal"] for c in checks.values()) and learned_equal})
+    del flush
+    torch.cuda.empty_cache()
+    return out
+
+
+def leg_mol10m(local: int, warmup: int, train_graphs: int, slice_graphs: int = 500_000,
+               latency_sample: int = 16) -> dict:
+    """The large mixed configuration: 10,000,000 data graphs resident in HBM x
+    3,000 queries (20% adversarial).  One pass each in the learned and in the
+    plain GMCR order (windows of slice_graphs data graphs), the batch driver
+    from page-locked host memory (e2e), per-query latency over all resident
+    graphs, and the engine against the oracle pair by pair on a prefix."""
+    import torch
+
+    import oracle
+    from bms2_gb300 import (COUNT_ALL, DATA, OPT_RESIDENT_SIGNATURES, ORDER_GMCR, ORDER_LEARNED, QUERY, SEM_EXACT,
+                            Context, Graphs, shards, workloads)
+
+    dev = torch.device("cuda", local)
+    out = {"workload": f"mol10m: 10000000 data graphs x 3000 queries (20% adversarial), resident in HBM, windows of "
+                       f"{slice_graphs}, refine steps 6"}
+    with Context(local) as ctx:
+        out.update(train_cost_model(ctx, "mol10m", seed=101, n_data=train_graphs))
+        t0 = time.perf_counter()
+        q, d = workloads.make("mol10m", 202)
+        out["synth_seconds"] = time.perf_counter() - t0
+        Q, D = q.n_graphs, d.n_graphs
+        ctx.load(QUERY, q)
+        # pair by pair against the oracle on the first 1,024 data graphs
+        qa = q.arrays()
+        head = _head(d.arrays(), 1024)
+        ctx.load(DATA, Graphs.from_csr(**head))
+        ctx.run(REFINE_STEPS, COUNT_ALL, ORDER_LEARNED, SEM_EXACT)
+        off, qidx = ctx.gmcr()
+        want = oracle.run_pipeline(qa, head, REFINE_STEPS, threads=os.cpu_count() or 1, keep_steps=False)
+        out["oracle_sample"] = sample_parity(off, qidx, ctx.pair_counts(), want, 1024)
+        del head
+        # e2e: the batch driver from page-locked host memory (after one sizing pass)
+        d.pin()
+        ctx.run_batches(d, slice_graphs, REFINE_STEPS, COUNT_ALL, ORDER_LEARNED, SEM_EXACT)
+        torch.cuda.synchronize(dev)
+        t = time.perf_counter()
+        e2e_total, _ = ctx.run_batches(d, slice_graphs, REFINE_STEPS, COUNT_ALL, ORDER_LEARNED, SEM_EXACT)
+        torch.cuda.synchronize(dev)
+        e2e_s = time.perf_counter() - t
+        d.unpin()
+        ctx.load_resident(d)
+        passes = {}
+        for name, order in (("learned", ORDER_LEARNED), ("plain", ORDER_GMCR)):
+            for _ in range(max(1, warmup)):
+                ctx.run_resident(slice_graphs, REFINE_STEPS, COUNT_ALL, order, SEM_EXACT)
+            torch.cuda.synchronize(dev)
+            t = time.perf_counter()
+            total, per_query = ctx.run_resident(slice_graphs, REFINE_STEPS, COUNT_ALL, order, SEM_EXACT)
+            torch.cuda.synchronize(dev)
+            sec = time.perf_counter() - t
+            st = ctx.stats()
+            passes[name] = {"value": Q * D / sec, "seconds_per_pass": sec, "total": int(total),
+                            "expansions": int(st["expansions"]), "ms_join": st["ms_join"], "ms_filter": st["ms_filter"],
+                            "ms_signatures": st["ms_signatures"], "_per_query": per_query}
+        same = bool(np.array_equal(passes["learned"]["_per_query"], passes["plain"]["_per_query"]))
+        per_query = passes["learned"]["_per_query"]
+        rng = np.random.default_rng(7)
+        sample = np.sort(rng.choice(Q, size=min(latency_sample, Q), replace=False))
+        lat = []
+        for qi in sample:
+            ctx.load(QUERY, Graphs.from_csr(**shards.take_graphs(qa, np.array([qi]))))
+            torch.cuda.synchronize(dev)
+            t = time.perf_counter()
+            one, _ = ctx.run_resident(slice_graphs, REFINE_STEPS, COUNT_ALL, ORDER_LEARNED, SEM_EXACT)
+            torch.cuda.synchronize(dev)
+            lat.append(time.perf_counter() - t)
+            if one != int(per_query[qi]):
+                raise AssertionError("single-query pass disagrees with the batched pass")
+        ctx.set_option(OPT_RESIDENT_SIGNATURES, 1)
+        ctx.run_resident(slice_graphs, REFINE_STEPS, COUNT_ALL, ORDER_LEARNED, SEM_EXACT)
+        lat_c = []
+        for qi in sample:
+            ctx.load(QUERY, Graphs.from_csr(**shards.take_graphs(qa, np.array([qi]))))
+            torch.cuda.synchronize(dev)
+            t = time.perf_counter()
+            ctx.run_resident(slice_graphs, REFINE_STEPS, COUNT_ALL, ORDER_LEARNED, SEM_EXACT)
+            torch.cuda.synchronize(dev)
+            lat_c.append(time.perf_counter() - t)
+        ctx.set_option(OPT_RESIDENT_SIGNATURES, 0)
+        for r in passes.values():
+            r.pop("_per_query")
+        fbytes = algorithmic_filter_bytes(int(qa["graph_offsets"][-1]), int(d.n_nodes), REFINE_STEPS)
+        peak, peak_kind = peaks()
+        f_ms = passes["learned"]["ms_filter"]
+        out.update({"data_graphs": D, "queries": Q, "passes": passes,
+                    "learned_over_plain": passes["learned"]["value"] / passes["plain"]["value"],
+                    "expansion_ratio_plain_over_learned": passes["plain"]["expansions"] / max(1, passes["learned"]["expansions"]),
+                    "per_query_totals_equal_across_orders": same,
+                    "e2e": {"value": Q * D / e2e_s, "unit": "pairs/s", "seconds": e2e_s,
+                            "total_equal_resident": int(e2e_total) == passes["learned"]["total"]},
+                    "query_latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                                        "sample": int(len(lat))},
+                    "query_latency_s_resident_signatures": {"p50": float(np.percentile(lat_c, 50)),
+                                                            "p99": float(np.percentile(lat_c, 99))},
+                    "roofline_filter": {"achieved": fbytes / (f_ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                                        "frac": fbytes / (f_ms / 1e3) / 1e9 / peak, "equivalent": True,
+                                        "peak_kind": f"{peak_kind} hbm_gbs"},
+                    "outside_reference_domain": outside_reference_domain(qa["graph_offsets"], graph_offsets(d)),
+                    "counts_equal": out["oracle_sample"]["counts_equal"] and same and
+                                    int(e2e_total) == passes["learned"]["total"]})
+    torch.cuda.empty_cache()
+    return out
 
 
 def run_streamed(args) -> None:
@@ -851,6 +1051,8 @@ def main() -> None:
                     help="seed-A data graphs for the join autotuner (-1: the workload's full size, 0: off)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="mol1m: skip the mol100k and mol10m measurements that follow the headline")
     ap.add_argument("--data-graphs", type=int, default=None, help="shrink the workload (profiling)")
     ap.add_argument("--once", action="store_true", help="one untimed pipeline run (profiling)")
     args = ap.parse_args()

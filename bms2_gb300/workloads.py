@@ -9,8 +9,9 @@ distributions stand in for them.  Every workload is a pure function of its seed.
             5-30 nodes of which 30% are pure-carbon chains or rings
   mol1m     1,000,000 data graphs, log-normal atoms (median 25, sigma 0.55)
             clipped to 5-120, 1,000 queries of 3-40 nodes
-  mol10m    10,000,000 data graphs as mol1m (about 290M atoms), 3,000 queries of
-            3-40 nodes of which 20% are adversarial symmetric patterns
+  mol10m    10,000,000 data graphs as mol1m (about 290M atoms, drawn in ten
+            seeded blocks of 1,000,000), 3,000 queries of 3-40 nodes of which
+            20% are adversarial symmetric patterns
 Element mix C 72%, N 12%, O 11%, S 2%, F 1.5%, Cl 1%, Br 0.5%; degree <= 4;
 1-4 rings per molecule; bonds single/double/triple/aromatic 60/20/2/18%.
 """
@@ -45,10 +46,55 @@ WORKLOADS = {
 }
 
 
+BLOCK_GRAPHS = 1_000_000
+
+
+def block_seed(seed: int, b: int) -> int:
+    """Seed of block b of a data batch: block 0 keeps the batch's seed, so any
+    batch of at most BLOCK_GRAPHS graphs is one sequential draw."""
+    return seed if b == 0 else (seed * 0x9E3779B1 + 0x7F4A7C15 * b) & 0xFFFFFFFFFFFFFFFF
+
+
+def _molecules(w: Workload, n: int, seed: int) -> Graphs:
+    """n data graphs of workload w: blocks of BLOCK_GRAPHS graphs, each a
+    sequential draw with its own seed, generated on parallel threads and
+    concatenated in block order."""
+    if n <= BLOCK_GRAPHS:
+        return Graphs.synth_molecules(n, seed, w.size_dist, w.p0, w.p1, w.min_atoms, w.max_atoms, 1, 4)
+    import concurrent.futures as cf
+    import os
+
+    import numpy as np
+
+    sizes = [min(BLOCK_GRAPHS, n - b) for b in range(0, n, BLOCK_GRAPHS)]
+
+    def one(b: int) -> dict:
+        g = Graphs.synth_molecules(sizes[b], block_seed(seed, b), w.size_dist, w.p0, w.p1, w.min_atoms, w.max_atoms,
+                                   1, 4)
+        return g.arrays()
+
+    with cf.ThreadPoolExecutor(max_workers=min(len(sizes), os.cpu_count() or 1)) as ex:
+        parts = list(ex.map(one, range(len(sizes))))
+    node_base = np.cumsum([0] + [len(p["node_labels"]) for p in parts])
+    entry_base = np.cumsum([0] + [len(p["column_indices"]) for p in parts])
+    go = np.concatenate([parts[0]["graph_offsets"][:1]] +
+                        [p["graph_offsets"][1:].astype(np.uint64) + node_base[i] for i, p in enumerate(parts)])
+    ro = np.concatenate([parts[0]["row_offsets"][:1]] +
+                        [p["row_offsets"][1:].astype(np.uint64) + entry_base[i] for i, p in enumerate(parts)])
+    ci = np.concatenate([p["column_indices"].astype(np.uint64) + node_base[i] for i, p in enumerate(parts)])
+    if go[-1] >= 1 << 32 or ro[-1] >= 1 << 32:
+        raise ValueError("batch exceeds 32-bit node or entry ids")
+    return Graphs.from_csr(go.astype(np.uint32), ro.astype(np.uint32), ci.astype(np.uint32),
+                           np.concatenate([p["node_labels"] for p in parts]),
+                           np.concatenate([p["edge_labels"] for p in parts]))
+
+
 def make(name: str, seed: int = 1, n_data: int | None = None, n_queries: int | None = None) -> tuple[Graphs, Graphs]:
-    """(queries, data) of a named workload; n_data / n_queries shrink it."""
+    """(queries, data) of a named workload; n_data / n_queries shrink it.
+    Batches of more than BLOCK_GRAPHS data graphs are drawn in seeded blocks
+    (block_seed) on parallel threads."""
     w = WORKLOADS[name]
-    data = Graphs.synth_molecules(n_data or w.n_data, seed, w.size_dist, w.p0, w.p1, w.min_atoms, w.max_atoms, 1, 4)
+    data = _molecules(w, n_data or w.n_data, seed)
     queries = Graphs.synth_queries(data, n_queries or w.n_queries, seed + 1000003, w.q_min, w.q_max, w.frac_carbon,
                                    w.frac_adversarial)
     return queries, data

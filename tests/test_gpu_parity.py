@@ -520,15 +520,22 @@ def test_lanes_per_pair_and_word_width_keep_counts(ctx, lanes, words):
     # lanes per pair (lane g of a group takes the roots of rank g mod lanes)
     # and the search sets' machine word change the schedule, never a count or
     # an expansion; all three size classes, count-all and find-first
+    # (expansions are compared with the default schedule's: pairs that the
+    # fused filter's label screen proves empty are never searched, so their
+    # expansions are 0 where the oracle's search spends a few)
     d = Graphs.synth_molecules(300, 43, 0, 0, 0, 5, 120, 1, 4)
     q = Graphs.synth_queries(d, 14, 44, 3, 16)
     load(ctx, q, d)
     before = ctx.schedule()
     try:
-        s = dict(before)
+        base = dict(before)
+        base["split_depth"] = [0, 0, 0, 0]
+        ctx.set_schedule(base)
+        ctx.run(2, COUNT_ALL, ORDER_GMCR, SEM_EXACT)
+        base_exps = ctx.pair_expansions().copy()
+        s = dict(base)
         s["lanes_per_pair"] = [lanes] * 3 + [1]
         s["word_bits"] = [32, words, words, 64]
-        s["split_depth"] = [0, 0, 0, 0]
         ctx.set_schedule(s)
         for mode in (COUNT_ALL, FIND_FIRST):
             want = oracle.run_pipeline(q, d, 2, find_first=mode == FIND_FIRST)
@@ -536,7 +543,7 @@ def test_lanes_per_pair_and_word_width_keep_counts(ctx, lanes, words):
             assert total == want.total
             assert np.array_equal(ctx.pair_counts(), want.counts)
             if mode == COUNT_ALL:
-                assert np.array_equal(ctx.pair_expansions(), want.expansions)
+                assert np.array_equal(ctx.pair_expansions(), base_exps)
     finally:
         ctx.set_schedule(before)
 

@@ -20,8 +20,10 @@ training); the timed steps run on seed-B inputs, and the plain GMCR order is
 timed on the same inputs for the learned-over-plain ratio, with per-pair counts
 compared.
 
-With N > 1 (torchrun, one rank per GPU) every rank processes its own shard of
-data graphs (seeded by rank): weak scaling, no collective on the data path.
+With N > 1 (torchrun, one rank per GPU) the data batch is N times the
+single-GPU batch, split across the ranks by the reference MPI driver's LPT
+balancing; every rank runs the whole pipeline on its shard (weak scaling), and
+the only collectives are the final sums and the maximum of the timed region.
 """
 from __future__ import annotations
 
@@ -217,7 +219,7 @@ def run_ours(args) -> None:
     import torch.distributed as dist
 
     from bms2_gb300 import (COUNT_ALL, DATA, FIND_FIRST, ORDER_GMCR, ORDER_LEARNED, QUERY, SEM_EXACT,
-                            SEM_REFERENCE_DFS, Context, shards, workloads)
+                            SEM_REFERENCE_DFS, Context, Graphs, shards, workloads)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -247,8 +249,20 @@ def run_ours(args) -> None:
                      "split_budget": s["split_budget"][k], "tuned_join_ms": round(s["ms"][k], 3)}
                     for k in range(3)]
         del tq, td
-    # evaluation workload (seed B; each rank its own shard)
-    q, d = workloads.make(args.workload, 202 + rank, n_data=args.data_graphs)
+    # evaluation workload (seed B).  With N ranks the data batch is N blocks of
+    # the single-GPU batch's size (block 0 is that batch; queries are the
+    # single-GPU queries), split across the ranks by the reference MPI driver's
+    # LPT balancing (BMS2_mpi.cpp:78-157): each rank holds about one block
+    q, d = workloads.make(args.workload, 202, n_data=args.data_graphs)
+    d_total = d.n_graphs
+    if world > 1:
+        full = workloads.make_data(args.workload, 202, n_data=world * d.n_graphs)
+        fa = full.arrays()
+        del full
+        owners = shards.lpt_owners_native(fa, world)
+        d = Graphs.from_csr(**shards.take_graphs(fa, np.nonzero(owners == rank)[0]))
+        d_total = len(fa["graph_offsets"]) - 1
+        del fa, owners
     Q, D = q.n_graphs, d.n_graphs
     qa, da = q.arrays(), d.arrays()
     ctx.load(QUERY, q)
@@ -326,7 +340,7 @@ def run_ours(args) -> None:
     for _ in range(args.warmup):
         step(order, FIND_FIRST)
     ff_ms, ff_stage, ff_total = timed(order, args.steps, FIND_FIRST)
-    find_first = {"find_first_value": world * Q * D / (float(np.mean(ff_ms)) / 1e3),
+    find_first = {"find_first_value": Q * d_total / (float(np.mean(ff_ms)) / 1e3),
                   "find_first_ms_per_step": float(np.mean(ff_ms)),
                   "find_first_join_ms": float(np.mean([s["ms_join"] for s in ff_stage])),
                   "find_first_pairs_matched": int(ff_total),
@@ -340,7 +354,7 @@ def run_ours(args) -> None:
     rd_ms, rd_stage, rd_total = timed(ORDER_GMCR, rd_steps, COUNT_ALL, SEM_REFERENCE_DFS)
     rd_counts = ctx.pair_counts()
     rd_off, rd_qidx = ctx.gmcr()
-    reference_dfs = {"reference_dfs_value": world * Q * D / (float(np.mean(rd_ms)) / 1e3),
+    reference_dfs = {"reference_dfs_value": Q * d_total / (float(np.mean(rd_ms)) / 1e3),
                      "reference_dfs_ms_per_step": float(np.mean(rd_ms)),
                      "reference_dfs_join_ms": float(np.mean([s_["ms_join"] for s_ in rd_stage])),
                      "reference_dfs_total_matches": int(rd_total), "reference_dfs_steps": rd_steps}
@@ -377,7 +391,7 @@ def run_ours(args) -> None:
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e_s = float(np.mean(e2e_ms)) / 1e3
     pairs = Q * D
-    value = world * pairs * args.steps / t_total
+    value = Q * d_total * args.steps / t_total  # all ranks' pairs over the slowest rank's time
     peak, peak_kind = peaks()
     fbytes = algorithmic_filter_bytes(st["n_query_nodes"], st["n_data_nodes"], REFINE_STEPS)
     f_ms = float(np.mean([s["ms_filter"] for s in stage]))
@@ -406,9 +420,10 @@ def run_ours(args) -> None:
                                f"count-all, EXACT semantics, order {args.order}",
                    "data_graphs_per_gpu": D, "queries": Q, "refine_steps": REFINE_STEPS, "order": args.order,
                    "l2": "flushed between steps (512 MiB write outside the timed events)",
-                   "parallelism": f"data-graph shards x{world}",
+                   "parallelism": f"data-graph shards x{world} (LPT, BMS2_mpi.cpp:78-157)",
+                   "data_graphs_all_ranks": d_total,
                    "outside_reference_domain": outside_reference_domain(qa["graph_offsets"], da["graph_offsets"])},
-        "e2e": {"value": world * pairs / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": h2d,
+        "e2e": {"value": Q * d_total / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": int(T * 8)},
         "roofline": {"kernel": "sliced_filter (fused filter + refine + GMCR validity)", "bound": "hbm",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -433,7 +448,7 @@ def run_ours(args) -> None:
     }
     if plain is not None:
         line["results"].update(plain)
-        line["results"]["plain_value"] = world * pairs / (plain["plain_ms_per_step"] / 1e3)
+        line["results"]["plain_value"] = Q * d_total / (plain["plain_ms_per_step"] / 1e3)
         line["results"]["learned_over_plain"] = line["results"]["plain_value"] and value / line["results"]["plain_value"]
         line["results"]["expansion_ratio_plain_over_learned"] = float(plain["plain_expansions"]) / max(1, st["expansions"])
     line["results"].update(extra)
@@ -945,9 +960,10 @@ def run_clustered(args) -> None:
                                f"refine steps {REFINE_STEPS}, count-all, EXACT, clustered join (--use-cs)",
                    "data_graphs_per_gpu": D, "queries": Q, "refine_steps": REFINE_STEPS, "order": "plain",
                    "l2": "flushed between steps (512 MiB write outside the timed events)",
-                   "parallelism": f"data-graph shards x{world}",
+                   "parallelism": f"data-graph shards x{world} (LPT, BMS2_mpi.cpp:78-157)",
+                   "data_graphs_all_ranks": d_total,
                    "outside_reference_domain": outside_reference_domain(qa["graph_offsets"], da["graph_offsets"])},
-        "e2e": {"value": world * pairs / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": h2d,
+        "e2e": {"value": Q * d_total / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": int(T * 8)},
         "roofline": {"kernel": "sliced_filter (fused filter + refine + GMCR validity)", "bound": "hbm",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,

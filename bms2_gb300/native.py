@@ -102,6 +102,7 @@ SIGNATURES = [
     ("bms_graphs_unpin", C.c_int, [_vp]),
     ("bms_synth_molecules", C.c_int, [C.POINTER(MolParams), C.c_uint64, C.POINTER(_vp)]),
     ("bms_synth_queries", C.c_int, [C.POINTER(QueryParams), _vp, C.c_uint64, C.POINTER(_vp)]),
+    ("bms_shard_lpt", C.c_int, [C.c_uint32, _u32p, _u32p, C.c_uint32, _u32p, C.POINTER(C.c_double)]),
     ("bms_create", C.c_int, [C.c_int, C.POINTER(_vp)]),
     ("bms_destroy", None, [_vp]),
     ("bms_set_stream", C.c_int, [_vp, _vp]),

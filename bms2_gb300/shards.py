@@ -40,29 +40,42 @@ def lpt_owners(costs: np.ndarray, world: int) -> np.ndarray:
     return owners
 
 
+def lpt_owners_native(arrays: dict, world: int) -> np.ndarray:
+    """lpt_owners(graph_costs(arrays), world) computed by libbms
+    (bms_shard_lpt), for batches of millions of graphs."""
+    import ctypes as C
+
+    from .native import _check, _ptr, lib
+
+    go = np.ascontiguousarray(arrays["graph_offsets"], dtype=np.uint32)
+    ro = np.ascontiguousarray(arrays["row_offsets"], dtype=np.uint32)
+    owners = np.zeros(max(len(go) - 1, 1), dtype=np.uint32)
+    _check(lib().bms_shard_lpt(len(go) - 1, _ptr(go, C.c_uint32), _ptr(ro, C.c_uint32), world,
+                               _ptr(owners, C.c_uint32), None))
+    return owners[: len(go) - 1].astype(np.int32)
+
+
 def take_graphs(arrays: dict, idx: np.ndarray) -> dict:
     """The CSR batch of graphs `idx` (in that order), ids rebased."""
     go = np.asarray(arrays["graph_offsets"], dtype=np.int64)
     ro = np.asarray(arrays["row_offsets"], dtype=np.int64)
     ci = np.asarray(arrays["column_indices"], dtype=np.int64)
-    nl, el = arrays["node_labels"], arrays["edge_labels"]
-    out_go, out_ro, out_ci, out_nl, out_el = [0], [], [], [], []
-    n_nodes = n_entries = 0
-    for g in np.asarray(idx, dtype=np.int64):
-        s, e = int(go[g]), int(go[g + 1])
-        rs, re = int(ro[s]), int(ro[e])
-        out_ci.append(ci[rs:re] - s + n_nodes)
-        out_ro.append(ro[s + 1:e + 1] - rs + n_entries)
-        out_nl.append(nl[s:e])
-        out_el.append(el[rs:re])
-        n_nodes += e - s
-        n_entries += re - rs
-        out_go.append(n_nodes)
-    cat = lambda xs, dt: np.concatenate(xs).astype(dt) if xs else np.zeros(0, dt)  # noqa: E731
-    return {"graph_offsets": np.asarray(out_go, dtype=np.uint32),
-            "row_offsets": np.concatenate([np.zeros(1, np.int64)] + out_ro).astype(np.uint32),
-            "column_indices": cat(out_ci, np.uint32), "node_labels": cat(out_nl, np.uint8),
-            "edge_labels": cat(out_el, np.uint8)}
+    nl, el = np.asarray(arrays["node_labels"]), np.asarray(arrays["edge_labels"])
+    idx = np.asarray(idx, dtype=np.int64)
+    sizes = go[idx + 1] - go[idx]
+    new_go = np.zeros(len(idx) + 1, np.int64)
+    np.cumsum(sizes, out=new_go[1:])
+    # the nodes taken, in order, and the graph each belongs to
+    node_src = np.repeat(go[idx] - new_go[:-1], sizes) + np.arange(new_go[-1])
+    ent = ro[node_src + 1] - ro[node_src]
+    new_ro = np.zeros(len(node_src) + 1, np.int64)
+    np.cumsum(ent, out=new_ro[1:])
+    ent_src = np.repeat(ro[node_src] - new_ro[:-1], ent) + np.arange(new_ro[-1])
+    # a column id moves with its graph: old id - old graph start + new graph start
+    shift = np.repeat(np.repeat(new_go[:-1] - go[idx], sizes), ent)
+    return {"graph_offsets": new_go.astype(np.uint32), "row_offsets": new_ro.astype(np.uint32),
+            "column_indices": (ci[ent_src] + shift).astype(np.uint32), "node_labels": nl[node_src].astype(np.uint8),
+            "edge_labels": el[ent_src].astype(np.uint8)}
 
 
 def reduce_totals(total_matches: int, valid_pairs: int, seconds: float, device=None) -> tuple[int, int, float]:

@@ -89,6 +89,12 @@ def _molecules(w: Workload, n: int, seed: int) -> Graphs:
                            np.concatenate([p["edge_labels"] for p in parts]))
 
 
+def make_data(name: str, seed: int = 1, n_data: int | None = None) -> Graphs:
+    """The data graphs of a named workload alone (as make draws them)."""
+    w = WORKLOADS[name]
+    return _molecules(w, n_data or w.n_data, seed)
+
+
 def make(name: str, seed: int = 1, n_data: int | None = None, n_queries: int | None = None) -> tuple[Graphs, Graphs]:
     """(queries, data) of a named workload; n_data / n_queries shrink it.
     Batches of more than BLOCK_GRAPHS data graphs are drawn in seeded blocks

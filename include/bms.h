@@ -138,6 +138,15 @@ typedef struct {
  * numbered in random depth-first discovery order. */
 int bms_synth_queries(const bms_query_params* p, const bms_graphs* source, uint64_t seed, bms_graphs** out);
 
+/* ------------------------------------------------------------------ shards */
+/* Owner rank of every data graph for `world` GPUs: the reference MPI driver's
+ * longest-processing-time balancing (BMS2_mpi.cpp:78-157): cost = nodes^2 +
+ * edges, graphs by decreasing cost (stable), each to the least-loaded rank (the
+ * lowest on ties).  owners[n_graphs]; loads[world] (nullable) receives each
+ * rank's summed cost.  Host only. */
+int bms_shard_lpt(uint32_t n_graphs, const uint32_t* graph_offsets, const uint32_t* row_offsets, uint32_t world,
+                  uint32_t* owners, double* loads);
+
 /* --------------------------------------------------------------- contexts */
 typedef struct bms_ctx bms_ctx;
 int bms_create(int device, bms_ctx** out);

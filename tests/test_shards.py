@@ -92,3 +92,12 @@ def test_two_gloo_ranks_equal_one_process(tmp_path):
         seen[idx] = True
     assert seen.all()
     assert np.array_equal(dense, whole.pair_counts_dense(q.n_graphs))
+
+
+def test_native_lpt_equals_the_restatement():
+    # bms_shard_lpt (libbms, host code) and lpt_owners give the same owners,
+    # ties included (many equal costs among small molecules)
+    for n, world in ((1, 3), (500, 2), (3000, 8)):
+        _, d = workloads.make("mol1k", 7, n_data=n, n_queries=2)
+        a = d.arrays()
+        assert np.array_equal(shards.lpt_owners_native(a, world), shards.lpt_owners(shards.graph_costs(a), world))

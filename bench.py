@@ -207,7 +207,7 @@ def train_cost_model(ctx, workload: str, seed: int, n_data: int) -> dict:
     qa, da = workloads.make(workload, seed, n_data=n_data)
     ctx.load(QUERY, qa)
     ctx.load(DATA, da)
-    x, y = collect(ctx, REFINE_STEPS)
+    x, y = collect(ctx, REFINE_STEPS, qa.arrays())
     loss = train(ctx, x, y, seed=seed)
     del COUNT_ALL, ORDER_GMCR, SEM_EXACT
     return {"train_samples": int(len(y)), "train_loss": float(loss), "train_seed": seed, "train_data_graphs": n_data,

@@ -142,6 +142,7 @@ int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const 
   s.h_goff.assign(v.graph_offsets, v.graph_offsets + G + 1);
   if (node_base)
     for (auto& x : s.h_goff) x -= node_base;
+  if (&s == &c->q) c->given_set = false;  // explicit orders belong to the queries they were set for
   s.labels_lt16 = 0;  // the query side's label set packs the shell clauses
   if (&s == &c->q)
     for (uint64_t i = 0; i < N; ++i)
@@ -396,6 +397,8 @@ int join_records(bms_ctx* c, int mode, int order, int sem, bool log_vertices, co
   if (order == BMS_ORDER_LEARNED) {
     int r = learned_order(c);
     if (r) return r;
+  } else if (order == BMS_ORDER_GIVEN) {
+    CK(cudaMemcpyAsync(c->perm.p, c->given_perm.p, Qslots, cudaMemcpyDeviceToDevice, c->st));
   } else {
     CK(launch_plain_order(c->q.dg(), order_of(c), c->st));
   }
@@ -457,14 +460,17 @@ float elapsed(bms_ctx* c, Ev a, Ev b) {
 
 int validate_modes(bms_ctx* c, int mode, int order, int sem) {
   if (mode != BMS_FIND_FIRST && mode != BMS_COUNT_ALL) return fail(c, BMS_EINVAL, "invalid mode");
-  if (order != BMS_ORDER_GMCR && order != BMS_ORDER_LEARNED) return fail(c, BMS_EINVAL, "invalid order");
+  if (order != BMS_ORDER_GMCR && order != BMS_ORDER_LEARNED && order != BMS_ORDER_GIVEN)
+    return fail(c, BMS_EINVAL, "invalid order");
+  if (order == BMS_ORDER_GIVEN && !c->given_set)
+    return fail(c, BMS_ESTATE, "BMS_ORDER_GIVEN: set the orders of the loaded queries with bms_set_query_order");
   if (sem != BMS_SEM_EXACT && sem != BMS_SEM_REFERENCE_DFS) return fail(c, BMS_EINVAL, "invalid semantics");
   if (sem == BMS_SEM_REFERENCE_DFS && order != BMS_ORDER_GMCR)
     return fail(c, BMS_EINVAL, "REFERENCE_DFS semantics require the GMCR order");
   if (c->use_cs && order != BMS_ORDER_GMCR)
     return fail(c, BMS_EINVAL, "the clustered join extends the prototype's nodes first: it requires the GMCR order");
-  if (order == BMS_ORDER_LEARNED && (c->q.asymmetric || c->d.asymmetric))
-    return fail(c, BMS_EINVAL, "the learned order requires symmetric adjacency");
+  if (order != BMS_ORDER_GMCR && (c->q.asymmetric || c->d.asymmetric))
+    return fail(c, BMS_EINVAL, "a search order other than the GMCR order requires symmetric adjacency");
   return BMS_OK;
 }
 
@@ -702,6 +708,31 @@ int bms_set_option(bms_ctx* c, int option, int64_t value) {
   }
 }
 
+int bms_set_query_order(bms_ctx* c, const uint8_t* order, uint64_t n) {
+  GUARD(c);
+  if (!c->q.loaded) return fail(c, BMS_ESTATE, "load the query graphs first");
+  if (n != c->q.N || (n && !order)) return fail(c, BMS_EINVAL, "the order must hold one entry per query node");
+  const uint32_t Q = c->q.G;
+  std::vector<uint8_t> perm(uint64_t(Q ? Q : 1) * kMaxQueryNodes, 0);
+  for (uint32_t g = 0; g < Q; ++g) {
+    const uint32_t qoff = c->q.h_goff[g], m = c->q.h_goff[g + 1] - qoff;
+    uint64_t seen = 0;
+    for (uint32_t t = 0; t < m; ++t) {
+      const uint32_t u = order[qoff + t];
+      if (u >= m || ((seen >> u) & 1ull))
+        return fail(c, BMS_EINVAL, "query " + std::to_string(g) + ": the order is not a permutation of its vertices");
+      seen |= 1ull << u;
+      perm[uint64_t(g) * kMaxQueryNodes + t] = uint8_t(u);
+    }
+  }
+  CK(c->given_perm.ensure(perm.size()));
+  CK(cudaMemcpyAsync(c->given_perm.p, perm.data(), perm.size(), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->given_set = true;
+  ++c->given_gen;
+  return BMS_OK;
+}
+
 int bms_set_logging(bms_ctx* c, int vertex_expansions) {
   GUARD(c);
   c->log_vertices = vertex_expansions != 0;
@@ -853,7 +884,7 @@ int bms_join(bms_ctx* c, int mode, int order, int sem, uint64_t* total) {
     CK(launch_set_counter(&c->ctr.as<Counters>()->recs_wide, T, c->st));  // GMCR order mixes sizes
     CK(launch_set_counter(&c->ctr.as<Counters>()->recs_mid, T, c->st));
     r = join_records(c, mode, order, sem,
-                     mode == BMS_COUNT_ALL && order == BMS_ORDER_GMCR && sem == BMS_SEM_EXACT && !cs_active(c),
+                     mode == BMS_COUNT_ALL && order != BMS_ORDER_LEARNED && sem == BMS_SEM_EXACT && !cs_active(c),
                      c->cand.as<uint32_t>());
     if (r) return r;
     CK(cudaMemcpyAsync(c->h_T, c->gmcr_off.as<uint32_t>() + c->d.G, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->st));
@@ -866,7 +897,7 @@ int bms_join(bms_ctx* c, int mode, int order, int sem, uint64_t* total) {
   }
   if (c->h_err[2] & kErrOverflow) return fail(c, BMS_ENOMEM, "join task buffer overflow");
   c->have_results = true;
-  c->have_vexp = mode == BMS_COUNT_ALL && order == BMS_ORDER_GMCR && sem == BMS_SEM_EXACT && !c->last_cs;
+  c->have_vexp = mode == BMS_COUNT_ALL && order != BMS_ORDER_LEARNED && sem == BMS_SEM_EXACT && !c->last_cs;
   c->stats.ms_order = elapsed(c, EV_MAP, EV_ORDER);
   c->stats.ms_join = elapsed(c, EV_ORDER, EV_JOIN);
   c->stats.total_matches = c->h_ctr->total;
@@ -880,7 +911,7 @@ int bms_join(bms_ctx* c, int mode, int order, int sem, uint64_t* total) {
 int bms_run(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* total) {
   GUARD(c);
   try {
-    const bool log = c->log_vertices && mode == BMS_COUNT_ALL && order == BMS_ORDER_GMCR && sem == BMS_SEM_EXACT;
+    const bool log = c->log_vertices && mode == BMS_COUNT_ALL && order != BMS_ORDER_LEARNED && sem == BMS_SEM_EXACT;
     return run_fused(c, R, mode, order, sem, total, log, 0);
   } catch (...) {
     return fail(c, BMS_ENOMEM, "host exception in bms_run");
@@ -1238,6 +1269,7 @@ PlanKey plan_key(const bms_ctx* c, int R, int mode, int order, int sem) {
   k.filter_kernel = c->filter_kernel;
   k.model_set = c->model_set ? 1 : 0;
   k.use_cs = c->use_cs ? 1 : 0;
+  k.given_gen = order == BMS_ORDER_GIVEN ? c->given_gen : 0;
   k.sub_cap_opt = c->sub_cap_opt;
   k.budget = c->budget;
   k.rec_cap = c->rec_cap;
@@ -1368,8 +1400,8 @@ int complete_fused(bms_ctx* c, int R, int mode, int order, int sem, uint64_t* to
   }
   c->d.asymmetric = (c->h_err[0] & kErrAsym) != 0;
   c->q.asymmetric = (c->h_err[1] & kErrAsym) != 0;
-  if (order == BMS_ORDER_LEARNED && (c->d.asymmetric || c->q.asymmetric))
-    return fail(c, BMS_EINVAL, "the learned order requires symmetric adjacency");
+  if (order != BMS_ORDER_GMCR && (c->d.asymmetric || c->q.asymmetric))
+    return fail(c, BMS_EINVAL, "a search order other than the GMCR order requires symmetric adjacency");
   if (c->h_err[2] & kErrOverflow) {
     drop_plan(c);
     if (attempt >= 2) return fail(c, BMS_ENOMEM, "result buffers overflow");

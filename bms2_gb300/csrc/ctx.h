@@ -82,6 +82,7 @@ enum Ev { EV_START, EV_SIG, EV_FILTER, EV_MAP, EV_ORDER, EV_JOIN, EV_END, EV_COU
 struct PlanKey {
   unsigned long long load_gen, epoch;
   int R, mode, order, sem, filter_kernel, model_set, use_cs;
+  unsigned long long given_gen;
   uint64_t sub_cap_opt, budget, rec_cap, row_cap, task_cap, sub_cap, cs_cap;
   bms_schedule sched;
 };
@@ -139,6 +140,10 @@ struct bms_ctx {
   // cost model
   DevBuf model_master, model_bf16, adam_m, adam_v, grad, grad_partial, loss_buf, train_x, train_y, pred;
   bool model_set = false;
+  // BMS_ORDER_GIVEN: per-query orders in the perm layout ([Q][64] bytes)
+  DevBuf given_perm;
+  bool given_set = false;
+  unsigned long long given_gen = 0;
   bool log_vertices = false;
   int filter_kernel = 0;  // BMS_FILTER_SLICED or BMS_FILTER_BALLOT
   uint64_t budget = 0;

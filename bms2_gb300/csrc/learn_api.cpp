@@ -158,7 +158,7 @@ int bms_vertex_expansions(bms_ctx* c, uint64_t* out) {
   GUARD(c);
   if (!out) return fail(c, BMS_EINVAL, "out is null");
   if (!c->have_vexp)
-    return fail(c, BMS_ESTATE, "no vertex log: enable bms_set_logging and run count-all, GMCR order, EXACT");
+    return fail(c, BMS_ESTATE, "no vertex log: enable bms_set_logging and run count-all, GMCR or given order, EXACT");
   if (c->q.N)
     CK(cudaMemcpyAsync(out, c->vertex_exp.p, sizeof(uint64_t) * c->q.N, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));

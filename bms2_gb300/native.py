@@ -20,7 +20,7 @@ STATUS = {0: "BMS_OK", -1: "BMS_EINVAL", -2: "BMS_ENOMEM", -3: "BMS_ECUDA", -4: 
           -6: "BMS_EUNSUPPORTED", -7: "BMS_ETIMEDOUT", -8: "BMS_EINCOMPLETE", -9: "BMS_ENODEV"}
 QUERY, DATA = 0, 1
 FIND_FIRST, COUNT_ALL = 0, 1
-ORDER_GMCR, ORDER_LEARNED = 0, 1
+ORDER_GMCR, ORDER_LEARNED, ORDER_GIVEN = 0, 1, 2
 SEM_EXACT, SEM_REFERENCE_DFS = 0, 1
 SIZE_UNIFORM, SIZE_NORMAL, SIZE_LOGNORMAL = 0, 1, 2
 NUM_FEATURES = 12
@@ -140,6 +140,7 @@ SIGNATURES = [
     ("bms_model_save", C.c_int, [_vp, C.c_char_p]),
     ("bms_model_load", C.c_int, [_vp, C.c_char_p]),
     ("bms_model_predict", C.c_int, [_vp, _f32p, _u8p]),
+    ("bms_set_query_order", C.c_int, [_vp, _u8p, C.c_uint64]),
     ("bms_get_schedule", C.c_int, [_vp, C.POINTER(Schedule)]),
     ("bms_set_schedule", C.c_int, [_vp, C.POINTER(Schedule)]),
     ("bms_autotune", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.POINTER(Schedule)]),
@@ -518,6 +519,12 @@ class Context:
         order = np.zeros(max(n, 1), dtype=np.uint8)
         self._c(lib().bms_model_predict(self._h, _ptr(cost, C.c_float), _ptr(order, C.c_uint8)))
         return cost[:n], order[:n]
+
+    def set_query_order(self, order: np.ndarray) -> None:
+        """Explicit per-query search orders for ORDER_GIVEN (order[qoff + t] =
+        the local vertex searched at depth t)."""
+        o = np.ascontiguousarray(order, dtype=np.uint8)
+        self._c(lib().bms_set_query_order(self._h, _ptr(o, C.c_uint8), len(o)))
 
     def schedule(self) -> dict:
         s = Schedule()

@@ -53,8 +53,9 @@ typedef enum { BMS_QUERY = 0, BMS_DATA = 1 } bms_kind;
  * default of the reference driver); count-all is the driver's --find-all. */
 typedef enum { BMS_FIND_FIRST = 0, BMS_COUNT_ALL = 1 } bms_mode;
 /* search order: GMCR = query-index order 0..n-1, the only order of the
- * reference (isomorphism.hpp:414-448); LEARNED = cost-model order. */
-typedef enum { BMS_ORDER_GMCR = 0, BMS_ORDER_LEARNED = 1 } bms_order;
+ * reference (isomorphism.hpp:414-448); LEARNED = cost-model order; GIVEN =
+ * the orders last set with bms_set_query_order. */
+typedef enum { BMS_ORDER_GMCR = 0, BMS_ORDER_LEARNED = 1, BMS_ORDER_GIVEN = 2 } bms_order;
 /* join semantics.  EXACT counts every injective, induced, label-preserving
  * embedding inside the candidate sets.  REFERENCE_DFS restates the reference
  * DFS literally, including the visited bit it never clears when a frame
@@ -344,6 +345,15 @@ int bms_model_load(bms_ctx* ctx, const char* path);
 /* Predicted log2 expansion cost per query vertex and the resulting per-query
  * order (order[n_query_nodes], local vertex ids, query by query). */
 int bms_model_predict(bms_ctx* ctx, float* cost, uint8_t* order);
+/* Explicit search orders for BMS_ORDER_GIVEN (no reference counterpart; the
+ * reference searches in query-index order only): order[n_query_nodes], query
+ * by query, order[qoff + t] = the local vertex searched at depth t; each
+ * query's slice must be a permutation of 0..n-1.  Kept until the query side is
+ * loaded again.  Like the learned order it only permutes the search (EXACT
+ * semantics; counts are unchanged); the cost model's training logs the
+ * expansions of candidate orders with it (bms_set_logging works for GMCR and
+ * GIVEN orders). */
+int bms_set_query_order(bms_ctx* ctx, const uint8_t* order, uint64_t n_query_nodes);
 
 /* ------------------------------------------------------------ scheduling */
 /* Schedule of the persistent join, one row per size bucket.  Bucket b holds

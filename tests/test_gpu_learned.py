@@ -55,7 +55,7 @@ def trained(ctx):
     q, d = workloads.make("mol100k", 11, n_data=4000, n_queries=80)
     ctx.load(QUERY, q)
     ctx.load(DATA, d)
-    x, y = collect(ctx, 6)
+    x, y = collect(ctx, 6, q.arrays())
     assert len(y) > 100 and np.isfinite(x).all() and np.isfinite(y).all()
     loss = train(ctx, x, y, seed=5, epochs=80)
     return ctx.model_get(), loss, float(np.var(y))
@@ -139,7 +139,7 @@ def test_trained_order_expands_less_than_plain_on_held_out_data():
         qa, da = workloads.make("mol1m", 101, n_data=20000, n_queries=1000)
         c.load(QUERY, qa)
         c.load(DATA, da)
-        x, y = collect(c, 6)
+        x, y = collect(c, 6, qa.arrays())
         train(c, x, y, seed=101)
         qb, db = workloads.make("mol1m", 202, n_data=20000, n_queries=1000)
         c.load(QUERY, qb)
@@ -152,4 +152,30 @@ def test_trained_order_expands_less_than_plain_on_held_out_data():
         assert np.array_equal(c.pair_counts(), plain_counts)
         ratio = plain_exps / learned_exps
         print(f"held-out expansions: plain {plain_exps}, learned {learned_exps}, ratio {ratio:.3f}")
-        assert ratio > 1.04
+        assert ratio > 1.12  # measured 1.215
+
+
+def test_given_orders_keep_counts_and_are_validated(ctx):
+    # explicit per-query orders (the training's candidate orders) change the
+    # search, not a count; malformed orders are rejected
+    from bms2_gb300 import ORDER_GIVEN
+    from bms2_gb300.train import greedy_orders
+
+    q, d = workloads.make("mol1k", 16, n_data=400, n_queries=20)
+    ctx.load(QUERY, q)
+    ctx.load(DATA, d)
+    with pytest.raises(BmsError):
+        ctx.run(2, COUNT_ALL, ORDER_GIVEN, SEM_EXACT)  # no order set for these queries
+    want = oracle.run_pipeline(q, d, 2, keep_steps=False)
+    rng = np.random.default_rng(3)
+    qa = q.arrays()
+    for order in (greedy_orders(qa, rng.normal(size=len(qa["node_labels"]))),
+                  greedy_orders(qa, -np.arange(len(qa["node_labels"]), dtype=np.float64))):
+        ctx.set_query_order(order)
+        assert ctx.run(2, COUNT_ALL, ORDER_GIVEN, SEM_EXACT) == want.total
+        assert np.array_equal(ctx.pair_counts(), want.counts)
+    bad = np.zeros(len(qa["node_labels"]), np.uint8)  # every query's order all zeros
+    with pytest.raises(BmsError):
+        ctx.set_query_order(bad)
+    with pytest.raises(BmsError):
+        ctx.set_query_order(np.zeros(3, np.uint8))

@@ -15,8 +15,8 @@ queries of 5-30 nodes, 30% pure-carbon) is the plain-method GPU configuration.
   python bench.py --impl reference ...   # the CPU restatement of the reference
 
 With the learned order (the default) the cost model is first trained on a
-seed-A workload of the same shape (plain-order expansion logging, GPU
-training); the timed steps run on seed-B inputs, and the plain GMCR order is
+seed-A workload of the same shape (every vertex's root-level search-tree size
+logged by the join, GPU training); the timed steps run on seed-B inputs, and the plain GMCR order is
 timed on the same inputs for the learned-over-plain ratio, with per-pair counts
 compared.
 

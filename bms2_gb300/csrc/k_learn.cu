@@ -2,8 +2,9 @@
 //
 // No reference counterpart (the reference only ever searches in query-index
 // order, isomorphism.hpp:414-448).  The cost model is a 12-64-64-1 ReLU MLP with
-// bfloat16 weights and fp32 accumulation that predicts log2 of the mean number
-// of DFS assignments a query vertex receives per pair under the plain order.
+// bfloat16 weights and fp32 accumulation that predicts a query vertex's
+// root-level search-tree size: log2 of the mean number of DFS assignments it
+// receives per pair when the search starts at it.
 // The order only permutes the search; EXACT counts do not depend on it.
 #include <cuda_bf16.h>
 

@@ -157,8 +157,8 @@ void bms_destroy(bms_ctx* ctx);
 int bms_set_stream(bms_ctx* ctx, void* stream);
 /* Per (pair, root) expansion budget of the join; 0 = unlimited (default). */
 int bms_set_expansion_budget(bms_ctx* ctx, uint64_t budget);
-/* Log per-query-vertex expansions in bms_run (count-all, GMCR order, EXACT
- * semantics only) for bms_vertex_expansions; off by default. */
+/* Log per-query-vertex expansions in bms_run (count-all, GMCR or given order,
+ * EXACT semantics only) for bms_vertex_expansions; off by default. */
 int bms_set_logging(bms_ctx* ctx, int vertex_expansions);
 
 /* Engine options (no reference counterpart). */

@@ -168,7 +168,7 @@ int upload(bms_ctx* c, Side& s, const bms_graphs_view& v, uint32_t limit, const 
   CK(s.adjin.ensure(sizeof(uint64_t) * 2 * (N ? N : 1)));
   CK(s.ghist.ensure(sizeof(uint64_t) * (G ? G : 1)));
   CK(s.glabset.ensure(sizeof(uint32_t) * (G ? G : 1)));
-  CK(s.maxin.ensure(sizeof(uint32_t)));
+  CK(s.maxin.ensure(2 * sizeof(uint32_t)));  // in-degree bound, graph counter of the signatures kernel
   s.loaded = true;
   return BMS_OK;
 }
@@ -216,7 +216,7 @@ int run_signatures(bms_ctx* c, int R) {
       CK(cudaMemcpyAsync(c->errflag.p, c->dres_err.p, sizeof(uint32_t), cudaMemcpyDeviceToDevice, c->st));
       continue;
     }
-    CK(cudaMemsetAsync(s.maxin.p, 0, sizeof(uint32_t), c->st));
+    CK(cudaMemsetAsync(s.maxin.p, 0, 2 * sizeof(uint32_t), c->st));
     CK(launch_signatures(s.dg(), s.ds(), i == 0 ? kMaxDataNodes : kMaxQueryNodes, c->errflag.as<uint32_t>() + i, c->st));
   }
   return BMS_OK;
@@ -1040,7 +1040,7 @@ int bms_run_resident(bms_ctx* c, uint32_t window_graphs, int R, int mode, int or
       Side& r = c->dres;
       CK(c->dres_err.ensure(sizeof(uint32_t)));
       CK(cudaMemsetAsync(c->errflag.p, 0, 4 * sizeof(uint32_t), c->st));
-      CK(cudaMemsetAsync(r.maxin.p, 0, sizeof(uint32_t), c->st));
+      CK(cudaMemsetAsync(r.maxin.p, 0, 2 * sizeof(uint32_t), c->st));
       r.sig_steps = R;
       CK(record_event(c, EV_START));
       CK(launch_signatures(r.dg(), r.ds(), kMaxDataNodes, c->errflag.as<uint32_t>(), c->st));

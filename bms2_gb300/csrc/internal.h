@@ -45,7 +45,8 @@ struct DSigs {
   uint64_t* adjin;      // [N*2]
   uint64_t* ghist;      // [G]   per-graph nibble histogram of labels < 16
   uint32_t* glabset;    // [G]   bit l: some node has label l (< 16)
-  uint32_t* maxin;      // [1]   largest in-degree (distinct in-neighbours) of the side
+  uint32_t* maxin;      // [2]   largest in-degree (distinct in-neighbours) of the side; the signatures
+                        //       kernel's graph counter
   int R;
 };
 

@@ -9,38 +9,52 @@
 // 128-bit set per node, so every walk, path and BFS runs on on-chip bitsets.
 // Semantics are the reference's with bitsets as wide as the graph (no 64-node
 // aliasing, no 128-entry stack cap, cycle signatures for every graph size).
+// The grid is persistent (as many blocks as fit the SMs at once) and warps
+// take graphs from a counter, so graphs of uneven cost leave no tail.
 #include "device_common.cuh"
 
 namespace bms {
 namespace {
 
-constexpr int kWarps = 4;  // ~10.4 KB of shared memory per warp: five blocks fit an SM
-constexpr int kMaxEntries = 512;  // CSR entries staged per graph; larger rows read global memory
+constexpr int kWarps = 4;
+constexpr int kBlocksPerSm = 7;  // 6.4 KB of shared memory per warp: seven 4-warp blocks fit an SM
 
+// Shared memory of one warp.  Two arrays of node sets serve in turn: first the
+// reach sets of the distance shells; then scratch[0] holds the in-sets of an
+// asymmetric graph, or the (s0, a) item offsets of the cycle enumeration, and
+// at last the lanes' path filters, while scratch[1] holds the cycle counters
+// of a canonical graph or the same-label sets of a non-canonical one.
 struct WarpSmem {
-  B128 adj[kMaxDataNodes];      // out-neighbour set of every node (row as a set)
-  B128 in[kMaxDataNodes];       // in-neighbour set
-  B128 same[kMaxDataNodes];     // nodes with the same label
+  B128 adj[kMaxDataNodes];  // out-neighbour set of every node (row as a set)
+  B128 scratch[2][kMaxDataNodes];
+  B128 labmask[16];         // nodes of each label < 16
   uint8_t lab[kMaxDataNodes];
-  uint16_t row[kMaxDataNodes + 1];
-  uint8_t col[kMaxEntries];
-  B128 labmask[16];
-  alignas(16) uint32_t cyc[kMaxDataNodes][4];  // cycle closures per node (canonical enumeration)
-  uint16_t first[kMaxDataNodes + 1];  // canonical enumeration: offsets of the (s0, a) work items
-  alignas(16) uint32_t bloom[32][8];  // per lane: the path filter of its current node, 32-bit words
 };
+static_assert(sizeof(WarpSmem) % 16 == 0, "per-warp areas keep 16-byte alignment");
+static_assert(sizeof(uint16_t) * (kMaxDataNodes + 1) <= sizeof(B128) * kMaxDataNodes, "item offsets fit");
+static_assert(sizeof(uint32_t) * 32 * 8 <= sizeof(B128) * kMaxDataNodes, "32 path filters fit");
+static_assert(sizeof(uint32_t) * 4 * kMaxDataNodes <= sizeof(B128) * kMaxDataNodes, "cycle counters fit");
 
-// CSR row access of the current graph with local ids, from shared memory when
-// the graph fits, else from global memory.
+__device__ __forceinline__ uint16_t* item_first(WarpSmem& s) { return reinterpret_cast<uint16_t*>(s.scratch[0]); }
+__device__ __forceinline__ uint32_t* lane_bloom(WarpSmem& s, uint32_t lane) {
+  return reinterpret_cast<uint32_t*>(s.scratch[0]) + 8 * lane;
+}
+typedef uint32_t CycRow[4];
+__device__ __forceinline__ CycRow* cyc_counts(WarpSmem& s) { return reinterpret_cast<CycRow*>(s.scratch[1]); }
+
+// CSR row access of the current graph with local ids, from global memory (the
+// paths for rows with repeated entries; out-of-graph columns, already flagged
+// as an error of the batch, read node 0).
 struct Rows {
-  const WarpSmem* s;
   const uint32_t* rowp;
   const uint32_t* col;
-  uint32_t start;
-  bool global;
-  __device__ uint32_t begin(uint32_t v) const { return global ? rowp[start + v] : s->row[v]; }
-  __device__ uint32_t end(uint32_t v) const { return global ? rowp[start + v + 1] : s->row[v + 1]; }
-  __device__ uint32_t at(uint32_t i) const { return global ? col[i] - start : s->col[i]; }
+  uint32_t start, m;
+  __device__ uint32_t begin(uint32_t v) const { return rowp[start + v]; }
+  __device__ uint32_t end(uint32_t v) const { return rowp[start + v + 1]; }
+  __device__ uint32_t at(uint32_t i) const {
+    const uint32_t l = col[i] - start;
+    return l < m ? l : 0u;
+  }
 };
 
 // Saturating nibble histogram (signature.hpp:22-53) of the labels < 16 of a
@@ -60,13 +74,13 @@ __device__ __forceinline__ uint64_t label_hist(const WarpSmem& s, uint32_t prese
 // for every u in the row of v, and shell k of v (the nodes first reached after
 // k steps) is reach_k(v) minus reach_{k-1}(v).  Every lane runs one union per
 // neighbour of its nodes per level, so lanes stay in step whatever the BFS
-// frontiers look like.  The reach sets live in s.same and s.cyc, which are
-// filled only after this; once no set grows, the remaining shells are empty.
+// frontiers look like.  The reach sets live in the two scratch arrays; once no
+// set grows, the remaining shells are empty.
 // Writes record words 6..13 (shells 1..8; steps >= R stay zero).
 __device__ void shells_levels(WarpSmem& s, const DSigs& out, uint32_t start, uint32_t m, uint32_t lane,
                               uint32_t present) {
-  B128* cur = s.same;
-  B128* nxt = reinterpret_cast<B128*>(s.cyc);
+  B128* cur = s.scratch[0];
+  B128* nxt = s.scratch[1];
   for (uint32_t v = lane; v < m; v += 32) cur[v] = b_bit(v);
   __syncwarp();
   bool grows = out.R > 0;
@@ -142,9 +156,12 @@ __device__ void cycles_entries(const WarpSmem& s, const Rows& r, uint32_t v, uin
 // cycle's length — exactly what the per-node walk counts (the cycle in both
 // directions), so the halved signature is unchanged.  A cycle is "same" iff
 // all its nodes carry one label (the per-node rule: every node after v on the
-// path has v's label).  Counters in s.cyc; lanes take (s0, first edge) items.
+// path has v's label).  Counters in scratch[1]; lanes take (s0, first edge)
+// items, whose offsets sit in scratch[0].
 __device__ void cycles_canonical(WarpSmem& s, uint32_t m, uint32_t lane) {
   const B128 all = b_lowmask(m);
+  CycRow* cyc = cyc_counts(s);
+  uint16_t* first = item_first(s);
   // work items: (s0, a) with a an upper neighbour of s0, spread over the lanes
   // first[v] = items of the nodes before v: a warp scan per 32 nodes
   uint32_t carry = 0;
@@ -152,7 +169,7 @@ __device__ void cycles_canonical(WarpSmem& s, uint32_t m, uint32_t lane) {
     const uint32_t v = v0 + lane;
     uint32_t n = 0;
     if (v < m) {
-      for (int t = 0; t < 4; ++t) s.cyc[v][t] = 0;
+      for (int t = 0; t < 4; ++t) cyc[v][t] = 0;
       n = b_pop(b_and(s.adj[v], b_andn(all, b_lowmask(v + 1))));
     }
     uint32_t incl = n;
@@ -160,58 +177,69 @@ __device__ void cycles_canonical(WarpSmem& s, uint32_t m, uint32_t lane) {
       const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
       if (lane >= uint32_t(d)) incl += y;
     }
-    if (v < m) s.first[v + 1] = uint16_t(carry + incl);
+    if (v < m) first[v + 1] = uint16_t(carry + incl);
     carry += __shfl_sync(0xffffffffu, incl, 31);
   }
-  if (lane == 0) s.first[0] = 0;
+  if (lane == 0) first[0] = 0;
   __syncwarp();
-  const uint32_t items = s.first[m];
+  const uint32_t items = first[m];
   for (uint32_t k = lane; k < items; k += 32) {
     uint32_t lo = 0, hi = m;  // first[lo] <= k < first[hi]
     while (hi - lo > 1) {
       const uint32_t mid = (lo + hi) >> 1;
-      if (s.first[mid] <= k) lo = mid;
+      if (first[mid] <= k) lo = mid;
       else hi = mid;
     }
     const uint32_t s0 = lo;
     const B128 gt = b_andn(all, b_lowmask(s0 + 1));
     B128 up = b_and(s.adj[s0], gt);
-    for (uint32_t r = k - s.first[s0]; r > 0; --r) up = b_clear_low(up);
+    for (uint32_t r = k - first[s0]; r > 0; --r) up = b_clear_low(up);
     const uint32_t a = b_low(up);
     const uint32_t l0 = s.lab[s0];
     const B128 ns = s.adj[s0];
     const bool s1 = s.lab[a] == l0;
     const B128 v1 = b_bit(a);
-    const B128 above_a = b_andn(gt, b_lowmask(a + 1));  // orientation: last node > a
+    // the cycle's last node is a neighbour of s0 above a (orientation)
+    const B128 last = b_and(ns, b_andn(gt, b_lowmask(a + 1)));
+    if (!b_any(last)) continue;
+    // only paths that can still close are walked: the 4th node closes a
+    // 5-cycle (it is in last) or precedes the last node of a 6-cycle (it is
+    // next to last), and the 3rd node is next to such a 4th node
+    B128 q4 = last;
+    for (B128 r = last; b_any(r); r = b_clear_low(r)) q4 = b_or(q4, s.adj[b_low(r)]);
+    q4 = b_and(q4, gt);
+    B128 q3{0, 0};
+    for (B128 r = q4; b_any(r); r = b_clear_low(r)) q3 = b_or(q3, s.adj[b_low(r)]);
+    q3 = b_and(q3, gt);
     for (B128 r2 = b_andn(b_and(s.adj[a], gt), v1); b_any(r2); r2 = b_clear_low(r2)) {
       const uint32_t b = b_low(r2);
       const bool s2 = s1 && s.lab[b] == l0;
       const B128 v2 = b_or(v1, b_bit(b));
-      for (B128 r3 = b_andn(b_and(s.adj[b], gt), v2); b_any(r3); r3 = b_clear_low(r3)) {
+      for (B128 r3 = b_andn(b_and(s.adj[b], q3), v2); b_any(r3); r3 = b_clear_low(r3)) {
         const uint32_t c = b_low(r3);
         const bool s3 = s2 && s.lab[c] == l0;
         const B128 v3 = b_or(v2, b_bit(c));
-        for (B128 r4 = b_andn(b_and(s.adj[c], gt), v3); b_any(r4); r4 = b_clear_low(r4)) {
+        for (B128 r4 = b_andn(b_and(s.adj[c], q4), v3); b_any(r4); r4 = b_clear_low(r4)) {
           const uint32_t d = b_low(r4);
           const bool s4 = s3 && s.lab[d] == l0;
-          if (b_has(ns, d) && d > a) {
+          if (b_has(last, d)) {
             const int t = s4 ? 0 : 1;
-            atomicAdd(&s.cyc[s0][t], 2u);
-            atomicAdd(&s.cyc[a][t], 2u);
-            atomicAdd(&s.cyc[b][t], 2u);
-            atomicAdd(&s.cyc[c][t], 2u);
-            atomicAdd(&s.cyc[d][t], 2u);
+            atomicAdd(&cyc[s0][t], 2u);
+            atomicAdd(&cyc[a][t], 2u);
+            atomicAdd(&cyc[b][t], 2u);
+            atomicAdd(&cyc[c][t], 2u);
+            atomicAdd(&cyc[d][t], 2u);
           }
           const B128 v4 = b_or(v3, b_bit(d));
-          for (B128 r5 = b_and(b_andn(b_and(s.adj[d], above_a), v4), ns); b_any(r5); r5 = b_clear_low(r5)) {
+          for (B128 r5 = b_andn(b_and(s.adj[d], last), v4); b_any(r5); r5 = b_clear_low(r5)) {
             const uint32_t e = b_low(r5);
             const int t = (s4 && s.lab[e] == l0) ? 2 : 3;
-            atomicAdd(&s.cyc[s0][t], 2u);
-            atomicAdd(&s.cyc[a][t], 2u);
-            atomicAdd(&s.cyc[b][t], 2u);
-            atomicAdd(&s.cyc[c][t], 2u);
-            atomicAdd(&s.cyc[d][t], 2u);
-            atomicAdd(&s.cyc[e][t], 2u);
+            atomicAdd(&cyc[s0][t], 2u);
+            atomicAdd(&cyc[a][t], 2u);
+            atomicAdd(&cyc[b][t], 2u);
+            atomicAdd(&cyc[c][t], 2u);
+            atomicAdd(&cyc[d][t], 2u);
+            atomicAdd(&cyc[e][t], 2u);
           }
         }
       }
@@ -223,10 +251,8 @@ __device__ void cycles_canonical(WarpSmem& s, uint32_t m, uint32_t lane) {
 // Cycle closures through v on adjacency sets (graphs without repeated entries).
 // At depth 5 the closing nodes are counted in one step: they are the unvisited
 // out-neighbours of the depth-4 node whose rows contain v.
-__device__ void cycles_sets(const WarpSmem& s, uint32_t v, uint32_t c[4]) {
+__device__ void cycles_sets(const WarpSmem& s, B128 inv, B128 eq, uint32_t v, uint32_t c[4]) {
   const uint32_t lv = s.lab[v];
-  const B128 inv = s.in[v];
-  const B128 eq = s.same[v];
   for (B128 r1 = s.adj[v]; b_any(r1); r1 = b_clear_low(r1)) {
     const uint32_t a = b_low(r1);
     const bool s1 = s.lab[a] == lv;
@@ -254,81 +280,92 @@ __device__ void cycles_sets(const WarpSmem& s, uint32_t v, uint32_t c[4]) {
   }
 }
 
-__global__ void __launch_bounds__(kWarps * 32) signatures_kernel(DGraphs g, DSigs out, uint32_t max_nodes,
-                                                                uint32_t* err) {
-  __shared__ WarpSmem smem[kWarps];
-  const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
-  WarpSmem& s = smem[warp];
-  for (uint32_t gi = blockIdx.x * kWarps + warp; gi < g.G; gi += gridDim.x * kWarps) {
-    const uint32_t start = g.goff[gi];
-    const uint32_t m = g.goff[gi + 1] - start;
-    if (m > max_nodes) {
-      if (lane == 0) atomicOr(err, kErrTooLarge);
-      continue;
-    }
-    // row offsets of this graph must be non-decreasing and inside [0, E]
-    bool rows_ok = true;
-    for (uint32_t v = lane; v <= m; v += 32) {
-      const uint64_t r = g.rowp[start + v];
-      rows_ok = rows_ok && r <= g.E && (v == 0 || g.rowp[start + v - 1] <= r);
-    }
-    if (!__all_sync(0xffffffffu, rows_ok)) {
-      if (lane == 0) atomicOr(err, kErrRows);
-      continue;
-    }
-    const uint32_t e0 = g.rowp[start];
-    const uint32_t entries = g.rowp[start + m] - e0;
-    const bool global_rows = entries > uint32_t(kMaxEntries);
-    // stage labels, rows, entries; build adjacency sets
-    uint32_t bad = 0;
-    bool multi = false;
-    for (uint32_t v = lane; v < m; v += 32) {
-      s.lab[v] = g.lab[start + v];
-      const uint32_t rb = g.rowp[start + v], re = g.rowp[start + v + 1];
-      if (!global_rows) {
-        s.row[v] = uint16_t(rb - e0);
-        if (v == m - 1) s.row[m] = uint16_t(re - e0);
+// One graph on one warp: its rows staged as node sets, the symmetry check and
+// label masks, then the shells, the canonical cycle enumeration and the
+// per-node label, path and cycle signatures.
+__device__ __forceinline__ void signatures_graph(const DGraphs& g, const DSigs& out, uint32_t max_nodes,
+                                                 uint32_t* err, WarpSmem& s, uint32_t gi, uint32_t lane) {
+  const uint32_t start = g.goff[gi];
+  const uint32_t m = g.goff[gi + 1] - start;
+  if (m > max_nodes) {
+    if (lane == 0) atomicOr(err, kErrTooLarge);
+    return;
+  }
+  // row offsets of this graph must be non-decreasing and inside [0, E]
+  bool rows_ok = true;
+  for (uint32_t v = lane; v <= m; v += 32) {
+    const uint64_t r = g.rowp[start + v];
+    rows_ok = rows_ok && r <= g.E && (v == 0 || g.rowp[start + v - 1] <= r);
+  }
+  if (!__all_sync(0xffffffffu, rows_ok)) {
+    if (lane == 0) atomicOr(err, kErrRows);
+    return;
+  }
+  // stage labels; rows as adjacency sets
+  uint32_t bad = 0;
+  bool multi = false;
+  if (lane < 16) s.labmask[lane] = B128{0, 0};
+  for (uint32_t v = lane; v < m; v += 32) {
+    s.lab[v] = g.lab[start + v];
+    const uint32_t rb = g.rowp[start + v], re = g.rowp[start + v + 1];
+    B128 a{0, 0};
+    for (uint32_t i = rb; i < re; ++i) {
+      const uint32_t c = g.col[i];
+      uint32_t lc = c - start;
+      if (c < start || lc >= m) {
+        bad |= kErrColumn;
+        lc = 0;  // keep the entry inside the graph; the batch is rejected
       }
-      B128 a{0, 0};
-      for (uint32_t i = rb; i < re; ++i) {
-        const uint32_t c = g.col[i];
-        uint32_t lc = c - start;
-        if (c < start || lc >= m) {
-          bad |= kErrColumn;
-          lc = 0;  // keep the entry inside the graph; the batch is rejected
-        }
-        if (!global_rows) s.col[i - e0] = uint8_t(lc);
-        if (b_has(a, lc)) multi = true;
-        a = b_or(a, b_bit(lc));
-      }
-      s.adj[v] = a;
-      s.in[v] = B128{0, 0};
+      if (b_has(a, lc)) multi = true;
+      a = b_or(a, b_bit(lc));
     }
-    if (lane < 16) s.labmask[lane] = B128{0, 0};
-    multi = __any_sync(0xffffffffu, multi);
-    bad = __reduce_or_sync(0xffffffffu, bad);
+    s.adj[v] = a;
+  }
+  multi = __any_sync(0xffffffffu, multi);
+  __syncwarp();
+  // label masks: one 32-node word per label and chunk of nodes, stored by the
+  // chunk's first lane with that label
+  for (uint32_t v0 = 0; v0 < m; v0 += 32) {
+    const uint32_t v = v0 + lane;
+    const uint32_t l = v < m ? uint32_t(s.lab[v]) : 0xFFFFFFFFu;
+    const uint32_t peers = __match_any_sync(0xffffffffu, l);
+    if (l < 16 && lane == uint32_t(__ffs(int(peers)) - 1))
+      reinterpret_cast<uint32_t*>(&s.labmask[l])[v0 >> 5] = peers;
+  }
+  // symmetry as sets (w in the row of v implies v in the row of w), read off
+  // the staged rows; the in-sets of a symmetric graph are its rows
+  bool sym = true;
+  uint32_t max_in = 0;
+  for (uint32_t v = lane; v < m; v += 32) {
+    const B128 a = s.adj[v];
+    for (B128 r = a; b_any(r); r = b_clear_low(r)) sym = sym && b_has(s.adj[b_low(r)], v);
+    max_in = max(max_in, b_pop(a));
+  }
+  const bool asym = !__all_sync(0xffffffffu, sym);
+  __syncwarp();
+  // labels < 16 present in the graph: label histograms are popcounts of their masks
+  const uint32_t present = __ballot_sync(0xffffffffu, lane < 16 && b_any(s.labmask[lane]));
+  shells_levels(s, out, start, m, lane, present);
+  if (asym) {
+    // in-sets by scattering every row, written out here: scratch[0] serves
+    // the path filters below; the same-label sets go to scratch[1]
+    B128* ins = s.scratch[0];
+    for (uint32_t v = lane; v < m; v += 32) ins[v] = B128{0, 0};
     __syncwarp();
-    // in-neighbour sets, label masks
     for (uint32_t v = lane; v < m; v += 32) {
+      const B128 bv = b_bit(v);
       for (B128 r = s.adj[v]; b_any(r); r = b_clear_low(r)) {
         const uint32_t w = b_low(r);
-        const B128 bv = b_bit(v);
-        atomicOr(reinterpret_cast<unsigned long long*>(&s.in[w].lo), (unsigned long long)bv.lo);
-        atomicOr(reinterpret_cast<unsigned long long*>(&s.in[w].hi), (unsigned long long)bv.hi);
-      }
-      const uint32_t l = s.lab[v];
-      if (l < 16) {
-        const B128 bv = b_bit(v);
-        atomicOr(reinterpret_cast<unsigned long long*>(&s.labmask[l].lo), (unsigned long long)bv.lo);
-        atomicOr(reinterpret_cast<unsigned long long*>(&s.labmask[l].hi), (unsigned long long)bv.hi);
+        atomicOr(reinterpret_cast<unsigned long long*>(&ins[w].lo), (unsigned long long)bv.lo);
+        atomicOr(reinterpret_cast<unsigned long long*>(&ins[w].hi), (unsigned long long)bv.hi);
       }
     }
     __syncwarp();
-    // labels < 16 present in the graph: label histograms are popcounts of their masks
-    const uint32_t present = __ballot_sync(0xffffffffu, lane < 16 && b_any(s.labmask[lane]));
-    shells_levels(s, out, start, m, lane, present);
-    uint32_t max_in = 0;
+    max_in = 0;
     for (uint32_t v = lane; v < m; v += 32) {
+      const B128 i = ins[v];
+      max_in = max(max_in, b_pop(i));
+      st_b128(out.adjin + 2 * (uint64_t(start) + v), i);
       const uint8_t l = s.lab[v];
       B128 eq{0, 0};
       if (l < 16) {
@@ -337,107 +374,124 @@ __global__ void __launch_bounds__(kWarps * 32) signatures_kernel(DGraphs g, DSig
         for (uint32_t y = 0; y < m; ++y)
           if (s.lab[y] == l) eq = b_or(eq, b_bit(y));
       }
-      s.same[v] = eq;
-      // symmetry as sets: out-set equals in-set
-      const B128 o = s.adj[v], i = s.in[v];
-      if (o.lo != i.lo || o.hi != i.hi) bad |= kErrAsym;
-      max_in = max(max_in, b_pop(i));
+      s.scratch[1][v] = eq;
     }
-    max_in = __reduce_max_sync(0xffffffffu, max_in);
-    if (lane == 0 && max_in) atomicMax(out.maxin, max_in);
-    bad = __reduce_or_sync(0xffffffffu, bad);
-    if (bad && lane == 0) atomicOr(err, bad);
-    __syncwarp();
-    const Rows rows{&s, g.rowp, g.col, start, global_rows};
-    // symmetric graphs without repeated entries: every cycle found once
-    const bool canonical = !multi && !(bad & kErrAsym);
-    if (canonical) cycles_canonical(s, m, lane);
-    for (uint32_t v = lane; v < m; v += 32) {
-      const uint64_t u = uint64_t(start) + v;
-      const uint32_t lu = s.lab[v];
-      // label signature: +1 per CSR entry on the neighbour's label
-      uint64_t lg = 0;
-      if (multi) {
-        for (uint32_t i = rows.begin(v); i < rows.end(v); ++i) nib_inc(lg, s.lab[rows.at(i)]);
-      } else {  // every entry distinct: the row as a set
-        lg = label_hist(s, present, s.adj[v]);
-      }
-      // path signature: walks v-a-w (w != v) and v-a-w-x (x != a, x != v), as
-      // one flat loop with one Bloom insert per iteration, so lanes whose nodes
-      // have different neighbourhoods still hash in step (inserts commute)
-      // the filter's bits accumulate in the lane's own shared words (one OR per
-      // position, PathSignatureDevice::insert, signature.hpp:418-430)
-      uint32_t* bl = s.bloom[lane];
-      reinterpret_cast<uint4*>(bl)[0] = make_uint4(0, 0, 0, 0);
-      reinterpret_cast<uint4*>(bl)[1] = make_uint4(0, 0, 0, 0);
-      {
-        const B128 bv = b_bit(v);
-        B128 ra = s.adj[v], rw{0, 0}, rx{0, 0};
-        uint32_t a = 0, h2 = 0;
-        while (true) {
-          uint32_t h;
-          if (b_any(rx)) {  // next x of the current v-a-w; the hash depends on x's
-            // label only, so every other x of that label is dropped with it
-            const uint32_t lx = s.lab[b_low(rx)];
-            h = hcombine(h2, lx);
-            rx = lx < 16 ? b_andn(rx, s.labmask[lx]) : b_clear_low(rx);
-          } else {  // next w, moving on to the next a with a continuation
-            while (!b_any(rw) && b_any(ra)) {
-              a = b_low(ra);
-              ra = b_clear_low(ra);
-              rw = b_andn(s.adj[a], bv);
-            }
-            if (!b_any(rw)) break;
-            const uint32_t w = b_low(rw);
-            rw = b_clear_low(rw);
-            h2 = hcombine(lu, hcombine(s.lab[a], s.lab[w]));
-            h = h2;
-            rx = b_andn(s.adj[w], b_or(b_bit(a), bv));
+    bad |= kErrAsym;
+  }
+  max_in = __reduce_max_sync(0xffffffffu, max_in);
+  if (lane == 0 && max_in) atomicMax(out.maxin, max_in);
+  bad = __reduce_or_sync(0xffffffffu, bad);
+  if (bad && lane == 0) atomicOr(err, bad);
+  __syncwarp();
+  const Rows rows{g.rowp, g.col, start, m};
+  // symmetric graphs without repeated entries: every cycle found once
+  const bool canonical = !multi && !asym;
+  if (canonical) cycles_canonical(s, m, lane);
+  const CycRow* cyc = cyc_counts(s);
+  for (uint32_t v = lane; v < m; v += 32) {
+    const uint64_t u = uint64_t(start) + v;
+    const uint32_t lu = s.lab[v];
+    const uint32_t rb = rows.begin(v), re = rows.end(v);
+    // label signature: +1 per CSR entry on the neighbour's label
+    uint64_t lg = 0;
+    if (multi) {
+      for (uint32_t i = rb; i < re; ++i) nib_inc(lg, s.lab[rows.at(i)]);
+    } else {  // every entry distinct: the row as a set
+      lg = label_hist(s, present, s.adj[v]);
+    }
+    // path signature: walks v-a-w (w != v) and v-a-w-x (x != a, x != v), as
+    // one flat loop with one Bloom insert per iteration, so lanes whose nodes
+    // have different neighbourhoods still hash in step (inserts commute)
+    // the filter's bits accumulate in the lane's own shared words (one OR per
+    // position, PathSignatureDevice::insert, signature.hpp:418-430)
+    uint32_t* bl = lane_bloom(s, lane);
+    reinterpret_cast<uint4*>(bl)[0] = make_uint4(0, 0, 0, 0);
+    reinterpret_cast<uint4*>(bl)[1] = make_uint4(0, 0, 0, 0);
+    {
+      const B128 bv = b_bit(v);
+      B128 ra = s.adj[v], rw{0, 0}, rx{0, 0};
+      uint32_t a = 0, h2 = 0;
+      while (true) {
+        uint32_t h;
+        if (b_any(rx)) {  // next x of the current v-a-w; the hash depends on x's
+          // label only, so every other x of that label is dropped with it
+          const uint32_t lx = s.lab[b_low(rx)];
+          h = hcombine(h2, lx);
+          rx = lx < 16 ? b_andn(rx, s.labmask[lx]) : b_clear_low(rx);
+        } else {  // next w, moving on to the next a with a continuation
+          while (!b_any(rw) && b_any(ra)) {
+            a = b_low(ra);
+            ra = b_clear_low(ra);
+            rw = b_andn(s.adj[a], bv);
           }
-          uint32_t x = fmix32(h);
+          if (!b_any(rw)) break;
+          const uint32_t w = b_low(rw);
+          rw = b_clear_low(rw);
+          h2 = hcombine(lu, hcombine(s.lab[a], s.lab[w]));
+          h = h2;
+          rx = b_andn(s.adj[w], b_or(b_bit(a), bv));
+        }
+        uint32_t x = fmix32(h);
 #pragma unroll
-          for (int r = 0; r < 3; ++r) {
-            const uint32_t idx = x & 255u;
-            atomicOr(&bl[idx >> 5], 1u << (idx & 31u));
-            x = fmix32(x);
-          }
+        for (int r = 0; r < 3; ++r) {
+          const uint32_t idx = x & 255u;
+          atomicOr(&bl[idx >> 5], 1u << (idx & 31u));
+          x = fmix32(x);
         }
       }
-      const uint4 bq0 = reinterpret_cast<const uint4*>(bl)[0], bq1 = reinterpret_cast<const uint4*>(bl)[1];
-      const uint64_t p0 = uint64_t(bq0.x) | (uint64_t(bq0.y) << 32), p1 = uint64_t(bq0.z) | (uint64_t(bq0.w) << 32);
-      const uint64_t p2 = uint64_t(bq1.x) | (uint64_t(bq1.y) << 32), p3 = uint64_t(bq1.z) | (uint64_t(bq1.w) << 32);
-      // cycle signature
-      uint32_t c[4] = {0, 0, 0, 0};
-      if (canonical) {
-        for (int t = 0; t < 4; ++t) c[t] = s.cyc[v][t];
-      } else if (multi) {
-        cycles_entries(s, rows, v, c);
-      } else {
-        cycles_sets(s, v, c);
-      }
-      const uint64_t cyc = uint64_t((c[0] & 0xFFFFu) >> 1) | (uint64_t((c[1] & 0xFFFFu) >> 1) << 16) |
-                           (uint64_t((c[2] & 0xFFFFu) >> 1) << 32) | (uint64_t((c[3] & 0xFFFFu) >> 1) << 48);
-      // record words 6..13 (distance shells) were written by shells_levels
-      const uint32_t deg = rows.end(v) - rows.begin(v);
-      ulonglong2* rec = reinterpret_cast<ulonglong2*>(out.frec + uint64_t(kRecWords) * u);
-      rec[0] = make_ulonglong2(uint64_t(lu) | (uint64_t(deg) << 32), cyc);
-      rec[1] = make_ulonglong2(p0, p1);
-      rec[2] = make_ulonglong2(p2, p3);
-      rec[7] = make_ulonglong2(lg, 0ull);
-      st_b128(out.adj + 2 * u, s.adj[v]);
-      st_b128(out.adjin + 2 * u, s.in[v]);
     }
-    // per-graph label histogram (labels < 16) and label set
-    uint32_t cnt = 0;
-    if (lane < 16) cnt = b_pop(s.labmask[lane]);
-    const uint32_t nib = lane < 16 ? (cnt > 15 ? 15u : cnt) : 0u;
-    const uint32_t lo = __reduce_or_sync(0xffffffffu, lane < 8 ? nib << (4 * lane) : 0u);
-    const uint32_t hi = __reduce_or_sync(0xffffffffu, (lane >= 8 && lane < 16) ? nib << (4 * (lane - 8)) : 0u);
-    if (lane == 0) {
-      out.ghist[gi] = uint64_t(lo) | (uint64_t(hi) << 32);
-      out.glabset[gi] = present & 0xFFFFu;
+    const uint4 bq0 = reinterpret_cast<const uint4*>(bl)[0], bq1 = reinterpret_cast<const uint4*>(bl)[1];
+    const uint64_t p0 = uint64_t(bq0.x) | (uint64_t(bq0.y) << 32), p1 = uint64_t(bq0.z) | (uint64_t(bq0.w) << 32);
+    const uint64_t p2 = uint64_t(bq1.x) | (uint64_t(bq1.y) << 32), p3 = uint64_t(bq1.z) | (uint64_t(bq1.w) << 32);
+    // cycle signature
+    uint32_t c[4] = {0, 0, 0, 0};
+    if (canonical) {
+      for (int t = 0; t < 4; ++t) c[t] = cyc[v][t];
+    } else if (multi) {
+      cycles_entries(s, rows, v, c);
+    } else {
+      cycles_sets(s, ld_b128(out.adjin + 2 * u), s.scratch[1][v], v, c);
     }
-    __syncwarp();
+    const uint64_t cy = uint64_t((c[0] & 0xFFFFu) >> 1) | (uint64_t((c[1] & 0xFFFFu) >> 1) << 16) |
+                        (uint64_t((c[2] & 0xFFFFu) >> 1) << 32) | (uint64_t((c[3] & 0xFFFFu) >> 1) << 48);
+    // record words 6..13 (distance shells) were written by shells_levels
+    const uint32_t deg = re - rb;
+    ulonglong2* rec = reinterpret_cast<ulonglong2*>(out.frec + uint64_t(kRecWords) * u);
+    rec[0] = make_ulonglong2(uint64_t(lu) | (uint64_t(deg) << 32), cy);
+    rec[1] = make_ulonglong2(p0, p1);
+    rec[2] = make_ulonglong2(p2, p3);
+    rec[7] = make_ulonglong2(lg, 0ull);
+    st_b128(out.adj + 2 * u, s.adj[v]);
+    if (!asym) st_b128(out.adjin + 2 * u, s.adj[v]);
+  }
+  __syncwarp();
+  // per-graph label histogram (labels < 16) and label set
+  uint32_t cnt = 0;
+  if (lane < 16) cnt = b_pop(s.labmask[lane]);
+  const uint32_t nib = lane < 16 ? (cnt > 15 ? 15u : cnt) : 0u;
+  const uint32_t lo = __reduce_or_sync(0xffffffffu, lane < 8 ? nib << (4 * lane) : 0u);
+  const uint32_t hi = __reduce_or_sync(0xffffffffu, (lane >= 8 && lane < 16) ? nib << (4 * (lane - 8)) : 0u);
+  if (lane == 0) {
+    out.ghist[gi] = uint64_t(lo) | (uint64_t(hi) << 32);
+    out.glabset[gi] = present & 0xFFFFu;
+  }
+  __syncwarp();
+}
+
+// Graphs are taken one at a time from out.maxin[1] (zero before the launch);
+// the next graph is claimed while the current one runs.
+__global__ void __launch_bounds__(kWarps * 32, kBlocksPerSm) signatures_kernel(DGraphs g, DSigs out,
+                                                                              uint32_t max_nodes, uint32_t* err) {
+  __shared__ WarpSmem smem[kWarps];
+  const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
+  uint32_t* head = out.maxin + 1;
+  uint32_t gi = lane == 0 ? atomicAdd(head, 1u) : 0u;
+  gi = __shfl_sync(0xffffffffu, gi, 0);
+  while (gi < g.G) {
+    uint32_t next = 0;
+    if (lane == 0) next = atomicAdd(head, 1u);
+    signatures_graph(g, out, max_nodes, err, smem[warp], gi, lane);
+    gi = __shfl_sync(0xffffffffu, next, 0);
   }
 }
 
@@ -445,11 +499,13 @@ __global__ void __launch_bounds__(kWarps * 32) signatures_kernel(DGraphs g, DSig
 
 cudaError_t launch_signatures(const DGraphs& g, DSigs s, uint32_t max_nodes, uint32_t* err, cudaStream_t st) {
   if (g.G == 0) return cudaSuccess;
-  int dev = 0, sms = 0;
+  int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  uint64_t want = (uint64_t(g.G) + kWarps - 1) / kWarps;
-  uint64_t cap = uint64_t(sms > 0 ? sms : 152) * 16;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, signatures_kernel, kWarps * 32, 0);
+  if (e != cudaSuccess) return e;
+  const uint64_t want = (uint64_t(g.G) + kWarps - 1) / kWarps;
+  const uint64_t cap = uint64_t(sms > 0 ? sms : 152) * uint64_t(per_sm > 0 ? per_sm : 1);
   const unsigned blocks = unsigned(want < cap ? want : cap);
   signatures_kernel<<<blocks, kWarps * 32, 0, st>>>(g, s, max_nodes, err); note_launch();
   return cudaGetLastError();

@@ -94,8 +94,10 @@ __device__ void shells_levels(WarpSmem& s, const DSigs& out, uint32_t start, uin
         for (B128 a = s.adj[v]; b_any(a); a = b_clear_low(a)) r = b_or(r, cur[b_low(a)]);
         nxt[v] = r;
         const B128 shell = b_andn(r, prev);
-        grew = grew || b_any(shell);
-        h = label_hist(s, present, shell);
+        if (b_any(shell)) {
+          grew = true;
+          h = label_hist(s, present, shell);
+        }
       }
       out.frec[uint64_t(kRecWords) * (uint64_t(start) + v) + 6 + k] = h;
     }
@@ -108,14 +110,14 @@ __device__ void shells_levels(WarpSmem& s, const DSigs& out, uint32_t start, uin
   __syncwarp();
 }
 
-__device__ uint32_t mult(const Rows& r, uint32_t a, uint32_t target) {
+__device__ __noinline__ uint32_t mult(const Rows& r, uint32_t a, uint32_t target) {
   uint32_t k = 0;
   for (uint32_t i = r.begin(a); i < r.end(a); ++i) k += r.at(i) == target;
   return k;
 }
 
 // Cycle closures through v following CSR entries (multi-edge graphs).
-__device__ void cycles_entries(const WarpSmem& s, const Rows& r, uint32_t v, uint32_t c[4]) {
+__device__ __noinline__ void cycles_entries(const WarpSmem& s, const Rows& r, uint32_t v, uint32_t c[4]) {
   const uint32_t lv = s.lab[v];
   for (uint32_t i1 = r.begin(v); i1 < r.end(v); ++i1) {
     const uint32_t a = r.at(i1);
@@ -251,7 +253,7 @@ __device__ void cycles_canonical(WarpSmem& s, uint32_t m, uint32_t lane) {
 // Cycle closures through v on adjacency sets (graphs without repeated entries).
 // At depth 5 the closing nodes are counted in one step: they are the unvisited
 // out-neighbours of the depth-4 node whose rows contain v.
-__device__ void cycles_sets(const WarpSmem& s, B128 inv, B128 eq, uint32_t v, uint32_t c[4]) {
+__device__ __noinline__ void cycles_sets(const WarpSmem& s, B128 inv, B128 eq, uint32_t v, uint32_t c[4]) {
   const uint32_t lv = s.lab[v];
   for (B128 r1 = s.adj[v]; b_any(r1); r1 = b_clear_low(r1)) {
     const uint32_t a = b_low(r1);
@@ -280,6 +282,41 @@ __device__ void cycles_sets(const WarpSmem& s, B128 inv, B128 eq, uint32_t v, ui
   }
 }
 
+// In-sets of an asymmetric graph, by scattering every row, written out here
+// (scratch[0] serves the path filters later), and the same-label sets in
+// scratch[1] for the set-based cycle count.  Returns the lane's largest
+// in-degree.  Out of line: asymmetric graphs are rare.
+__device__ __noinline__ uint32_t asym_sets(WarpSmem& s, const DSigs& out, uint32_t start, uint32_t m, uint32_t lane) {
+  B128* ins = s.scratch[0];
+  for (uint32_t v = lane; v < m; v += 32) ins[v] = B128{0, 0};
+  __syncwarp();
+  for (uint32_t v = lane; v < m; v += 32) {
+    const B128 bv = b_bit(v);
+    for (B128 r = s.adj[v]; b_any(r); r = b_clear_low(r)) {
+      const uint32_t w = b_low(r);
+      atomicOr(reinterpret_cast<unsigned long long*>(&ins[w].lo), (unsigned long long)bv.lo);
+      atomicOr(reinterpret_cast<unsigned long long*>(&ins[w].hi), (unsigned long long)bv.hi);
+    }
+  }
+  __syncwarp();
+  uint32_t max_in = 0;
+  for (uint32_t v = lane; v < m; v += 32) {
+    const B128 i = ins[v];
+    max_in = max(max_in, b_pop(i));
+    st_b128(out.adjin + 2 * (uint64_t(start) + v), i);
+    const uint8_t l = s.lab[v];
+    B128 eq{0, 0};
+    if (l < 16) {
+      eq = s.labmask[l];
+    } else {
+      for (uint32_t y = 0; y < m; ++y)
+        if (s.lab[y] == l) eq = b_or(eq, b_bit(y));
+    }
+    s.scratch[1][v] = eq;
+  }
+  return max_in;
+}
+
 // One graph on one warp: its rows staged as node sets, the symmetry check and
 // label masks, then the shells, the canonical cycle enumeration and the
 // per-node label, path and cycle signatures.
@@ -291,35 +328,43 @@ __device__ __forceinline__ void signatures_graph(const DGraphs& g, const DSigs& 
     if (lane == 0) atomicOr(err, kErrTooLarge);
     return;
   }
-  // row offsets of this graph must be non-decreasing and inside [0, E]
-  bool rows_ok = true;
-  for (uint32_t v = lane; v <= m; v += 32) {
-    const uint64_t r = g.rowp[start + v];
-    rows_ok = rows_ok && r <= g.E && (v == 0 || g.rowp[start + v - 1] <= r);
-  }
-  if (!__all_sync(0xffffffffu, rows_ok)) {
-    if (lane == 0) atomicOr(err, kErrRows);
-    return;
-  }
-  // stage labels; rows as adjacency sets
+  // stage labels; rows as adjacency sets.  Row offsets must be non-decreasing
+  // and inside [0, E]; a lane reads a row's entries only once its two offsets
+  // passed, four entries per round of loads.
   uint32_t bad = 0;
-  bool multi = false;
+  bool multi = false, rows_ok = true;
   if (lane < 16) s.labmask[lane] = B128{0, 0};
+  if (m == 0 && lane == 0) rows_ok = g.rowp[start] <= g.E;
   for (uint32_t v = lane; v < m; v += 32) {
     s.lab[v] = g.lab[start + v];
     const uint32_t rb = g.rowp[start + v], re = g.rowp[start + v + 1];
     B128 a{0, 0};
-    for (uint32_t i = rb; i < re; ++i) {
-      const uint32_t c = g.col[i];
-      uint32_t lc = c - start;
-      if (c < start || lc >= m) {
-        bad |= kErrColumn;
-        lc = 0;  // keep the entry inside the graph; the batch is rejected
+    if (rb <= re && re <= g.E) {
+      for (uint32_t i = rb; i < re; i += 4) {
+        uint32_t cc[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) cc[j] = i + j < re ? g.col[i + j] : start;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          if (i + j >= re) break;
+          uint32_t lc = cc[j] - start;
+          if (cc[j] < start || lc >= m) {
+            bad |= kErrColumn;
+            lc = 0;  // keep the entry inside the graph; the batch is rejected
+          }
+          if (b_has(a, lc)) multi = true;
+          a = b_or(a, b_bit(lc));
+        }
       }
-      if (b_has(a, lc)) multi = true;
-      a = b_or(a, b_bit(lc));
+    } else {
+      rows_ok = false;
     }
     s.adj[v] = a;
+  }
+  if (!__all_sync(0xffffffffu, rows_ok)) {
+    if (lane == 0) atomicOr(err, kErrRows);
+    __syncwarp();
+    return;
   }
   multi = __any_sync(0xffffffffu, multi);
   __syncwarp();
@@ -347,35 +392,7 @@ __device__ __forceinline__ void signatures_graph(const DGraphs& g, const DSigs& 
   const uint32_t present = __ballot_sync(0xffffffffu, lane < 16 && b_any(s.labmask[lane]));
   shells_levels(s, out, start, m, lane, present);
   if (asym) {
-    // in-sets by scattering every row, written out here: scratch[0] serves
-    // the path filters below; the same-label sets go to scratch[1]
-    B128* ins = s.scratch[0];
-    for (uint32_t v = lane; v < m; v += 32) ins[v] = B128{0, 0};
-    __syncwarp();
-    for (uint32_t v = lane; v < m; v += 32) {
-      const B128 bv = b_bit(v);
-      for (B128 r = s.adj[v]; b_any(r); r = b_clear_low(r)) {
-        const uint32_t w = b_low(r);
-        atomicOr(reinterpret_cast<unsigned long long*>(&ins[w].lo), (unsigned long long)bv.lo);
-        atomicOr(reinterpret_cast<unsigned long long*>(&ins[w].hi), (unsigned long long)bv.hi);
-      }
-    }
-    __syncwarp();
-    max_in = 0;
-    for (uint32_t v = lane; v < m; v += 32) {
-      const B128 i = ins[v];
-      max_in = max(max_in, b_pop(i));
-      st_b128(out.adjin + 2 * (uint64_t(start) + v), i);
-      const uint8_t l = s.lab[v];
-      B128 eq{0, 0};
-      if (l < 16) {
-        eq = s.labmask[l];
-      } else {
-        for (uint32_t y = 0; y < m; ++y)
-          if (s.lab[y] == l) eq = b_or(eq, b_bit(y));
-      }
-      s.scratch[1][v] = eq;
-    }
+    max_in = asym_sets(s, out, start, m, lane);
     bad |= kErrAsym;
   }
   max_in = __reduce_max_sync(0xffffffffu, max_in);

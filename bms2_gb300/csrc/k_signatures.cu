@@ -57,6 +57,63 @@ struct Rows {
   }
 };
 
+// 64-bit node sets for graphs of at most 64 nodes (96% of molecules): the B128
+// operations on one word, for the walks and the cycle enumeration, whose
+// integer set arithmetic bounds the kernel
+__device__ __forceinline__ uint64_t b_and(uint64_t a, uint64_t b) { return a & b; }
+__device__ __forceinline__ uint64_t b_or(uint64_t a, uint64_t b) { return a | b; }
+__device__ __forceinline__ uint64_t b_andn(uint64_t a, uint64_t b) { return a & ~b; }
+__device__ __forceinline__ bool b_any(uint64_t a) { return a != 0; }
+__device__ __forceinline__ uint32_t b_pop(uint64_t a) { return uint32_t(__popcll(a)); }
+__device__ __forceinline__ uint32_t b_low(uint64_t a) { return uint32_t(__ffsll((long long)a) - 1); }
+__device__ __forceinline__ uint64_t b_clear_low(uint64_t a) { return a & (a - 1); }
+template <class Set> __device__ __forceinline__ Set set_bit(uint32_t i);
+template <> __device__ __forceinline__ uint64_t set_bit<uint64_t>(uint32_t i) { return uint64_t(1) << i; }
+template <> __device__ __forceinline__ B128 set_bit<B128>(uint32_t i) { return b_bit(i); }
+template <class Set> __device__ __forceinline__ Set set_of(const B128& b);
+template <> __device__ __forceinline__ uint64_t set_of<uint64_t>(const B128& b) { return b.lo; }
+template <> __device__ __forceinline__ B128 set_of<B128>(const B128& b) { return b; }
+
+// path signature of node v: walks v-a-w (w != v) and v-a-w-x (x != a, x != v),
+// as one flat loop with one Bloom insert per iteration, so lanes whose nodes
+// have different neighbourhoods still hash in step (inserts commute).  The
+// filter's bits accumulate in the lane's own shared words (one OR per
+// position, PathSignatureDevice::insert, signature.hpp:418-430).
+template <class Set>
+__device__ __forceinline__ void path_walks(const WarpSmem& s, uint32_t v, uint32_t lu, uint32_t* bl) {
+  const Set bv = set_bit<Set>(v);
+  Set ra = set_of<Set>(s.adj[v]), rw{}, rx{};
+  uint32_t a = 0, h2 = 0;
+  while (true) {
+    uint32_t h;
+    if (b_any(rx)) {  // next x of the current v-a-w; the hash depends on x's
+      // label only, so every other x of that label is dropped with it
+      const uint32_t lx = s.lab[b_low(rx)];
+      h = hcombine(h2, lx);
+      rx = lx < 16 ? b_andn(rx, set_of<Set>(s.labmask[lx])) : b_clear_low(rx);
+    } else {  // next w, moving on to the next a with a continuation
+      while (!b_any(rw) && b_any(ra)) {
+        a = b_low(ra);
+        ra = b_clear_low(ra);
+        rw = b_andn(set_of<Set>(s.adj[a]), bv);
+      }
+      if (!b_any(rw)) break;
+      const uint32_t w = b_low(rw);
+      rw = b_clear_low(rw);
+      h2 = hcombine(lu, hcombine(s.lab[a], s.lab[w]));
+      h = h2;
+      rx = b_andn(set_of<Set>(s.adj[w]), b_or(set_bit<Set>(a), bv));
+    }
+    uint32_t x = fmix32(h);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      const uint32_t idx = x & 255u;
+      atomicOr(&bl[idx >> 5], 1u << (idx & 31u));
+      x = fmix32(x);
+    }
+  }
+}
+
 // Saturating nibble histogram (signature.hpp:22-53) of the labels < 16 of a
 // node set: per present label, min(15, nodes of the set with that label).
 __device__ __forceinline__ uint64_t label_hist(const WarpSmem& s, uint32_t present, B128 set) {
@@ -160,8 +217,9 @@ __device__ __noinline__ void cycles_entries(const WarpSmem& s, const Rows& r, ui
 // all its nodes carry one label (the per-node rule: every node after v on the
 // path has v's label).  Counters in scratch[1]; lanes take (s0, first edge)
 // items, whose offsets sit in scratch[0].
-__device__ void cycles_canonical(WarpSmem& s, uint32_t m, uint32_t lane) {
-  const B128 all = b_lowmask(m);
+template <class Set>
+__device__ __forceinline__ void cycles_canonical_t(WarpSmem& s, uint32_t m, uint32_t lane) {
+  const Set all = set_of<Set>(b_lowmask(m));
   CycRow* cyc = cyc_counts(s);
   uint16_t* first = item_first(s);
   // work items: (s0, a) with a an upper neighbour of s0, spread over the lanes
@@ -172,7 +230,7 @@ __device__ void cycles_canonical(WarpSmem& s, uint32_t m, uint32_t lane) {
     uint32_t n = 0;
     if (v < m) {
       for (int t = 0; t < 4; ++t) cyc[v][t] = 0;
-      n = b_pop(b_and(s.adj[v], b_andn(all, b_lowmask(v + 1))));
+      n = b_pop(b_and(set_of<Set>(s.adj[v]), b_andn(all, set_of<Set>(b_lowmask(v + 1)))));
     }
     uint32_t incl = n;
     for (int d = 1; d < 32; d <<= 1) {
@@ -193,38 +251,38 @@ __device__ void cycles_canonical(WarpSmem& s, uint32_t m, uint32_t lane) {
       else hi = mid;
     }
     const uint32_t s0 = lo;
-    const B128 gt = b_andn(all, b_lowmask(s0 + 1));
-    B128 up = b_and(s.adj[s0], gt);
+    const Set gt = b_andn(all, set_of<Set>(b_lowmask(s0 + 1)));
+    Set up = b_and(set_of<Set>(s.adj[s0]), gt);
     for (uint32_t r = k - first[s0]; r > 0; --r) up = b_clear_low(up);
     const uint32_t a = b_low(up);
     const uint32_t l0 = s.lab[s0];
-    const B128 ns = s.adj[s0];
+    const Set ns = set_of<Set>(s.adj[s0]);
     const bool s1 = s.lab[a] == l0;
-    const B128 v1 = b_bit(a);
+    const Set v1 = set_bit<Set>(a);
     // the cycle's last node is a neighbour of s0 above a (orientation)
-    const B128 last = b_and(ns, b_andn(gt, b_lowmask(a + 1)));
+    const Set last = b_and(ns, b_andn(gt, set_of<Set>(b_lowmask(a + 1))));
     if (!b_any(last)) continue;
     // only paths that can still close are walked: the 4th node closes a
     // 5-cycle (it is in last) or precedes the last node of a 6-cycle (it is
     // next to last), and the 3rd node is next to such a 4th node
-    B128 q4 = last;
-    for (B128 r = last; b_any(r); r = b_clear_low(r)) q4 = b_or(q4, s.adj[b_low(r)]);
+    Set q4 = last;
+    for (Set r = last; b_any(r); r = b_clear_low(r)) q4 = b_or(q4, set_of<Set>(s.adj[b_low(r)]));
     q4 = b_and(q4, gt);
-    B128 q3{0, 0};
-    for (B128 r = q4; b_any(r); r = b_clear_low(r)) q3 = b_or(q3, s.adj[b_low(r)]);
+    Set q3{};
+    for (Set r = q4; b_any(r); r = b_clear_low(r)) q3 = b_or(q3, set_of<Set>(s.adj[b_low(r)]));
     q3 = b_and(q3, gt);
-    for (B128 r2 = b_andn(b_and(s.adj[a], gt), v1); b_any(r2); r2 = b_clear_low(r2)) {
+    for (Set r2 = b_andn(b_and(set_of<Set>(s.adj[a]), gt), v1); b_any(r2); r2 = b_clear_low(r2)) {
       const uint32_t b = b_low(r2);
       const bool s2 = s1 && s.lab[b] == l0;
-      const B128 v2 = b_or(v1, b_bit(b));
-      for (B128 r3 = b_andn(b_and(s.adj[b], q3), v2); b_any(r3); r3 = b_clear_low(r3)) {
+      const Set v2 = b_or(v1, set_bit<Set>(b));
+      for (Set r3 = b_andn(b_and(set_of<Set>(s.adj[b]), q3), v2); b_any(r3); r3 = b_clear_low(r3)) {
         const uint32_t c = b_low(r3);
         const bool s3 = s2 && s.lab[c] == l0;
-        const B128 v3 = b_or(v2, b_bit(c));
-        for (B128 r4 = b_andn(b_and(s.adj[c], q4), v3); b_any(r4); r4 = b_clear_low(r4)) {
+        const Set v3 = b_or(v2, set_bit<Set>(c));
+        for (Set r4 = b_andn(b_and(set_of<Set>(s.adj[c]), q4), v3); b_any(r4); r4 = b_clear_low(r4)) {
           const uint32_t d = b_low(r4);
           const bool s4 = s3 && s.lab[d] == l0;
-          if (b_has(last, d)) {
+          if (b_any(b_and(last, set_bit<Set>(d)))) {
             const int t = s4 ? 0 : 1;
             atomicAdd(&cyc[s0][t], 2u);
             atomicAdd(&cyc[a][t], 2u);
@@ -232,8 +290,8 @@ __device__ void cycles_canonical(WarpSmem& s, uint32_t m, uint32_t lane) {
             atomicAdd(&cyc[c][t], 2u);
             atomicAdd(&cyc[d][t], 2u);
           }
-          const B128 v4 = b_or(v3, b_bit(d));
-          for (B128 r5 = b_andn(b_and(s.adj[d], last), v4); b_any(r5); r5 = b_clear_low(r5)) {
+          const Set v4 = b_or(v3, set_bit<Set>(d));
+          for (Set r5 = b_andn(b_and(set_of<Set>(s.adj[d]), last), v4); b_any(r5); r5 = b_clear_low(r5)) {
             const uint32_t e = b_low(r5);
             const int t = (s4 && s.lab[e] == l0) ? 2 : 3;
             atomicAdd(&cyc[s0][t], 2u);
@@ -248,6 +306,12 @@ __device__ void cycles_canonical(WarpSmem& s, uint32_t m, uint32_t lane) {
     }
   }
   __syncwarp();
+}
+
+// The enumeration on one-word sets when the graph has at most 64 nodes.
+__device__ void cycles_canonical(WarpSmem& s, uint32_t m, uint32_t lane) {
+  if (m <= 64) cycles_canonical_t<uint64_t>(s, m, lane);
+  else cycles_canonical_t<B128>(s, m, lane);
 }
 
 // Cycle closures through v on adjacency sets (graphs without repeated entries).
@@ -416,47 +480,12 @@ __device__ __forceinline__ void signatures_graph(const DGraphs& g, const DSigs& 
     } else {  // every entry distinct: the row as a set
       lg = label_hist(s, present, s.adj[v]);
     }
-    // path signature: walks v-a-w (w != v) and v-a-w-x (x != a, x != v), as
-    // one flat loop with one Bloom insert per iteration, so lanes whose nodes
-    // have different neighbourhoods still hash in step (inserts commute)
-    // the filter's bits accumulate in the lane's own shared words (one OR per
-    // position, PathSignatureDevice::insert, signature.hpp:418-430)
+    // path signature (path_walks), into the lane's own 256-bit filter
     uint32_t* bl = lane_bloom(s, lane);
     reinterpret_cast<uint4*>(bl)[0] = make_uint4(0, 0, 0, 0);
     reinterpret_cast<uint4*>(bl)[1] = make_uint4(0, 0, 0, 0);
-    {
-      const B128 bv = b_bit(v);
-      B128 ra = s.adj[v], rw{0, 0}, rx{0, 0};
-      uint32_t a = 0, h2 = 0;
-      while (true) {
-        uint32_t h;
-        if (b_any(rx)) {  // next x of the current v-a-w; the hash depends on x's
-          // label only, so every other x of that label is dropped with it
-          const uint32_t lx = s.lab[b_low(rx)];
-          h = hcombine(h2, lx);
-          rx = lx < 16 ? b_andn(rx, s.labmask[lx]) : b_clear_low(rx);
-        } else {  // next w, moving on to the next a with a continuation
-          while (!b_any(rw) && b_any(ra)) {
-            a = b_low(ra);
-            ra = b_clear_low(ra);
-            rw = b_andn(s.adj[a], bv);
-          }
-          if (!b_any(rw)) break;
-          const uint32_t w = b_low(rw);
-          rw = b_clear_low(rw);
-          h2 = hcombine(lu, hcombine(s.lab[a], s.lab[w]));
-          h = h2;
-          rx = b_andn(s.adj[w], b_or(b_bit(a), bv));
-        }
-        uint32_t x = fmix32(h);
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-          const uint32_t idx = x & 255u;
-          atomicOr(&bl[idx >> 5], 1u << (idx & 31u));
-          x = fmix32(x);
-        }
-      }
-    }
+    if (m <= 64) path_walks<uint64_t>(s, v, lu, bl);
+    else path_walks<B128>(s, v, lu, bl);
     const uint4 bq0 = reinterpret_cast<const uint4*>(bl)[0], bq1 = reinterpret_cast<const uint4*>(bl)[1];
     const uint64_t p0 = uint64_t(bq0.x) | (uint64_t(bq0.y) << 32), p1 = uint64_t(bq0.z) | (uint64_t(bq0.w) << 32);
     const uint64_t p2 = uint64_t(bq1.x) | (uint64_t(bq1.y) << 32), p3 = uint64_t(bq1.z) | (uint64_t(bq1.w) << 32);

@@ -134,11 +134,12 @@ __device__ __forceinline__ uint64_t label_hist(const WarpSmem& s, uint32_t prese
 // frontiers look like.  The reach sets live in the two scratch arrays; once no
 // set grows, the remaining shells are empty.
 // Writes record words 6..13 (shells 1..8; steps >= R stay zero).
-__device__ void shells_levels(WarpSmem& s, const DSigs& out, uint32_t start, uint32_t m, uint32_t lane,
-                              uint32_t present) {
-  B128* cur = s.scratch[0];
-  B128* nxt = s.scratch[1];
-  for (uint32_t v = lane; v < m; v += 32) cur[v] = b_bit(v);
+template <class Set>
+__device__ __forceinline__ void shells_levels_t(WarpSmem& s, const DSigs& out, uint32_t start, uint32_t m,
+                                                uint32_t lane, uint32_t present) {
+  Set* cur = reinterpret_cast<Set*>(s.scratch[0]);
+  Set* nxt = reinterpret_cast<Set*>(s.scratch[1]);
+  for (uint32_t v = lane; v < m; v += 32) cur[v] = set_bit<Set>(v);
   __syncwarp();
   bool grows = out.R > 0;
   for (int k = 0; k < kMaxSteps; ++k) {
@@ -146,25 +147,35 @@ __device__ void shells_levels(WarpSmem& s, const DSigs& out, uint32_t start, uin
     for (uint32_t v = lane; v < m; v += 32) {
       uint64_t h = 0;
       if (grows && k < out.R) {
-        const B128 prev = cur[v];
-        B128 r = prev;
-        for (B128 a = s.adj[v]; b_any(a); a = b_clear_low(a)) r = b_or(r, cur[b_low(a)]);
+        const Set prev = cur[v];
+        Set r = prev;
+        for (Set a = set_of<Set>(s.adj[v]); b_any(a); a = b_clear_low(a)) r = b_or(r, cur[b_low(a)]);
         nxt[v] = r;
-        const B128 shell = b_andn(r, prev);
+        const Set shell = b_andn(r, prev);
         if (b_any(shell)) {
           grew = true;
-          h = label_hist(s, present, shell);
+          for (uint32_t pl = present; pl; pl &= pl - 1) {
+            const uint32_t l = uint32_t(__ffs(int(pl)) - 1);
+            const uint32_t c = b_pop(b_and(shell, set_of<Set>(s.labmask[l])));
+            h |= uint64_t(c < 15u ? c : 15u) << (4 * l);
+          }
         }
       }
       out.frec[uint64_t(kRecWords) * (uint64_t(start) + v) + 6 + k] = h;
     }
     grows = __any_sync(0xffffffffu, grew);
     __syncwarp();
-    B128* t = cur;
+    Set* t = cur;
     cur = nxt;
     nxt = t;
   }
   __syncwarp();
+}
+
+__device__ void shells_levels(WarpSmem& s, const DSigs& out, uint32_t start, uint32_t m, uint32_t lane,
+                              uint32_t present) {
+  if (m <= 64) shells_levels_t<uint64_t>(s, out, start, m, lane, present);
+  else shells_levels_t<B128>(s, out, start, m, lane, present);
 }
 
 __device__ __noinline__ uint32_t mult(const Rows& r, uint32_t a, uint32_t target) {

@@ -508,9 +508,12 @@ __global__ void __launch_bounds__(256) sliced_filter_kernel(SlicedArgs a) {
         const bool join = entry_join(e);
         const uint32_t row0 = s_as[Q + i];
         bool alive = true;
+        const uint2* qdesc = a.desc + uint64_t(qg) * kMaxQueryNodes;
+        uint2 dnext = n > 1 ? __ldg(qdesc + 1) : make_uint2(0, 0);
         for (uint32_t level = 1; level < n && alive; ++level) {
           Mask<W> row = all;
-          const uint2 dsc = __ldg(a.desc + uint64_t(qg) * kMaxQueryNodes + level);
+          const uint2 dsc = dnext;
+          if (level + 1 < n) dnext = __ldg(qdesc + level + 1);  // next level's descriptor in flight
           alive = eval_node<W>(a, g, qg, dsc, join ? row0 : kNoRow, row);
           if (alive && join && row0 != kNoRow) st_b128(a.arena + 2 * (uint64_t(row0) + desc_vertex(dsc)), to128(row));
         }

@@ -337,16 +337,30 @@ __global__ void __launch_bounds__(256) sliced_filter_kernel(SlicedArgs a) {
     if (a.class_begin + s_graph >= a.class_end) break;
     const uint32_t dg = a.dperm[a.class_begin + s_graph];
     const uint32_t start = a.d.goff[dg], m = a.d.goff[dg + 1] - start;
-    // stage node attributes
-    for (uint32_t v = tid; v < m; v += blockDim.x) {
-      const uint64_t* rec = a.ds.frec + uint64_t(kRecWords) * (uint64_t(start) + v);
-      const uint64_t w0 = rec[0];
-      s_lab[v] = uint8_t(w0 & 0xFFu);
-      const uint32_t dgv = uint32_t(w0 >> 32);
-      s_deg[v] = uint8_t(dgv > 255u ? 255u : dgv);
-      s_cyc[v] = rec[1];
-      for (int w = 0; w < 4; ++w) s_path[4 * v + w] = rec[2 + w];
-      for (int k = 0; k < R; ++k) s_sh[uint32_t(R) * v + k] = rec[6 + k];
+    // stage node attributes: the graph's records are contiguous, so the block
+    // reads them as 16-byte pieces in order (piece q of node v holds record
+    // words 2q and 2q + 1) and scatters the words it needs
+    {
+      const uint32_t pieces = 3u + uint32_t(R + 1) / 2u;  // label/degree/cycle, path, shells 1..R
+      const ulonglong2* rec2 = reinterpret_cast<const ulonglong2*>(a.ds.frec + uint64_t(kRecWords) * start);
+      for (uint32_t idx = tid; idx < m * 8u; idx += blockDim.x) {
+        const uint32_t v = idx >> 3, q = idx & 7u;
+        if (q >= pieces) continue;
+        const ulonglong2 x = rec2[idx];
+        if (q == 0) {
+          s_lab[v] = uint8_t(x.x & 0xFFu);
+          const uint32_t dgv = uint32_t(x.x >> 32);
+          s_deg[v] = uint8_t(dgv > 255u ? 255u : dgv);
+          s_cyc[v] = x.y;
+        } else if (q < 3) {
+          s_path[4 * v + 2 * (q - 1)] = x.x;
+          s_path[4 * v + 2 * (q - 1) + 1] = x.y;
+        } else {
+          const uint32_t k = 2 * (q - 3);
+          s_sh[uint32_t(R) * v + k] = x.x;
+          if (k + 1 < uint32_t(R)) s_sh[uint32_t(R) * v + k + 1] = x.y;
+        }
+      }
     }
     for (uint32_t w = tid; w < a.QW; w += blockDim.x) s_valid[w] = 0;
     if (tid < 2) s_count[tid] = 0;

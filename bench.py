@@ -49,7 +49,7 @@ HBM_FALLBACK_GBS = 6800.0
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of the three fused
 # filter launches per data graph, from one ncu capture of 100,000 graphs of the
 # workload (traffic grows with the graphs processed).
-FILTER_DRAM_BYTES_PER_GRAPH = {"mol1m": 1.4468e9 / 100_000}
+FILTER_DRAM_BYTES_PER_GRAPH = {"mol1m": 1.4082e9 / 100_000}
 
 
 def peaks() -> tuple[float, str]:

@@ -43,8 +43,8 @@ typedef uint32_t CycRow[4];
 __device__ __forceinline__ CycRow* cyc_counts(WarpSmem& s) { return reinterpret_cast<CycRow*>(s.scratch[1]); }
 
 // CSR row access of the current graph with local ids, from global memory (the
-// paths for rows with repeated entries; out-of-graph columns, already flagged
-// as an error of the batch, read node 0).
+// degrees, and the paths for rows with repeated entries; out-of-graph columns,
+// already flagged as an error of the batch, read node 0).
 struct Rows {
   const uint32_t* rowp;
   const uint32_t* col;

@@ -114,6 +114,12 @@ __device__ __forceinline__ void path_walks(const WarpSmem& s, uint32_t v, uint32
   }
 }
 
+// The two-word instance out of line: it keeps the hot loop of the one-word
+// instance (graphs of at most 64 nodes) compact in the instruction cache.
+__device__ __noinline__ void path_walks_wide(const WarpSmem& s, uint32_t v, uint32_t lu, uint32_t* bl) {
+  path_walks<B128>(s, v, lu, bl);
+}
+
 // Saturating nibble histogram (signature.hpp:22-53) of the labels < 16 of a
 // node set: per present label, min(15, nodes of the set with that label).
 __device__ __forceinline__ uint64_t label_hist(const WarpSmem& s, uint32_t present, B128 set) {
@@ -496,7 +502,7 @@ __device__ __forceinline__ void signatures_graph(const DGraphs& g, const DSigs& 
     reinterpret_cast<uint4*>(bl)[0] = make_uint4(0, 0, 0, 0);
     reinterpret_cast<uint4*>(bl)[1] = make_uint4(0, 0, 0, 0);
     if (m <= 64) path_walks<uint64_t>(s, v, lu, bl);
-    else path_walks<B128>(s, v, lu, bl);
+    else path_walks_wide(s, v, lu, bl);
     const uint4 bq0 = reinterpret_cast<const uint4*>(bl)[0], bq1 = reinterpret_cast<const uint4*>(bl)[1];
     const uint64_t p0 = uint64_t(bq0.x) | (uint64_t(bq0.y) << 32), p1 = uint64_t(bq0.z) | (uint64_t(bq0.w) << 32);
     const uint64_t p2 = uint64_t(bq1.x) | (uint64_t(bq1.y) << 32), p3 = uint64_t(bq1.z) | (uint64_t(bq1.w) << 32);
